@@ -1,0 +1,152 @@
+/*
+ * warp_gb300.h -- C ABI of libwarp_gb300.so, the sm_103a (GB300) implementation of Warp's
+ * finite-element linear-solve path.
+ *
+ * Conventions
+ *   - All array arguments are DEVICE pointers unless named *_host.  Sizes are element counts.
+ *   - Every call is stream-ordered on `stream` (a cudaStream_t; 0 = legacy default stream) and
+ *     never synchronises the host, except where a host output is documented.
+ *   - Return value: 0 on success, a negative GbStatus on failure; gb_last_error() returns the
+ *     message (per host thread).  No exception crosses the ABI.
+ *   - The library allocates no device memory: callers pass workspaces sized by the matching
+ *     *_workspace_bytes() query (the Krylov handle owns only its CUDA graphs).
+ *   - Kernels report device-side conditions by OR-ing GB_DEV_* bits into a caller-provided int32
+ *     status word; waits inside kernels are bounded.
+ * Reference citations are paths inside the Warp source tree.
+ */
+#ifndef WARP_GB300_H
+#define WARP_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* gb_stream_t; /* == cudaStream_t */
+
+enum { GB_OK = 0, GB_ERR_INVALID = -1, GB_ERR_CUDA = -2, GB_ERR_UNSUPPORTED = -3, GB_ERR_CAPACITY = -4 };
+enum { GB_F32 = 0, GB_F64 = 1, GB_BF16 = 2, GB_F16 = 3 };
+enum { GB_DEV_WAIT_TIMEOUT = 1, GB_DEV_BREAKDOWN = 2, GB_DEV_NONFINITE = 4, GB_DEV_STAGNATION = 8 };
+enum { GB_KRYLOV_CG = 0, GB_KRYLOV_BICGSTAB = 1 };
+
+/* ---- library ------------------------------------------------------------------------------ */
+const char* gb_last_error(void);
+void gb_clear_error(void);
+int gb_version(void);
+int gb_device_arch(void);
+
+/* ---- prefix sums ---------------------------------------------------------------------------
+ * Replaces wp_array_scan_int_device (warp/native/warp.h:449; warp/native/scan.cu). */
+size_t gb_scan_i32_workspace_bytes(int64_t n);
+int gb_scan_i32(const int* in, int* out, int64_t n, int inclusive, void* workspace, size_t workspace_bytes,
+                gb_stream_t stream);
+
+/* ---- triplets -> BSR -------------------------------------------------------------------------
+ * gb_bsr_matrix_from_triplets_device replaces wp_bsr_matrix_from_triplets_device
+ * (warp/native/warp.h:583-602; warp/native/sparse.cu:1168-1325): same arguments and semantics
+ * (invalid indices and, when scalar_zero_mask != 0, all-zero blocks are pruned; masked_topology
+ * keeps only blocks present in bsr_offsets/bsr_columns; tpl_block_offsets = inclusive run ends,
+ * tpl_block_indices = triplet ids in stable sorted order; bsr_nnz_host receives offsets[nrow]
+ * asynchronously and bsr_nnz_event (a cudaEvent_t, optional) is recorded after that copy), plus
+ * a caller workspace and the stream.
+ * gb_bsr_accumulate_triplet_values replaces the _bsr_accumulate_triplet_values launch
+ * (warp/_src/sparse.py:1073-1090, 1503-1515). */
+size_t gb_bsr_from_triplets_workspace_bytes(int nnz, int nrow, int ncol);
+int gb_bsr_matrix_from_triplets_device(int block_size, int scalar_size, int row_count, int col_count, int nnz,
+                                       const int* tpl_nnz, const int* tpl_rows, const int* tpl_columns,
+                                       const void* tpl_values, uint64_t scalar_zero_mask, int masked_topology,
+                                       int* tpl_block_offsets, int* tpl_block_indices, int* bsr_offsets,
+                                       const int* bsr_row_counts, int* bsr_columns, int* bsr_nnz_host,
+                                       void* bsr_nnz_event, void* workspace, size_t workspace_bytes,
+                                       gb_stream_t stream);
+int gb_bsr_accumulate_triplet_values(int dtype, int block_size, int row_count, const int* bsr_offsets,
+                                     const int* tpl_block_offsets, const int* tpl_block_indices,
+                                     const void* tpl_values, void* bsr_values, int nnz_upper, gb_stream_t stream);
+
+/* ---- SpMV --------------------------------------------------------------------------------------
+ * Replaces bsr_mv (warp/_src/sparse.py:4792-4913; kernels bsr_mv_kernel :4627-4665,
+ * bsr_mv_tiled_kernel :4668-4715, bsr_mv_transpose_kernel :4718-4747).
+ * y_out = alpha * op(A) x + beta * y_in; y_in may equal y_out; x must not alias y_out.
+ * val_dtype GB_F32 / GB_F64 / GB_BF16; vec_dtype GB_F32 / GB_F64; ncap = entries available in
+ * columns/values.  rows_per_cta / lanes_per_row / cap_blocks <= 0 (cap_blocks < 0) select the
+ * built-in tile heuristic. */
+int gb_bsr_mv(int block_rows, int block_cols, int nrow, int ncol, int64_t nnz_upper, int64_t ncap, const int* offsets,
+              const int* row_counts, const int* columns, const void* values, int val_dtype, const void* x,
+              const void* y_in, void* y_out, int vec_dtype, double alpha, double beta, int transpose,
+              int rows_per_cta, int lanes_per_row, int cap_blocks, int* status, gb_stream_t stream);
+int gb_bsr_mv_default_shape(int block_rows, int block_cols, int val_dtype, int nrow, int64_t nnz, int* rows_per_cta,
+                            int* lanes_per_row, int* cap_blocks);
+
+/* ---- diagonal, small operators, reductions -----------------------------------------------------
+ * gb_bsr_get_diag: bsr_get_diag (warp/_src/sparse.py:2871-2887).
+ * gb_bsr_inverse_diagonal: preconditioner(A, "diag"/"diag_abs") (warp/_src/optim/linear.py:236-329).
+ * gb_diag_mv / gb_dense_mv: aslinearoperator diag_mv / dense_mv (warp/_src/optim/linear.py:135-233,
+ *   kernels :2250-2287).
+ * gb_dots: TiledDot.compute (warp/_src/optim/linear.py:309-576), fp64 accumulation, deterministic.
+ * gb_axpby: array_axpy (warp/_src/utils.py). */
+int gb_bsr_get_diag(int dtype, int br, int bc, int nrow, const int* offsets, const int* row_counts,
+                    const int* columns, const void* values, void* out, gb_stream_t stream);
+int gb_bsr_inverse_diagonal(int dtype, int bdim, int nrow, const int* offsets, const int* row_counts,
+                            const int* columns, const void* values, int use_abs, void* inv, gb_stream_t stream);
+int gb_diag_mv(int dtype, int64_t n, const void* A, const void* x, const void* y, void* z, double alpha, double beta,
+               gb_stream_t stream);
+int gb_dense_mv(int dtype, int m, int n, const void* A, const void* x, const void* y, void* z, double alpha,
+                double beta, gb_stream_t stream);
+size_t gb_dots_workspace_bytes(void);
+int gb_dots(int dtype, int64_t n, int ncols, const void* const* xs, const void* const* ys, double* out,
+            void* workspace, gb_stream_t stream);
+int gb_axpby(int dtype, int64_t n, double alpha, const void* x, double beta, const void* y, void* out,
+             gb_stream_t stream);
+
+/* ---- fused Krylov solvers (CG / BiCGSTAB with Jacobi or no preconditioner) ----------------------
+ * Replace CG._run (warp/_src/optim/linear.py:934-1032), BiCGSTAB._run (:1466-1574), their update
+ * kernels (:2332-2373, :2426-2493), TiledDot and the capturable loop (_run_capturable_loop /
+ * _update_condition / capture_while, :2086-2179; warp/native/warp.h:777).
+ * gb_krylov_launch modes: 0 whole solve (init + device-side while loop, one graph), 1 init,
+ * 2 `chunk_iters` iterations, 3 one eager iteration, 4 eager init.  Inside a caller's stream
+ * capture, mode 0 appends the conditional loop to that capture. */
+size_t gb_krylov_workspace_bytes(int kind, int block_dim, int nrow, int64_t nnz, int val_dtype);
+int gb_krylov_create(int kind, int block_dim, int nrow, int64_t nnz, int64_t ncap, int val_dtype, int rows_per_cta,
+                     int lanes_per_row, int cap_blocks, void* workspace, size_t workspace_bytes, void** handle_out);
+int gb_krylov_destroy(void* handle);
+int gb_krylov_set_operands(void* handle, const int* offsets, const int* row_counts, const int* columns,
+                           const void* values, const float* dinv, const float* b, float* x, int x_is_zero, double tol,
+                           double atol, int maxiter, int left_precond, gb_stream_t stream);
+int gb_krylov_launch(void* handle, int what, int chunk_iters, gb_stream_t stream);
+int gb_krylov_scalars(void* handle, int** iter, double** rr, double** atol_sq, int** status);
+int gb_krylov_read(void* handle, int* host_ints3, double* host_doubles3, gb_stream_t stream);
+int gb_krylov_vectors(void* handle, float** r, float** p, float** Ap);
+
+/* ---- FP64 refinement pieces (no reference counterpart: the reference solves in the matrix
+ * scalar type only; these wrap the fp32 solver of CG._run in iterative refinement) ------------- */
+size_t gb_residual_f64_workspace_bytes(int block_dim, int nrow, int64_t nnz, int val_dtype);
+int gb_residual_f64(int block_dim, int nrow, int64_t nnz, int64_t ncap, const int* offsets, const int* row_counts,
+                    const int* columns, const void* values, int val_dtype, const double* x, const float* b,
+                    double* r64, float* r32, double* norms, void* workspace, size_t workspace_bytes, int* status,
+                    gb_stream_t stream);
+int gb_axpy_f64_f32(int64_t n, double* x, const float* d, double alpha, gb_stream_t stream);
+
+/* ---- Q1 FEM assembly on regular grids ------------------------------------------------------------
+ * gb_q1_assemble_triplets replaces fem.integrate's bilinear dispatch path for Q1 Grid2D/Grid3D
+ * spaces (warp/_src/fem/integrate.py:1627-1878; warp/_src/fem/field/virtual.py:884-1116), writing
+ * triplets in the reference's order.  gb_q1_assemble_rhs: the linear form sum_e M_e f
+ * (integrate.py:1404-1625).  gb_grid_boundary_mask + gb_dirichlet_project: the nodal boundary
+ * projector and project_linear_system (warp/_src/fem/dirichlet.py:69-124). */
+int64_t gb_q1_triplet_count(int dim, int nx, int ny, int nz);
+int gb_q1_assemble_triplets(int dim, int nx, int ny, int nz, int ncomp, const double* K0, const double* K1,
+                            const float* coef0, float coef0_const, const float* coef1, float coef1_const, int* rows,
+                            int* cols, float* vals, gb_stream_t stream);
+int gb_q1_assemble_rhs(int dim, int nx, int ny, int nz, int ncomp, const double* M, const float* f, float f0, float f1,
+                       float f2, float* out, gb_stream_t stream);
+int gb_grid_boundary_mask(int dim, int nx, int ny, int nz, int face_bits, int ncomp, int comp_mask, float* mask,
+                          gb_stream_t stream);
+int gb_dirichlet_project(int bdim, int nrow, const int* offsets, const int* columns, float* values, const float* mask,
+                         float* rhs, const float* fixed, float* tmp, int project_matrix, gb_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* WARP_GB300_H */

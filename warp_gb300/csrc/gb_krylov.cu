@@ -1,0 +1,921 @@
+// gb_krylov.cu -- fused Jacobi-preconditioned CG and BiCGSTAB for BSR systems, captured as CUDA
+// graphs with a device-side conditional while loop, plus the FP64 iterative-refinement helpers.
+//
+// Replaces, for BSR operators with the Jacobi ("diag") preconditioner or none:
+//   CG._run          warp/_src/optim/linear.py:934-1032  (kernels _cg_kernel_1/2 :2332-2373)
+//   BiCGSTAB._run    warp/_src/optim/linear.py:1466-1574 (kernels _bicgstab_kernel_1/2/3 :2426-2493)
+//   TiledDot         warp/_src/optim/linear.py:309-576   (multi-level tree reductions)
+//   _run_capturable_loop / _update_condition / capture_while  linear.py:2086-2179
+// Per CG iteration the reference launches SpMV + ~5 vector kernels + 2 multi-level dot trees.
+// Here one iteration is three kernels: (1) SpMV Ap = A p fused with p.Ap, (2) x/r update fused
+// with z = D^-1 r and the r.r / r.z reductions, (3) p = z + beta p.  Each reduction is a single
+// pass: CTAs publish partials and the last CTA to finish sums them in a fixed order (so results
+// are deterministic) and computes the next scalar (alpha, beta, the loop condition).  Nothing
+// spins: there is no inter-CTA waiting anywhere in the solve.
+//
+// Solver scalars live in device memory; the loop condition is evaluated on the device and drives
+// a cudaGraphCondTypeWhile node, so a whole solve is one graph launch with no host round trip.
+// Kernels read the operand pointers through a small device-side argument block so one captured
+// graph serves every right-hand side / solution vector / matrix with the same shape.
+#include "gb_common.cuh"
+#include "gb_spmv.cuh"
+
+#include <new>
+
+namespace gb {
+
+enum KrylovKind : int { KRYLOV_CG = 0, KRYLOV_BICGSTAB = 1 };
+
+struct KrylovScalars {
+    double bb, atol_sq, rr, rz, pAp, alpha, beta;
+    double rho, r0v, st, tt, omega, beta_omega;
+    int iter, cond, maxiter, status;
+    unsigned int counters[8];
+};
+
+struct SolveArgs {
+    const int* offsets;
+    const int* row_counts;
+    const int* columns;
+    const void* values;
+    const float* dinv;  // inverse diagonal (scalar per dof) or null for no preconditioner
+    const float* b;
+    float* x;
+    // work vectors
+    float *r, *p, *Ap, *z, *r0, *v, *t, *y;
+    double* partials;
+    KrylovScalars* S;
+    double tol, atol;
+    int maxiter;
+    int x_is_zero;
+    int left_precond;
+    int64_t n;  // scalar dofs
+};
+
+constexpr int VEC_THREADS = 256;
+
+__device__ __forceinline__ void set_cond(KrylovScalars* S, int cond, cudaGraphConditionalHandle h, int has_cond)
+{
+    S->cond = cond;
+    if (has_cond) cudaGraphSetConditional(h, cond ? 1u : 0u);
+}
+
+__device__ __forceinline__ bool finite(double v) { return isfinite(v); }
+
+// ---------------------------------------------------------------------------------------------
+// CG
+// ---------------------------------------------------------------------------------------------
+template <int BR, typename AT> struct EpiCgInit {
+    const float *b, *dinv;
+    float *r, *p;
+    AT sign;  // r = b - A x  (sign = -1) or r = b when x is zero (sign = 0)
+    double bb = 0, rr = 0, rz = 0;
+    __device__ __forceinline__ void operator()(int row, const AT (&acc)[BR], int lane_g)
+    {
+        if (lane_g < BR) {
+            const size_t i = (size_t)row * BR + lane_g;
+            const float bi = b[i];
+            const float ri = bi + sign * pick<BR>(acc, lane_g);
+            const float zi = dinv ? dinv[i] * ri : ri;
+            r[i] = ri;
+            p[i] = zi;
+            bb += (double)bi * bi;
+            rr += (double)ri * ri;
+            rz += (double)ri * zi;
+        }
+    }
+};
+
+__device__ __forceinline__ void cg_init_finish(const SolveArgs& a, const double (&t)[3],
+                                               cudaGraphConditionalHandle h, int has_cond)
+{
+    KrylovScalars* S = a.S;
+    const double bnorm = sqrt(t[0]);
+    const double at = fmax(a.tol * bnorm, a.atol);
+    S->bb = t[0];
+    S->atol_sq = at * at;
+    S->rr = t[1];
+    S->rz = t[2];
+    S->iter = 0;
+    S->maxiter = a.maxiter;
+    S->alpha = S->beta = 0.0;
+    int cond = (t[1] > S->atol_sq) && (a.maxiter > 0);
+    if (!finite(t[1])) {
+        S->status |= GB_DEV_NONFINITE;
+        cond = 0;
+    }
+    set_cond(S, cond, h, has_cond);
+}
+
+template <int BR, typename VT>
+__global__ __launch_bounds__(SPMV_THREADS) void k_cg_init(const SolveArgs* __restrict__ args, int nrow, SpmvShape sh,
+                                                          cudaGraphConditionalHandle h, int has_cond)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double s_red[32 * 3];
+    const SolveArgs a = *args;
+    EpiCgInit<BR, float> epi{a.b, a.dinv, a.r, a.p, -1.0f};
+    if (a.x_is_zero) {
+        // r = b: no product needed; same epilogue with a zero accumulator.
+        const int r0 = blockIdx.x * sh.rows, nr = min(sh.rows, nrow - r0);
+        const int lane_g = threadIdx.x & (sh.G - 1);
+        for (int k = threadIdx.x / sh.G; k < nr; k += blockDim.x / sh.G) {
+            float acc[BR];
+#pragma unroll
+            for (int q = 0; q < BR; ++q) acc[q] = 0.f;
+            epi(r0 + k, acc, lane_g);
+        }
+    } else {
+        spmv_tile<BR, BR, VT, float, float>(nrow, sh, a.offsets, a.row_counts, a.columns, (const VT*)a.values, a.x,
+                                            smem, &a.S->status, epi);
+    }
+    double v[3] = {epi.bb, epi.rr, epi.rz};
+    grid_reduce<3>(v, a.partials, &a.S->counters[0], s_red,
+                   [&](const double (&t)[3]) { cg_init_finish(a, t, h, has_cond); });
+}
+
+template <int BR, typename AT> struct EpiCgAp {
+    float* Ap;
+    const float* p;
+    double pAp = 0;
+    __device__ __forceinline__ void operator()(int row, const AT (&acc)[BR], int lane_g)
+    {
+        if (lane_g < BR) {
+            const size_t i = (size_t)row * BR + lane_g;
+            const float ap = pick<BR>(acc, lane_g);
+            Ap[i] = ap;
+            pAp += (double)p[i] * ap;
+        }
+    }
+};
+
+template <int BR, typename VT>
+__global__ __launch_bounds__(SPMV_THREADS) void k_cg_spmv(const SolveArgs* __restrict__ args, int nrow, SpmvShape sh)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double s_red[32];
+    const SolveArgs a = *args;
+    KrylovScalars* S = a.S;
+    if (!S->cond) return;
+    EpiCgAp<BR, float> epi{a.Ap, a.p};
+    spmv_tile<BR, BR, VT, float, float>(nrow, sh, a.offsets, a.row_counts, a.columns, (const VT*)a.values, a.p, smem,
+                                        &S->status, epi);
+    double v[1] = {epi.pAp};
+    grid_reduce<1>(v, a.partials, &S->counters[1], s_red, [&](const double (&t)[1]) {
+        S->pAp = t[0];
+        double alpha = 0.0;
+        if (S->rr > S->atol_sq) {
+            alpha = S->rz / t[0];
+            if (!finite(alpha)) {
+                S->status |= GB_DEV_BREAKDOWN;
+                alpha = 0.0;
+            }
+        }
+        S->alpha = alpha;
+    });
+}
+
+// x += alpha p; r -= alpha Ap; z = D^-1 r; reductions r.r, r.z; then beta and the loop condition.
+__global__ __launch_bounds__(VEC_THREADS) void k_cg_update(const SolveArgs* __restrict__ args,
+                                                           cudaGraphConditionalHandle h, int has_cond)
+{
+    __shared__ double s_red[32 * 2];
+    const SolveArgs a = *args;
+    KrylovScalars* S = a.S;
+    if (!S->cond) return;
+    const float alpha = (float)S->alpha;
+    const int64_t n = a.n;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double rr = 0.0, rz = 0.0;
+    const bool vec4 = ((((uintptr_t)a.x | (uintptr_t)a.r | (uintptr_t)a.p | (uintptr_t)a.Ap |
+                         (uintptr_t)(a.dinv ? a.dinv : a.r)) & 15) == 0);
+    int64_t done = 0;
+    if (vec4) {
+        const int64_t n4 = n >> 2;
+        float4* x4 = reinterpret_cast<float4*>(a.x);
+        float4* r4 = reinterpret_cast<float4*>(a.r);
+        const float4* p4 = reinterpret_cast<const float4*>(a.p);
+        const float4* ap4 = reinterpret_cast<const float4*>(a.Ap);
+        const float4* d4 = reinterpret_cast<const float4*>(a.dinv);
+        for (int64_t i = tid; i < n4; i += stride) {
+            float4 xv = x4[i], rv = r4[i];
+            const float4 pv = p4[i], av = ap4[i];
+            xv.x += alpha * pv.x; xv.y += alpha * pv.y; xv.z += alpha * pv.z; xv.w += alpha * pv.w;
+            rv.x -= alpha * av.x; rv.y -= alpha * av.y; rv.z -= alpha * av.z; rv.w -= alpha * av.w;
+            float4 zv = rv;
+            if (d4) {
+                const float4 dv = d4[i];
+                zv.x *= dv.x; zv.y *= dv.y; zv.z *= dv.z; zv.w *= dv.w;
+            }
+            x4[i] = xv;
+            r4[i] = rv;
+            rr += (double)rv.x * rv.x + (double)rv.y * rv.y + (double)rv.z * rv.z + (double)rv.w * rv.w;
+            rz += (double)rv.x * zv.x + (double)rv.y * zv.y + (double)rv.z * zv.z + (double)rv.w * zv.w;
+        }
+        done = n4 << 2;
+    }
+    for (int64_t i = done + tid; i < n; i += stride) {
+        const float xi = a.x[i] + alpha * a.p[i];
+        const float ri = a.r[i] - alpha * a.Ap[i];
+        const float zi = a.dinv ? a.dinv[i] * ri : ri;
+        a.x[i] = xi;
+        a.r[i] = ri;
+        rr += (double)ri * ri;
+        rz += (double)ri * zi;
+    }
+    double v[2] = {rr, rz};
+    grid_reduce<2>(v, a.partials, &S->counters[2], s_red, [&](const double (&t)[2]) {
+        const double rz_old = S->rz;
+        S->rr = t[0];
+        S->rz = t[1];
+        double beta = 0.0;
+        if (t[0] > S->atol_sq) {
+            beta = t[1] / rz_old;
+            if (!finite(beta)) {
+                S->status |= GB_DEV_BREAKDOWN;
+                beta = 0.0;
+            }
+        }
+        S->beta = beta;
+        S->iter += 1;
+        int cond = (t[0] > S->atol_sq) && (S->iter < S->maxiter);
+        if (!finite(t[0])) {
+            S->status |= GB_DEV_NONFINITE;
+            cond = 0;
+        }
+        set_cond(S, cond, h, has_cond);
+    });
+}
+
+// p = D^-1 r + beta p
+__global__ __launch_bounds__(VEC_THREADS) void k_cg_pupdate(const SolveArgs* __restrict__ args)
+{
+    const SolveArgs a = *args;
+    KrylovScalars* S = a.S;
+    if (!S->cond) return;
+    const float beta = (float)S->beta;
+    const int64_t n = a.n;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool vec4 = ((((uintptr_t)a.r | (uintptr_t)a.p | (uintptr_t)(a.dinv ? a.dinv : a.r)) & 15) == 0);
+    int64_t done = 0;
+    if (vec4) {
+        const int64_t n4 = n >> 2;
+        const float4* r4 = reinterpret_cast<const float4*>(a.r);
+        float4* p4 = reinterpret_cast<float4*>(a.p);
+        const float4* d4 = reinterpret_cast<const float4*>(a.dinv);
+        for (int64_t i = tid; i < n4; i += stride) {
+            float4 zv = r4[i];
+            if (d4) {
+                const float4 dv = d4[i];
+                zv.x *= dv.x; zv.y *= dv.y; zv.z *= dv.z; zv.w *= dv.w;
+            }
+            float4 pv = p4[i];
+            pv.x = zv.x + beta * pv.x; pv.y = zv.y + beta * pv.y; pv.z = zv.z + beta * pv.z; pv.w = zv.w + beta * pv.w;
+            p4[i] = pv;
+        }
+        done = n4 << 2;
+    }
+    for (int64_t i = done + tid; i < n; i += stride) {
+        const float zi = a.dinv ? a.dinv[i] * a.r[i] : a.r[i];
+        a.p[i] = zi + beta * a.p[i];
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// BiCGSTAB (right preconditioning by default, left with left_precond; M = D^-1 or identity)
+// ---------------------------------------------------------------------------------------------
+template <int BR, typename AT> struct EpiBiInit {
+    const float *b, *dinv;
+    float *r, *r0, *p, *y;
+    AT sign;
+    double bb = 0, rr = 0;
+    __device__ __forceinline__ void operator()(int row, const AT (&acc)[BR], int lane_g)
+    {
+        if (lane_g < BR) {
+            const size_t i = (size_t)row * BR + lane_g;
+            const float bi = b[i];
+            const float ri = bi + sign * pick<BR>(acc, lane_g);
+            r[i] = ri;
+            r0[i] = ri;
+            p[i] = ri;
+            y[i] = dinv ? dinv[i] * ri : ri;
+            bb += (double)bi * bi;
+            rr += (double)ri * ri;
+        }
+    }
+};
+
+template <int BR, typename VT>
+__global__ __launch_bounds__(SPMV_THREADS) void k_bi_init(const SolveArgs* __restrict__ args, int nrow, SpmvShape sh,
+                                                          cudaGraphConditionalHandle h, int has_cond)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double s_red[32 * 2];
+    const SolveArgs a = *args;
+    EpiBiInit<BR, float> epi{a.b, a.dinv, a.r, a.r0, a.p, a.y, -1.0f};
+    if (a.x_is_zero) {
+        const int r0 = blockIdx.x * sh.rows, nr = min(sh.rows, nrow - r0);
+        const int lane_g = threadIdx.x & (sh.G - 1);
+        for (int k = threadIdx.x / sh.G; k < nr; k += blockDim.x / sh.G) {
+            float acc[BR];
+#pragma unroll
+            for (int q = 0; q < BR; ++q) acc[q] = 0.f;
+            epi(r0 + k, acc, lane_g);
+        }
+    } else {
+        spmv_tile<BR, BR, VT, float, float>(nrow, sh, a.offsets, a.row_counts, a.columns, (const VT*)a.values, a.x,
+                                            smem, &a.S->status, epi);
+    }
+    double v[2] = {epi.bb, epi.rr};
+    grid_reduce<2>(v, a.partials, &a.S->counters[0], s_red, [&](const double (&t)[2]) {
+        KrylovScalars* S = a.S;
+        const double at = fmax(a.tol * sqrt(t[0]), a.atol);
+        S->bb = t[0];
+        S->atol_sq = at * at;
+        S->rr = t[1];
+        S->rho = t[1];
+        S->iter = 0;
+        S->maxiter = a.maxiter;
+        int cond = (t[1] > S->atol_sq) && (a.maxiter > 0);
+        if (!finite(t[1])) {
+            S->status |= GB_DEV_NONFINITE;
+            cond = 0;
+        }
+        set_cond(S, cond, h, has_cond);
+    });
+}
+
+// v = A y ; r0.v -> alpha
+template <int BR, typename AT> struct EpiBiV {
+    float* v;
+    const float* r0;
+    double r0v = 0;
+    __device__ __forceinline__ void operator()(int row, const AT (&acc)[BR], int lane_g)
+    {
+        if (lane_g < BR) {
+            const size_t i = (size_t)row * BR + lane_g;
+            const float vi = pick<BR>(acc, lane_g);
+            v[i] = vi;
+            r0v += (double)r0[i] * vi;
+        }
+    }
+};
+
+template <int BR, typename VT>
+__global__ __launch_bounds__(SPMV_THREADS) void k_bi_spmv_v(const SolveArgs* __restrict__ args, int nrow,
+                                                            SpmvShape sh)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double s_red[32];
+    const SolveArgs a = *args;
+    KrylovScalars* S = a.S;
+    if (!S->cond) return;
+    EpiBiV<BR, float> epi{a.v, a.r0};
+    spmv_tile<BR, BR, VT, float, float>(nrow, sh, a.offsets, a.row_counts, a.columns, (const VT*)a.values, a.y, smem,
+                                        &S->status, epi);
+    double v[1] = {epi.r0v};
+    grid_reduce<1>(v, a.partials, &S->counters[1], s_red, [&](const double (&t)[1]) {
+        S->r0v = t[0];
+        double alpha = 0.0;
+        if (S->rr > S->atol_sq) {
+            alpha = S->rho / t[0];
+            if (!finite(alpha)) {
+                S->status |= GB_DEV_BREAKDOWN;
+                alpha = 0.0;
+            }
+        }
+        S->alpha = alpha;
+    });
+}
+
+// x += alpha y; r -= alpha v; z = M r; rr
+__global__ __launch_bounds__(VEC_THREADS) void k_bi_update1(const SolveArgs* __restrict__ args)
+{
+    __shared__ double s_red[32];
+    const SolveArgs a = *args;
+    KrylovScalars* S = a.S;
+    if (!S->cond) return;
+    const float alpha = (float)S->alpha;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    double rr = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+        a.x[i] += alpha * a.y[i];
+        const float ri = a.r[i] - alpha * a.v[i];
+        a.r[i] = ri;
+        a.z[i] = a.dinv ? a.dinv[i] * ri : ri;
+        rr += (double)ri * ri;
+    }
+    double v[1] = {rr};
+    grid_reduce<1>(v, a.partials, &S->counters[2], s_red, [&](const double (&t)[1]) { S->rr = t[0]; });
+}
+
+// t = A z ; st, tt (right: r.t, t.t ; left: z.Mt, Mt.Mt) -> omega
+template <int BR, typename AT> struct EpiBiT {
+    float* t;
+    const float *r, *z, *dinv;
+    int left;
+    double st = 0, tt = 0;
+    __device__ __forceinline__ void operator()(int row, const AT (&acc)[BR], int lane_g)
+    {
+        if (lane_g < BR) {
+            const size_t i = (size_t)row * BR + lane_g;
+            const float ti = pick<BR>(acc, lane_g);
+            t[i] = ti;
+            if (left) {
+                const float mt = dinv ? dinv[i] * ti : ti;
+                st += (double)z[i] * mt;
+                tt += (double)mt * mt;
+            } else {
+                st += (double)r[i] * ti;
+                tt += (double)ti * ti;
+            }
+        }
+    }
+};
+
+template <int BR, typename VT>
+__global__ __launch_bounds__(SPMV_THREADS) void k_bi_spmv_t(const SolveArgs* __restrict__ args, int nrow,
+                                                            SpmvShape sh)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double s_red[32 * 2];
+    const SolveArgs a = *args;
+    KrylovScalars* S = a.S;
+    if (!S->cond) return;
+    EpiBiT<BR, float> epi{a.t, a.r, a.z, a.dinv, a.left_precond};
+    spmv_tile<BR, BR, VT, float, float>(nrow, sh, a.offsets, a.row_counts, a.columns, (const VT*)a.values, a.z, smem,
+                                        &S->status, epi);
+    double v[2] = {epi.st, epi.tt};
+    grid_reduce<2>(v, a.partials, &S->counters[3], s_red, [&](const double (&t)[2]) {
+        S->st = t[0];
+        S->tt = t[1];
+        double omega = 0.0;
+        if (S->rr > S->atol_sq) {
+            omega = t[0] / t[1];
+            if (!finite(omega)) {
+                S->status |= GB_DEV_BREAKDOWN;
+                omega = 0.0;
+            }
+        }
+        S->omega = omega;
+    });
+}
+
+// x += omega z; r -= omega t; rr, rho = r0.r -> beta, beta*omega, condition
+__global__ __launch_bounds__(VEC_THREADS) void k_bi_update2(const SolveArgs* __restrict__ args,
+                                                            cudaGraphConditionalHandle h, int has_cond)
+{
+    __shared__ double s_red[32 * 2];
+    const SolveArgs a = *args;
+    KrylovScalars* S = a.S;
+    if (!S->cond) return;
+    const float omega = (float)S->omega;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    double rr = 0.0, rho = 0.0;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+        a.x[i] += omega * a.z[i];
+        const float ri = a.r[i] - omega * a.t[i];
+        a.r[i] = ri;
+        rr += (double)ri * ri;
+        rho += (double)a.r0[i] * ri;
+    }
+    double v[2] = {rr, rho};
+    grid_reduce<2>(v, a.partials, &S->counters[4], s_red, [&](const double (&t)[2]) {
+        S->rr = t[0];
+        const bool active = t[0] > S->atol_sq;
+        double beta = 0.0, beta_omega = 0.0;
+        if (active) {
+            beta = t[1] * S->tt / (S->r0v * S->st);
+            beta_omega = t[1] / S->r0v;
+            if (!finite(beta) || !finite(beta_omega)) {
+                S->status |= GB_DEV_BREAKDOWN;
+                beta = beta_omega = 0.0;
+            }
+        }
+        S->rho = t[1];
+        S->beta = beta;
+        S->beta_omega = beta_omega;
+        S->iter += 1;
+        int cond = active && (S->iter < S->maxiter);
+        if (!finite(t[0])) {
+            S->status |= GB_DEV_NONFINITE;
+            cond = 0;
+        }
+        set_cond(S, cond, h, has_cond);
+    });
+}
+
+// p = r + beta p - beta_omega v ; y = M p
+__global__ __launch_bounds__(VEC_THREADS) void k_bi_pupdate(const SolveArgs* __restrict__ args)
+{
+    const SolveArgs a = *args;
+    KrylovScalars* S = a.S;
+    if (!S->cond) return;
+    const float beta = (float)S->beta, bo = (float)S->beta_omega;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+        const float pi = a.r[i] + beta * a.p[i] - bo * a.v[i];
+        a.p[i] = pi;
+        a.y[i] = a.dinv ? a.dinv[i] * pi : pi;
+    }
+}
+
+__global__ void k_store_args(SolveArgs* dst, SolveArgs src, int reset_status)
+{
+    *dst = src;
+    if (reset_status) {
+        src.S->status = 0;
+        for (int k = 0; k < 8; ++k) src.S->counters[k] = 0u;
+        src.S->cond = 1;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Host-side solver handle
+// ---------------------------------------------------------------------------------------------
+struct Solver {
+    int kind, br, nrow, val_dtype;
+    int64_t n;
+    SpmvShape sh;
+    int spmv_grid, vec_grid;
+    size_t spmv_smem;
+    SolveArgs host;     // operand pointers currently set
+    SolveArgs* d_args;  // device copy (inside the workspace)
+    cudaStream_t cap_stream = nullptr;
+    cudaGraphExec_t exec_while = nullptr, exec_init = nullptr, exec_chunk = nullptr;
+    int chunk_iters = 0;
+};
+
+static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+struct WsLayout {
+    size_t args, scalars, partials, vec;
+    int nvec;
+    size_t total;
+};
+
+static WsLayout ws_layout(int kind, int64_t n, int spmv_grid, int vec_grid)
+{
+    WsLayout L;
+    L.args = align256(sizeof(SolveArgs));
+    L.scalars = align256(sizeof(KrylovScalars));
+    L.partials = align256(sizeof(double) * 3 * (size_t)std::max(spmv_grid, vec_grid));
+    L.vec = align256(sizeof(float) * (size_t)n);
+    L.nvec = (kind == KRYLOV_CG) ? 3 : 7;  // CG: r p Ap ; BiCGSTAB: r r0 p v t y z
+    L.total = L.args + L.scalars + L.partials + L.nvec * L.vec + 256;
+    return L;
+}
+
+template <int BR, typename VT> static void set_smem_attr(Solver* s)
+{
+    if (s->spmv_smem > 48 * 1024) {
+        cudaFuncSetAttribute(k_cg_init<BR, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->spmv_smem);
+        cudaFuncSetAttribute(k_cg_spmv<BR, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->spmv_smem);
+        cudaFuncSetAttribute(k_bi_init<BR, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->spmv_smem);
+        cudaFuncSetAttribute(k_bi_spmv_v<BR, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->spmv_smem);
+        cudaFuncSetAttribute(k_bi_spmv_t<BR, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->spmv_smem);
+    }
+}
+
+template <int BR, typename VT>
+static int launch_init_t(Solver* s, cudaStream_t st, cudaGraphConditionalHandle h, int has_cond)
+{
+    if (s->kind == KRYLOV_CG)
+        k_cg_init<BR, VT><<<s->spmv_grid, SPMV_THREADS, s->spmv_smem, st>>>(s->d_args, s->nrow, s->sh, h, has_cond);
+    else
+        k_bi_init<BR, VT><<<s->spmv_grid, SPMV_THREADS, s->spmv_smem, st>>>(s->d_args, s->nrow, s->sh, h, has_cond);
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+template <int BR, typename VT>
+static int launch_iter_t(Solver* s, cudaStream_t st, cudaGraphConditionalHandle h, int has_cond)
+{
+    if (s->kind == KRYLOV_CG) {
+        k_cg_spmv<BR, VT><<<s->spmv_grid, SPMV_THREADS, s->spmv_smem, st>>>(s->d_args, s->nrow, s->sh);
+        k_cg_update<<<s->vec_grid, VEC_THREADS, 0, st>>>(s->d_args, h, has_cond);
+        k_cg_pupdate<<<s->vec_grid, VEC_THREADS, 0, st>>>(s->d_args);
+    } else {
+        k_bi_spmv_v<BR, VT><<<s->spmv_grid, SPMV_THREADS, s->spmv_smem, st>>>(s->d_args, s->nrow, s->sh);
+        k_bi_update1<<<s->vec_grid, VEC_THREADS, 0, st>>>(s->d_args);
+        k_bi_spmv_t<BR, VT><<<s->spmv_grid, SPMV_THREADS, s->spmv_smem, st>>>(s->d_args, s->nrow, s->sh);
+        k_bi_update2<<<s->vec_grid, VEC_THREADS, 0, st>>>(s->d_args, h, has_cond);
+        k_bi_pupdate<<<s->vec_grid, VEC_THREADS, 0, st>>>(s->d_args);
+    }
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+static int launch_init(Solver* s, cudaStream_t st, cudaGraphConditionalHandle h, int has_cond)
+{
+    if (s->br == 1) return s->val_dtype == GB_BF16 ? launch_init_t<1, __nv_bfloat16>(s, st, h, has_cond)
+                                                   : launch_init_t<1, float>(s, st, h, has_cond);
+    return s->val_dtype == GB_BF16 ? launch_init_t<3, __nv_bfloat16>(s, st, h, has_cond)
+                                   : launch_init_t<3, float>(s, st, h, has_cond);
+}
+
+static int launch_iter(Solver* s, cudaStream_t st, cudaGraphConditionalHandle h, int has_cond)
+{
+    if (s->br == 1) return s->val_dtype == GB_BF16 ? launch_iter_t<1, __nv_bfloat16>(s, st, h, has_cond)
+                                                   : launch_iter_t<1, float>(s, st, h, has_cond);
+    return s->val_dtype == GB_BF16 ? launch_iter_t<3, __nv_bfloat16>(s, st, h, has_cond)
+                                   : launch_iter_t<3, float>(s, st, h, has_cond);
+}
+
+// Appends init + while(condition){iteration} to the capture active on `st`.  Works both for the
+// solver's own cached graph and inside a caller's stream capture (the reference's
+// check_every=0 contract: the whole solve is capturable).
+static int capture_full_solve(Solver* s, cudaStream_t st)
+{
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t g;
+    const cudaGraphNode_t* deps;
+    const cudaGraphEdgeData* edata;
+    size_t ndeps;
+    GB_CHECK_CUDA(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, &edata, &ndeps));
+    if (cs != cudaStreamCaptureStatusActive) {
+        gb::set_error("capture_full_solve: stream is not capturing");
+        return GB_ERR_INVALID;
+    }
+    cudaGraphConditionalHandle h;
+    GB_CHECK_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
+    int rc = launch_init(s, st, h, 1);
+    if (rc) return rc;
+    GB_CHECK_CUDA(cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, &edata, &ndeps));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t cnode;
+    GB_CHECK_CUDA(cudaGraphAddNode(&cnode, g, deps, edata, ndeps, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    GB_CHECK_CUDA(cudaStreamUpdateCaptureDependencies(st, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+    GB_CHECK_CUDA(cudaStreamBeginCaptureToGraph(s->cap_stream, body, nullptr, nullptr, 0,
+                                                cudaStreamCaptureModeRelaxed));
+    rc = launch_iter(s, s->cap_stream, h, 1);
+    cudaGraph_t body_out;
+    cudaError_t e = cudaStreamEndCapture(s->cap_stream, &body_out);
+    if (rc) return rc;
+    GB_CHECK_CUDA(e);
+    return GB_OK;
+}
+
+static int build_graphs(Solver* s, int chunk_iters)
+{
+    cudaGraph_t g;
+    // full solve: init + conditional while loop
+    if (!s->exec_while) {
+        GB_CHECK_CUDA(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeRelaxed));
+        // capture_full_solve needs a second stream for the body capture
+        cudaStream_t outer = s->cap_stream;
+        cudaStream_t body_stream;
+        GB_CHECK_CUDA(cudaStreamCreateWithFlags(&body_stream, cudaStreamNonBlocking));
+        s->cap_stream = body_stream;
+        int rc = capture_full_solve(s, outer);
+        s->cap_stream = outer;
+        cudaError_t e = cudaStreamEndCapture(outer, &g);
+        cudaStreamDestroy(body_stream);
+        if (rc) return rc;
+        GB_CHECK_CUDA(e);
+        GB_CHECK_CUDA(cudaGraphInstantiate(&s->exec_while, g, 0));
+        cudaGraphDestroy(g);
+    }
+    if (!s->exec_init) {
+        GB_CHECK_CUDA(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeRelaxed));
+        int rc = launch_init(s, s->cap_stream, 0, 0);
+        cudaError_t e = cudaStreamEndCapture(s->cap_stream, &g);
+        if (rc) return rc;
+        GB_CHECK_CUDA(e);
+        GB_CHECK_CUDA(cudaGraphInstantiate(&s->exec_init, g, 0));
+        cudaGraphDestroy(g);
+    }
+    if (chunk_iters > 0 && chunk_iters != s->chunk_iters) {
+        if (s->exec_chunk) cudaGraphExecDestroy(s->exec_chunk);
+        s->exec_chunk = nullptr;
+        GB_CHECK_CUDA(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeRelaxed));
+        int rc = GB_OK;
+        for (int k = 0; k < chunk_iters && rc == GB_OK; ++k) rc = launch_iter(s, s->cap_stream, 0, 0);
+        cudaError_t e = cudaStreamEndCapture(s->cap_stream, &g);
+        if (rc) return rc;
+        GB_CHECK_CUDA(e);
+        GB_CHECK_CUDA(cudaGraphInstantiate(&s->exec_chunk, g, 0));
+        cudaGraphDestroy(g);
+        s->chunk_iters = chunk_iters;
+    }
+    return GB_OK;
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+GB_API size_t gb_krylov_workspace_bytes(int kind, int block_dim, int nrow, int64_t nnz, int val_dtype)
+{
+    SpmvShape sh = default_shape(block_dim, block_dim, val_dtype, nrow, nnz, nnz, true);
+    const int64_t n = (int64_t)nrow * block_dim;
+    const int spmv_grid = ceil_div(std::max(nrow, 1), sh.rows);
+    const int vec_grid = kSmCount * 4;
+    return ws_layout(kind, n, spmv_grid, vec_grid).total;
+}
+
+// Creates a solver handle for a BSR system with block_dim x block_dim blocks (1 or 3) and values
+// of val_dtype (GB_F32 or GB_BF16).  The workspace (from gb_krylov_workspace_bytes) holds the
+// work vectors, scalars and reduction partials; the handle owns only its CUDA graphs.
+GB_API int gb_krylov_create(int kind, int block_dim, int nrow, int64_t nnz, int64_t ncap, int val_dtype,
+                            int rows_per_cta, int lanes_per_row, int cap_blocks, void* workspace,
+                            size_t workspace_bytes, void** handle_out)
+{
+    GB_REQUIRE(kind == KRYLOV_CG || kind == KRYLOV_BICGSTAB, "krylov: unknown solver kind %d", kind);
+    GB_REQUIRE(block_dim == 1 || block_dim == 3, "krylov: block_dim must be 1 or 3");
+    GB_REQUIRE(val_dtype == GB_F32 || val_dtype == GB_BF16, "krylov: values must be float32 or bfloat16");
+    GB_REQUIRE(nrow > 0 && handle_out && workspace, "krylov: bad arguments");
+    Solver* s = new (std::nothrow) Solver();
+    if (!s) {
+        gb::set_error("krylov: out of host memory");
+        return GB_ERR_INVALID;
+    }
+    s->kind = kind;
+    s->br = block_dim;
+    s->nrow = nrow;
+    s->val_dtype = val_dtype;
+    s->n = (int64_t)nrow * block_dim;
+    s->sh = default_shape(block_dim, block_dim, val_dtype, nrow, nnz, ncap, true);
+    if (rows_per_cta > 0) s->sh.rows = rows_per_cta;
+    if (lanes_per_row > 0) s->sh.G = lanes_per_row;
+    if (cap_blocks > 0) s->sh.cap = cap_blocks & ~(SPMV_ALIGN - 1);
+    s->sh.ncap = ncap;
+    s->spmv_grid = ceil_div(nrow, s->sh.rows);
+    s->vec_grid = kSmCount * 4;
+    s->spmv_smem = (block_dim == 1)
+                       ? (val_dtype == GB_BF16 ? spmv_smem_bytes<1, 1, __nv_bfloat16>(s->sh.rows, s->sh.cap)
+                                               : spmv_smem_bytes<1, 1, float>(s->sh.rows, s->sh.cap))
+                       : (val_dtype == GB_BF16 ? spmv_smem_bytes<3, 3, __nv_bfloat16>(s->sh.rows, s->sh.cap)
+                                               : spmv_smem_bytes<3, 3, float>(s->sh.rows, s->sh.cap));
+    WsLayout L = ws_layout(kind, s->n, s->spmv_grid, s->vec_grid);
+    if (workspace_bytes < L.total) {
+        gb::set_error("krylov: workspace too small (%zu < %zu)", workspace_bytes, L.total);
+        delete s;
+        return GB_ERR_CAPACITY;
+    }
+    unsigned char* ws = reinterpret_cast<unsigned char*>(((uintptr_t)workspace + 255) & ~(uintptr_t)255);
+    s->d_args = reinterpret_cast<SolveArgs*>(ws);
+    ws += L.args;
+    s->host = SolveArgs{};
+    s->host.S = reinterpret_cast<KrylovScalars*>(ws);
+    ws += L.scalars;
+    s->host.partials = reinterpret_cast<double*>(ws);
+    ws += L.partials;
+    float* vecs[7] = {nullptr};
+    for (int k = 0; k < L.nvec; ++k) {
+        vecs[k] = reinterpret_cast<float*>(ws);
+        ws += L.vec;
+    }
+    if (kind == KRYLOV_CG) {
+        s->host.r = vecs[0];
+        s->host.p = vecs[1];
+        s->host.Ap = vecs[2];
+    } else {
+        s->host.r = vecs[0];
+        s->host.r0 = vecs[1];
+        s->host.p = vecs[2];
+        s->host.v = vecs[3];
+        s->host.t = vecs[4];
+        s->host.y = vecs[5];
+        s->host.z = vecs[6];
+    }
+    s->host.n = s->n;
+    if (block_dim == 1) {
+        if (val_dtype == GB_BF16) set_smem_attr<1, __nv_bfloat16>(s); else set_smem_attr<1, float>(s);
+    } else {
+        if (val_dtype == GB_BF16) set_smem_attr<3, __nv_bfloat16>(s); else set_smem_attr<3, float>(s);
+    }
+    cudaError_t e = cudaStreamCreateWithFlags(&s->cap_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+        delete s;
+        return gb::cuda_fail(e, "cudaStreamCreateWithFlags");
+    }
+    // scalars/counters start zeroed
+    e = cudaMemset(s->host.S, 0, sizeof(KrylovScalars));
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(s->cap_stream);
+        delete s;
+        return gb::cuda_fail(e, "cudaMemset");
+    }
+    *handle_out = s;
+    return GB_OK;
+}
+
+GB_API int gb_krylov_destroy(void* handle)
+{
+    Solver* s = static_cast<Solver*>(handle);
+    if (!s) return GB_OK;
+    if (s->exec_while) cudaGraphExecDestroy(s->exec_while);
+    if (s->exec_init) cudaGraphExecDestroy(s->exec_init);
+    if (s->exec_chunk) cudaGraphExecDestroy(s->exec_chunk);
+    if (s->cap_stream) cudaStreamDestroy(s->cap_stream);
+    delete s;
+    return GB_OK;
+}
+
+// Sets the operands of the next solve (stream-ordered: a one-thread kernel writes the device
+// argument block, so this is capturable too).  dinv may be null (no preconditioner).
+GB_API int gb_krylov_set_operands(void* handle, const int* offsets, const int* row_counts, const int* columns,
+                                  const void* values, const float* dinv, const float* b, float* x, int x_is_zero,
+                                  double tol, double atol, int maxiter, int left_precond, cudaStream_t stream)
+{
+    Solver* s = static_cast<Solver*>(handle);
+    GB_REQUIRE(s && offsets && columns && values && b && x, "krylov_set_operands: null argument");
+    s->host.offsets = offsets;
+    s->host.row_counts = row_counts;
+    s->host.columns = columns;
+    s->host.values = values;
+    s->host.dinv = dinv;
+    s->host.b = b;
+    s->host.x = x;
+    s->host.x_is_zero = x_is_zero;
+    s->host.tol = tol;
+    s->host.atol = atol;
+    s->host.maxiter = maxiter;
+    s->host.left_precond = left_precond;
+    const bool aligned = ((uintptr_t)columns % 16 == 0) && ((uintptr_t)values % 16 == 0);
+    if (!aligned && s->sh.cap != 0) {
+        gb::set_error("krylov_set_operands: columns/values must be 16-byte aligned");
+        return GB_ERR_INVALID;
+    }
+    k_store_args<<<1, 1, 0, stream>>>(s->d_args, s->host, 1);
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+// what: 0 = whole solve (init + device-side while loop), 1 = init only, 2 = `chunk_iters`
+// iterations (each iteration is a no-op once converged), 3 = one eager (non-graph) iteration,
+// 4 = eager init.  Modes 0-2 replay cached graphs; if `stream` is capturing, mode 0 is appended
+// to the caller's capture instead.
+GB_API int gb_krylov_launch(void* handle, int what, int chunk_iters, cudaStream_t stream)
+{
+    Solver* s = static_cast<Solver*>(handle);
+    GB_REQUIRE(s, "krylov_launch: null handle");
+    cudaStreamCaptureStatus cs;
+    GB_CHECK_CUDA(cudaStreamIsCapturing(stream, &cs));
+    const bool capturing = (cs == cudaStreamCaptureStatusActive);
+    if (what == 3) return launch_iter(s, stream, 0, 0);
+    if (what == 4) return launch_init(s, stream, 0, 0);
+    if (capturing) {
+        if (what == 0) return capture_full_solve(s, stream);
+        if (what == 1) return launch_init(s, stream, 0, 0);
+        int rc = GB_OK;
+        for (int k = 0; k < chunk_iters && rc == GB_OK; ++k) rc = launch_iter(s, stream, 0, 0);
+        return rc;
+    }
+    int rc = build_graphs(s, what == 2 ? chunk_iters : 0);
+    if (rc) return rc;
+    if (what == 0) GB_CHECK_CUDA(cudaGraphLaunch(s->exec_while, stream));
+    else if (what == 1) GB_CHECK_CUDA(cudaGraphLaunch(s->exec_init, stream));
+    else if (what == 2) GB_CHECK_CUDA(cudaGraphLaunch(s->exec_chunk, stream));
+    else {
+        gb::set_error("krylov_launch: bad mode %d", what);
+        return GB_ERR_INVALID;
+    }
+    return GB_OK;
+}
+
+// Device addresses of the solver scalars (iteration count, residual^2, atol^2, status), so the
+// host can return them as device arrays (the check_every == 0 contract) or copy them back.
+GB_API int gb_krylov_scalars(void* handle, int** iter, double** rr, double** atol_sq, int** status)
+{
+    Solver* s = static_cast<Solver*>(handle);
+    GB_REQUIRE(s, "krylov_scalars: null handle");
+    if (iter) *iter = &s->host.S->iter;
+    if (rr) *rr = &s->host.S->rr;
+    if (atol_sq) *atol_sq = &s->host.S->atol_sq;
+    if (status) *status = &s->host.S->status;
+    return GB_OK;
+}
+
+// Copies {iter, cond, status} and {rr, atol_sq, bb} to host buffers (stream-ordered).
+GB_API int gb_krylov_read(void* handle, int* host_ints3, double* host_doubles3, cudaStream_t stream)
+{
+    Solver* s = static_cast<Solver*>(handle);
+    GB_REQUIRE(s && host_ints3 && host_doubles3, "krylov_read: null argument");
+    KrylovScalars* S = s->host.S;
+    GB_CHECK_CUDA(cudaMemcpyAsync(host_ints3, &S->iter, 2 * sizeof(int), cudaMemcpyDeviceToHost, stream));
+    GB_CHECK_CUDA(cudaMemcpyAsync(host_ints3 + 2, &S->status, sizeof(int), cudaMemcpyDeviceToHost, stream));
+    GB_CHECK_CUDA(cudaMemcpyAsync(host_doubles3, &S->rr, sizeof(double), cudaMemcpyDeviceToHost, stream));
+    GB_CHECK_CUDA(cudaMemcpyAsync(host_doubles3 + 1, &S->atol_sq, sizeof(double), cudaMemcpyDeviceToHost, stream));
+    GB_CHECK_CUDA(cudaMemcpyAsync(host_doubles3 + 2, &S->bb, sizeof(double), cudaMemcpyDeviceToHost, stream));
+    return GB_OK;
+}
+
+// Device pointers of the work vectors (r, p/r0, Ap/p, ...) for tests and the FCG driver.
+GB_API int gb_krylov_vectors(void* handle, float** r, float** p, float** Ap)
+{
+    Solver* s = static_cast<Solver*>(handle);
+    GB_REQUIRE(s, "krylov_vectors: null handle");
+    if (r) *r = s->host.r;
+    if (p) *p = s->host.p;
+    if (Ap) *Ap = s->kind == KRYLOV_CG ? s->host.Ap : s->host.v;
+    return GB_OK;
+}

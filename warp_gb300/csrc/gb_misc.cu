@@ -1,0 +1,259 @@
+// gb_misc.cu -- small kernels around the solve path: BSR diagonal extraction and the Jacobi
+// inverse diagonal, diagonal / dense operator products, deterministic multi-column dot products
+// and axpby for the generic (non-BSR) LinearOperator path.
+//
+// Replaces: bsr_get_diag (warp/_src/sparse.py:2871-2887), _extract_inverse_diagonal_* and
+// _inverse_diag_coefficient (warp/_src/optim/linear.py:2290-2329), _diag_mv_kernel (:2271-2287),
+// _dense_mv_kernel (:2250-2268), TiledDot.compute (:506-568) and array_axpy.
+#include "gb_common.cuh"
+
+namespace gb {
+
+template <typename T>
+__global__ void k_bsr_get_diag(int nrow, int br, int bc, const int* __restrict__ offsets,
+                               const int* __restrict__ row_counts, const int* __restrict__ columns,
+                               const T* __restrict__ values, T* __restrict__ out)
+{
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= nrow) return;
+    const int bs = br * bc;
+    int beg = offsets[row];
+    const int end = row_counts ? beg + row_counts[row] : offsets[row + 1];
+    // columns are sorted within a row: binary search for the diagonal block
+    int lo = beg, hi = end - 1, found = -1;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        const int c = columns[mid];
+        if (c == row) {
+            found = mid;
+            break;
+        }
+        if (c < row) lo = mid + 1; else hi = mid - 1;
+    }
+    for (int q = 0; q < bs; ++q) out[(size_t)row * bs + q] = (found >= 0) ? values[(size_t)found * bs + q] : T(0);
+}
+
+// inverse of the diagonal entries of the diagonal blocks: 1/d, 1/|d| (use_abs) or 1 when d == 0.
+template <typename T>
+__global__ void k_bsr_inverse_diag(int nrow, int bdim, const int* __restrict__ offsets,
+                                   const int* __restrict__ row_counts, const int* __restrict__ columns,
+                                   const T* __restrict__ values, int use_abs, T* __restrict__ inv)
+{
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= nrow) return;
+    const int bs = bdim * bdim;
+    const int beg = offsets[row];
+    const int end = row_counts ? beg + row_counts[row] : offsets[row + 1];
+    int lo = beg, hi = end - 1, found = -1;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        const int c = columns[mid];
+        if (c == row) {
+            found = mid;
+            break;
+        }
+        if (c < row) lo = mid + 1; else hi = mid - 1;
+    }
+    for (int k = 0; k < bdim; ++k) {
+        T d = (found >= 0) ? values[(size_t)found * bs + k * bdim + k] : T(0);
+        if (use_abs) d = d < T(0) ? -d : d;
+        inv[(size_t)row * bdim + k] = (d == T(0)) ? T(1) : T(1) / d;
+    }
+}
+
+template <typename T>
+__global__ void k_diag_mv(int64_t n, const T* __restrict__ A, const T* __restrict__ x, const T* y, T* z, T alpha,
+                          T beta)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        T s = T(0);
+        if (alpha != T(0)) s += alpha * (A[i] * x[i]);
+        if (beta != T(0)) s += beta * y[i];
+        z[i] = s;
+    }
+}
+
+// z = alpha A x + beta y for a dense row-major m x n matrix; one warp per row.
+template <typename T>
+__global__ void k_dense_mv(int m, int n, const T* __restrict__ A, const T* __restrict__ x, const T* y, T* z, T alpha,
+                           T beta)
+{
+    const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
+    if (row >= m) return;
+    T s = T(0);
+    if (alpha != T(0))
+        for (int c = lane; c < n; c += 32) s += A[(size_t)row * n + c] * x[c];
+    s = warp_sum(s);
+    if (lane == 0) {
+        T v = alpha * s;
+        if (beta != T(0)) v += beta * y[row];
+        z[row] = v;
+    }
+}
+
+// Multi-column dot products out[k] = sum_i x_k[i] y_k[i] (k < ncols <= 4), accumulated in fp64,
+// single-pass deterministic grid reduction.
+struct DotPtrs {
+    const void* x[4];
+    const void* y[4];
+};
+
+template <typename T>
+__global__ void k_dots(int64_t n, int ncols, DotPtrs P, double* partials, unsigned int* counter, double* out)
+{
+    __shared__ double s_red[32 * 4];
+    double acc[4] = {0, 0, 0, 0};
+    for (int k = 0; k < ncols; ++k) {
+        const T* x = static_cast<const T*>(P.x[k]);
+        const T* y = static_cast<const T*>(P.y[k]);
+        double a = 0.0;
+        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+            a += (double)x[i] * (double)y[i];
+        acc[k] = a;
+    }
+    grid_reduce<4>(acc, partials, counter, s_red, [&](const double (&t)[4]) {
+        for (int k = 0; k < ncols; ++k) out[k] = t[k];
+    });
+}
+
+template <typename T>
+__global__ void k_axpby(int64_t n, T alpha, const T* __restrict__ x, T beta, const T* y, T* out)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        T v = alpha * x[i];
+        if (beta != T(0)) v += beta * y[i];
+        out[i] = v;
+    }
+}
+
+static int vgrid(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(n, 256), kSmCount * 8)); }
+
+}  // namespace gb
+
+using namespace gb;
+
+GB_API int gb_bsr_get_diag(int dtype, int br, int bc, int nrow, const int* offsets, const int* row_counts,
+                           const int* columns, const void* values, void* out, cudaStream_t stream)
+{
+    GB_REQUIRE(nrow >= 0 && br >= 1 && bc >= 1, "bsr_get_diag: bad shape");
+    if (nrow == 0) return GB_OK;
+    const int grid = ceil_div(nrow, 128);
+    if (dtype == GB_F32)
+        k_bsr_get_diag<float><<<grid, 128, 0, stream>>>(nrow, br, bc, offsets, row_counts, columns,
+                                                        (const float*)values, (float*)out);
+    else if (dtype == GB_F64)
+        k_bsr_get_diag<double><<<grid, 128, 0, stream>>>(nrow, br, bc, offsets, row_counts, columns,
+                                                         (const double*)values, (double*)out);
+    else {
+        gb::set_error("bsr_get_diag: unsupported dtype");
+        return GB_ERR_UNSUPPORTED;
+    }
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+GB_API int gb_bsr_inverse_diagonal(int dtype, int bdim, int nrow, const int* offsets, const int* row_counts,
+                                   const int* columns, const void* values, int use_abs, void* inv, cudaStream_t stream)
+{
+    GB_REQUIRE(nrow >= 0 && bdim >= 1, "bsr_inverse_diagonal: bad shape");
+    if (nrow == 0) return GB_OK;
+    const int grid = ceil_div(nrow, 128);
+    if (dtype == GB_F32)
+        k_bsr_inverse_diag<float><<<grid, 128, 0, stream>>>(nrow, bdim, offsets, row_counts, columns,
+                                                            (const float*)values, use_abs, (float*)inv);
+    else if (dtype == GB_F64)
+        k_bsr_inverse_diag<double><<<grid, 128, 0, stream>>>(nrow, bdim, offsets, row_counts, columns,
+                                                             (const double*)values, use_abs, (double*)inv);
+    else {
+        gb::set_error("bsr_inverse_diagonal: unsupported dtype");
+        return GB_ERR_UNSUPPORTED;
+    }
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+GB_API int gb_diag_mv(int dtype, int64_t n, const void* A, const void* x, const void* y, void* z, double alpha,
+                      double beta, cudaStream_t stream)
+{
+    if (n <= 0) return GB_OK;
+    if (dtype == GB_F32)
+        k_diag_mv<float><<<vgrid(n), 256, 0, stream>>>(n, (const float*)A, (const float*)x, (const float*)y,
+                                                       (float*)z, (float)alpha, (float)beta);
+    else if (dtype == GB_F64)
+        k_diag_mv<double><<<vgrid(n), 256, 0, stream>>>(n, (const double*)A, (const double*)x, (const double*)y,
+                                                        (double*)z, alpha, beta);
+    else {
+        gb::set_error("diag_mv: unsupported dtype");
+        return GB_ERR_UNSUPPORTED;
+    }
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+GB_API int gb_dense_mv(int dtype, int m, int n, const void* A, const void* x, const void* y, void* z, double alpha,
+                       double beta, cudaStream_t stream)
+{
+    if (m <= 0) return GB_OK;
+    const int grid = ceil_div(m, 8);
+    if (dtype == GB_F32)
+        k_dense_mv<float><<<grid, 256, 0, stream>>>(m, n, (const float*)A, (const float*)x, (const float*)y,
+                                                   (float*)z, (float)alpha, (float)beta);
+    else if (dtype == GB_F64)
+        k_dense_mv<double><<<grid, 256, 0, stream>>>(m, n, (const double*)A, (const double*)x, (const double*)y,
+                                                    (double*)z, alpha, beta);
+    else {
+        gb::set_error("dense_mv: unsupported dtype");
+        return GB_ERR_UNSUPPORTED;
+    }
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+GB_API size_t gb_dots_workspace_bytes(void) { return 256 + sizeof(double) * 4 * (size_t)(kSmCount * 2); }
+
+// out[k] = x_k . y_k for k < ncols (<= 4), fp64 accumulation, deterministic.  xs/ys are host
+// arrays of device pointers (passed by value to the kernel, so the call is capturable).  The
+// workspace's first bytes hold the arrival counter (zero before first use; the kernel leaves it 0).
+GB_API int gb_dots(int dtype, int64_t n, int ncols, const void* const* xs, const void* const* ys, double* out,
+                   void* workspace, cudaStream_t stream)
+{
+    GB_REQUIRE(ncols >= 1 && ncols <= 4, "dots: 1 to 4 columns");
+    unsigned char* ws = static_cast<unsigned char*>(workspace);
+    unsigned int* counter = reinterpret_cast<unsigned int*>(ws);
+    double* partials = reinterpret_cast<double*>(ws + 256);
+    DotPtrs P = {};
+    for (int k = 0; k < ncols; ++k) {
+        P.x[k] = xs[k];
+        P.y[k] = ys[k];
+    }
+    const int grid = kSmCount * 2;
+    if (dtype == GB_F32)
+        k_dots<float><<<grid, 256, 0, stream>>>(n, ncols, P, partials, counter, out);
+    else if (dtype == GB_F64)
+        k_dots<double><<<grid, 256, 0, stream>>>(n, ncols, P, partials, counter, out);
+    else {
+        gb::set_error("dots: unsupported dtype");
+        return GB_ERR_UNSUPPORTED;
+    }
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+GB_API int gb_axpby(int dtype, int64_t n, double alpha, const void* x, double beta, const void* y, void* out,
+                    cudaStream_t stream)
+{
+    if (n <= 0) return GB_OK;
+    if (dtype == GB_F32)
+        k_axpby<float><<<vgrid(n), 256, 0, stream>>>(n, (float)alpha, (const float*)x, (float)beta, (const float*)y,
+                                                     (float*)out);
+    else if (dtype == GB_F64)
+        k_axpby<double><<<vgrid(n), 256, 0, stream>>>(n, alpha, (const double*)x, beta, (const double*)y,
+                                                      (double*)out);
+    else {
+        gb::set_error("axpby: unsupported dtype");
+        return GB_ERR_UNSUPPORTED;
+    }
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}

@@ -1,0 +1,253 @@
+// gb_spmv.cu -- y = alpha * A x + beta * y for BSR matrices (bsr_mv).
+//
+// Replaces the JIT kernels bsr_mv_kernel / bsr_mv_tiled_kernel / bsr_mv_transpose_kernel
+// launched by warp/_src/sparse.py:4792-4913 (kernels :4627-4747).  1x1 and 3x3 blocks (the
+// shapes of the Q1 scalar and vector spaces) use the staged row-tile kernel of gb_spmv.cuh;
+// other block shapes use a one-thread-per-scalar-row kernel like the reference's.
+#include "gb_common.cuh"
+#include "gb_spmv.cuh"
+
+namespace gb {
+
+template <int BR, typename XT, typename AT> struct EpiAxpby {
+    XT* y_out;
+    const XT* y_in;
+    AT alpha, beta;
+    __device__ __forceinline__ void operator()(int row, const AT (&acc)[BR], int lane_g)
+    {
+        if (lane_g < BR) {
+            const size_t i = (size_t)row * BR + lane_g;
+            AT v = alpha * pick<BR>(acc, lane_g);
+            if (beta != AT(0)) v += beta * (AT)y_in[i];
+            y_out[i] = (XT)v;
+        }
+    }
+};
+
+template <int BR, int BC, typename VT, typename XT, typename AT>
+__global__ __launch_bounds__(SPMV_THREADS) void k_bsr_mv(int nrow, SpmvShape sh, const int* __restrict__ offsets,
+                                                         const int* __restrict__ row_counts,
+                                                         const int* __restrict__ columns,
+                                                         const VT* __restrict__ values, const XT* __restrict__ x,
+                                                         const XT* y_in, XT* y_out, AT alpha, AT beta, int* status)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    EpiAxpby<BR, XT, AT> epi{y_out, y_in, alpha, beta};
+    spmv_tile<BR, BC, VT, XT, AT>(nrow, sh, offsets, row_counts, columns, values, x, smem, status, epi);
+}
+
+// alpha == 0: y_out = beta * y_in without reading A or x (reference semantics, sparse.py:4649).
+template <typename XT, typename AT>
+__global__ void k_scale(int64_t n, const XT* y_in, XT* y_out, AT beta)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        y_out[i] = (beta != AT(0)) ? (XT)(beta * (AT)y_in[i]) : XT(0);
+}
+
+// Generic block shapes: one thread per scalar row, as bsr_mv_kernel (sparse.py:4627-4665).
+template <typename VT, typename XT, typename AT>
+__global__ void k_bsr_mv_generic(int nrow, int br, int bc, const int* __restrict__ offsets,
+                                 const int* __restrict__ row_counts, const int* __restrict__ columns,
+                                 const VT* __restrict__ values, const XT* __restrict__ x, const XT* y_in, XT* y_out,
+                                 AT alpha, AT beta)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nrow * br) return;
+    const int row = (int)(t / br), sub = (int)(t - (int64_t)row * br);
+    const int beg = offsets[row];
+    const int end = row_counts ? beg + row_counts[row] : offsets[row + 1];
+    AT v = AT(0);
+    for (int b = beg; b < end; ++b) {
+        const int xs = columns[b] * bc;
+        for (int c = 0; c < bc; ++c) v += cvt<AT>(values[((size_t)b * br + sub) * bc + c]) * (AT)x[xs + c];
+    }
+    v *= alpha;
+    if (beta != AT(0)) v += beta * (AT)y_in[t];
+    y_out[t] = (XT)v;
+}
+
+// Transposed product y += alpha * A^T x with atomics (non-deterministic, as the reference's
+// bsr_mv_transpose_kernel, sparse.py:4718-4747).  y must already hold beta * y.
+template <typename VT, typename XT, typename AT>
+__global__ void k_bsr_mv_transpose(int nrow, int br, int bc, const int* __restrict__ offsets,
+                                   const int* __restrict__ row_counts, const int* __restrict__ columns,
+                                   const VT* __restrict__ values, const XT* __restrict__ x, XT* y, AT alpha)
+{
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nrow * bc) return;
+    const int row = (int)(t / bc), j = (int)(t - (int64_t)row * bc);
+    const int beg = offsets[row];
+    const int end = row_counts ? beg + row_counts[row] : offsets[row + 1];
+    for (int b = beg; b < end; ++b) {
+        AT s = AT(0);
+        for (int i = 0; i < br; ++i) s += cvt<AT>(values[((size_t)b * br + i) * bc + j]) * (AT)x[(size_t)row * br + i];
+        atomicAdd(&y[(size_t)columns[b] * bc + j], (XT)(alpha * s));
+    }
+}
+
+template <int BR, int BC, typename VT, typename XT, typename AT>
+static int launch_mv(int nrow, SpmvShape sh, const int* offsets, const int* row_counts, const int* columns,
+                     const void* values, const void* x, const void* y_in, void* y_out, double alpha, double beta,
+                     int* status, cudaStream_t stream)
+{
+    const size_t smem = spmv_smem_bytes<BR, BC, VT>(sh.rows, sh.cap);
+    auto kern = k_bsr_mv<BR, BC, VT, XT, AT>;
+    if (smem > 48 * 1024) GB_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int grid = ceil_div(nrow, sh.rows);
+    kern<<<grid, SPMV_THREADS, smem, stream>>>(nrow, sh, offsets, row_counts, columns, (const VT*)values,
+                                               (const XT*)x, (const XT*)y_in, (XT*)y_out, (AT)alpha, (AT)beta, status);
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+// Default tile shape (the autotuner in warp_gb300.tuning may override it per matrix).
+SpmvShape default_shape(int br, int bc, int val_dtype, int nrow, int64_t nnzb, int64_t ncap, bool aligned)
+{
+    SpmvShape sh;
+    const double avg = nrow > 0 ? (double)nnzb / (double)nrow : 0.0;
+    const int bb = br * bc;
+    const int vbytes = (val_dtype == GB_F64) ? 8 : (val_dtype == GB_BF16 ? 2 : 4);
+    // lanes per row: about 3-4 blocks per lane
+    int G = 1;
+    while (G < 32 && G * 4 < avg) G <<= 1;
+    if (br > 1 && G < 4) G = 4;
+    sh.G = G;
+    // rows per CTA so that a tile stages ~24-40 KB
+    const double bytes_per_row = avg * (4.0 + bb * vbytes);
+    int rows = 256 / G;
+    while (rows * 2 <= 1024 && (rows * 2) * bytes_per_row <= 28 * 1024) rows *= 2;
+    sh.rows = rows;
+    int cap = (int)(avg * rows * 1.25) + 2 * SPMV_ALIGN + 16;
+    cap = (cap + SPMV_ALIGN - 1) & ~(SPMV_ALIGN - 1);
+    sh.cap = aligned ? cap : 0;
+    sh.ncap = ncap;
+    return sh;
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+// y_out = alpha * A x + beta * y_in (y_in may equal y_out; x must not alias y_out).
+// Replaces bsr_mv (warp/_src/sparse.py:4792-4913).  val_dtype: GB_F32 / GB_F64 / GB_BF16;
+// vec_dtype: GB_F32 / GB_F64 (x and y).  ncap: entries available in columns/values.
+// rows_per_cta / lanes_per_row / cap_blocks <= 0 select the built-in heuristic.
+GB_API int gb_bsr_mv(int block_rows, int block_cols, int nrow, int ncol, int64_t nnz_upper, int64_t ncap,
+                     const int* offsets, const int* row_counts, const int* columns, const void* values,
+                     int val_dtype, const void* x, const void* y_in, void* y_out, int vec_dtype, double alpha,
+                     double beta, int transpose, int rows_per_cta, int lanes_per_row, int cap_blocks, int* status,
+                     cudaStream_t stream)
+{
+    GB_REQUIRE(nrow >= 0 && ncol >= 0, "bsr_mv: negative size");
+    GB_REQUIRE(block_rows >= 1 && block_cols >= 1, "bsr_mv: bad block shape");
+    GB_REQUIRE(status != nullptr, "bsr_mv: status word required");
+    const int br = block_rows, bc = block_cols;
+    const int64_t ny = (int64_t)(transpose ? ncol * bc : nrow * br);
+    if (ny == 0) return GB_OK;
+    if (alpha == 0.0 || nrow == 0) {
+        const int grid = (int)std::min<int64_t>(ceil_div<int64_t>(ny, 256), kSmCount * 8);
+        if (vec_dtype == GB_F32) k_scale<float, float><<<grid, 256, 0, stream>>>(ny, (const float*)y_in, (float*)y_out, (float)beta);
+        else k_scale<double, double><<<grid, 256, 0, stream>>>(ny, (const double*)y_in, (double*)y_out, beta);
+        GB_CHECK_CUDA(cudaGetLastError());
+        return GB_OK;
+    }
+    GB_REQUIRE(offsets && columns && values && x && y_out, "bsr_mv: null pointer");
+
+    if (transpose) {
+        const int grid_s = (int)std::min<int64_t>(ceil_div<int64_t>(ny, 256), kSmCount * 8);
+        if (vec_dtype == GB_F32) k_scale<float, float><<<grid_s, 256, 0, stream>>>(ny, (const float*)y_in, (float*)y_out, (float)beta);
+        else k_scale<double, double><<<grid_s, 256, 0, stream>>>(ny, (const double*)y_in, (double*)y_out, beta);
+        const int grid = (int)ceil_div<int64_t>((int64_t)nrow * bc, 256);
+        if (val_dtype == GB_F32 && vec_dtype == GB_F32)
+            k_bsr_mv_transpose<float, float, float><<<grid, 256, 0, stream>>>(nrow, br, bc, offsets, row_counts, columns,
+                                                                             (const float*)values, (const float*)x,
+                                                                             (float*)y_out, (float)alpha);
+        else if (val_dtype == GB_F64 && vec_dtype == GB_F64)
+            k_bsr_mv_transpose<double, double, double><<<grid, 256, 0, stream>>>(
+                nrow, br, bc, offsets, row_counts, columns, (const double*)values, (const double*)x, (double*)y_out,
+                alpha);
+        else {
+            gb::set_error("bsr_mv transpose: unsupported dtype combination");
+            return GB_ERR_UNSUPPORTED;
+        }
+        GB_CHECK_CUDA(cudaGetLastError());
+        return GB_OK;
+    }
+
+    const bool aligned = ((uintptr_t)columns % 16 == 0) && ((uintptr_t)values % 16 == 0);
+    SpmvShape sh = default_shape(br, bc, val_dtype, nrow, nnz_upper, ncap, aligned);
+    if (rows_per_cta > 0) sh.rows = rows_per_cta;
+    if (lanes_per_row > 0) sh.G = lanes_per_row;
+    if (cap_blocks >= 0 && (rows_per_cta > 0 || cap_blocks > 0)) sh.cap = aligned ? (cap_blocks & ~(SPMV_ALIGN - 1)) : 0;
+    GB_REQUIRE(sh.G >= 1 && sh.G <= 32 && (sh.G & (sh.G - 1)) == 0, "bsr_mv: lanes_per_row must be a power of two <= 32");
+    GB_REQUIRE(sh.rows >= 1 && sh.rows <= 4096, "bsr_mv: rows_per_cta out of range");
+
+    if (br == 1 && bc == 1) {
+        if (val_dtype == GB_F32 && vec_dtype == GB_F32)
+            return launch_mv<1, 1, float, float, float>(nrow, sh, offsets, row_counts, columns, values, x, y_in, y_out, alpha, beta, status, stream);
+        if (val_dtype == GB_BF16 && vec_dtype == GB_F32)
+            return launch_mv<1, 1, __nv_bfloat16, float, float>(nrow, sh, offsets, row_counts, columns, values, x, y_in, y_out, alpha, beta, status, stream);
+        if (val_dtype == GB_F32 && vec_dtype == GB_F64)
+            return launch_mv<1, 1, float, double, double>(nrow, sh, offsets, row_counts, columns, values, x, y_in, y_out, alpha, beta, status, stream);
+        if (val_dtype == GB_F64 && vec_dtype == GB_F64)
+            return launch_mv<1, 1, double, double, double>(nrow, sh, offsets, row_counts, columns, values, x, y_in, y_out, alpha, beta, status, stream);
+    } else if (br == 3 && bc == 3) {
+        if (val_dtype == GB_F32 && vec_dtype == GB_F32)
+            return launch_mv<3, 3, float, float, float>(nrow, sh, offsets, row_counts, columns, values, x, y_in, y_out, alpha, beta, status, stream);
+        if (val_dtype == GB_BF16 && vec_dtype == GB_F32)
+            return launch_mv<3, 3, __nv_bfloat16, float, float>(nrow, sh, offsets, row_counts, columns, values, x, y_in, y_out, alpha, beta, status, stream);
+        if (val_dtype == GB_F32 && vec_dtype == GB_F64)
+            return launch_mv<3, 3, float, double, double>(nrow, sh, offsets, row_counts, columns, values, x, y_in, y_out, alpha, beta, status, stream);
+        if (val_dtype == GB_F64 && vec_dtype == GB_F64)
+            return launch_mv<3, 3, double, double, double>(nrow, sh, offsets, row_counts, columns, values, x, y_in, y_out, alpha, beta, status, stream);
+    }
+    // generic shapes
+    const int grid = (int)ceil_div<int64_t>((int64_t)nrow * br, 256);
+    if (val_dtype == GB_F32 && vec_dtype == GB_F32)
+        k_bsr_mv_generic<float, float, float><<<grid, 256, 0, stream>>>(nrow, br, bc, offsets, row_counts, columns,
+                                                                       (const float*)values, (const float*)x,
+                                                                       (const float*)y_in, (float*)y_out, (float)alpha,
+                                                                       (float)beta);
+    else if (val_dtype == GB_F64 && vec_dtype == GB_F64)
+        k_bsr_mv_generic<double, double, double><<<grid, 256, 0, stream>>>(nrow, br, bc, offsets, row_counts,
+                                                                          columns, (const double*)values,
+                                                                          (const double*)x, (const double*)y_in,
+                                                                          (double*)y_out, alpha, beta);
+    else if (val_dtype == GB_F32 && vec_dtype == GB_F64)
+        k_bsr_mv_generic<float, double, double><<<grid, 256, 0, stream>>>(nrow, br, bc, offsets, row_counts, columns,
+                                                                         (const float*)values, (const double*)x,
+                                                                         (const double*)y_in, (double*)y_out, alpha,
+                                                                         beta);
+    else {
+        gb::set_error("bsr_mv: unsupported dtype combination (values %d, vectors %d)", val_dtype, vec_dtype);
+        return GB_ERR_UNSUPPORTED;
+    }
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+// y -= A x for fp32 1x1 / 3x3 matrices without staging (used by the Dirichlet projection).
+int gb_bsr_mv_internal(int bdim, int nrow, const int* offsets, const int* columns, const float* values,
+                       const float* x, float* y, cudaStream_t stream)
+{
+    SpmvShape sh = default_shape(bdim, bdim, GB_F32, nrow, 0, 0, false);
+    sh.rows = 64;
+    sh.G = 8;
+    sh.cap = 0;
+    if (bdim == 1)
+        return launch_mv<1, 1, float, float, float>(nrow, sh, offsets, nullptr, columns, values, x, y, y, -1.0, 1.0,
+                                                   nullptr, stream);
+    return launch_mv<3, 3, float, float, float>(nrow, sh, offsets, nullptr, columns, values, x, y, y, -1.0, 1.0,
+                                               nullptr, stream);
+}
+
+// Reports the tile shape the heuristic picks (for the autotuner and the roofline accounting).
+GB_API int gb_bsr_mv_default_shape(int block_rows, int block_cols, int val_dtype, int nrow, int64_t nnz,
+                                   int* rows_per_cta, int* lanes_per_row, int* cap_blocks)
+{
+    SpmvShape sh = default_shape(block_rows, block_cols, val_dtype, nrow, nnz, nnz, true);
+    *rows_per_cta = sh.rows;
+    *lanes_per_row = sh.G;
+    *cap_blocks = sh.cap;
+    return GB_OK;
+}

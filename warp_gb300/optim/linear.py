@@ -1,0 +1,630 @@
+"""Iterative linear solvers: the drop-in for ``warp.optim.linear`` on the FEM solve path.
+
+Mirrors ``warp/_src/optim/linear.py``: ``LinearOperator`` (:33), ``aslinearoperator`` (:135),
+``preconditioner`` (:236), ``cg`` (:1035) / ``CG`` (:893), ``bicgstab`` (:1577) / ``BiCGSTAB``
+(:1377), with the same arguments, tolerance rules (:2010-2083) and return conventions:
+
+* ``check_every > 0``: returns ``(iterations, residual_norm, absolute_tolerance)`` (host numbers);
+* ``check_every == 0``: returns device arrays ``(iterations[1], residual_norm_sq[1],
+  atol_sq[1])`` and performs no host synchronisation -- the whole solve is one CUDA graph with a
+  device-side while loop (and may itself be captured by the caller);
+* ``run=False``: returns the pre-allocated solver functor.
+
+BSR operators with 1x1 or 3x3 float32 (or bfloat16-valued) blocks and the Jacobi / identity
+preconditioner take the fused native path of ``libwarp_gb300.so`` (three kernels per CG
+iteration, single-pass grid reductions, conditional-while CUDA graph).  Any other
+``LinearOperator`` (dense, user-defined matvec, batched) runs the generic path, whose vector
+updates and dot products are also library kernels.
+
+Additions beyond the reference: ``solve_refined`` (FP32 Krylov inside FP64 iterative
+refinement, FP64 true residual and solution) and ``fcg`` (flexible CG with a nonlinear
+preconditioner and a Jacobi-CG fallback), used by the learned preconditioner.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import math
+from typing import Callable
+
+import numpy as np
+import torch
+
+from .. import _arrays as A
+from .. import _native as N
+from .. import sparse
+
+__all__ = [
+    "LinearOperator",
+    "aslinearoperator",
+    "preconditioner",
+    "cg",
+    "bicgstab",
+    "CG",
+    "BiCGSTAB",
+    "solve_refined",
+]
+
+
+class LinearOperator:
+    """Linear operator for the iterative solvers (reference: ``linear.py:33-133``).
+
+    ``matvec(x, y, z, alpha, beta)`` computes ``z = alpha * A x + beta * y``.
+    """
+
+    def __init__(self, shape, dtype, device, matvec: Callable, batch_offsets=None, max_batch_length=None):
+        if max_batch_length is not None:
+            if batch_offsets is None:
+                raise ValueError("max_batch_length requires batch_offsets")
+            if max_batch_length < 0:
+                raise ValueError("max_batch_length must be non-negative")
+        self._shape = tuple(shape)
+        self._dtype = dtype
+        self._device = device
+        self._matvec = matvec
+        self._batch_offsets = batch_offsets
+        self._max_batch_length = max_batch_length
+        self._bsr = None  # set for BSR operators (fused path)
+        self._inv_diag = None  # set for Jacobi preconditioners (fused path)
+
+    @property
+    def shape(self):
+        return self._shape
+
+    @property
+    def dtype(self):
+        return self._dtype
+
+    @property
+    def device(self):
+        return self._device
+
+    @property
+    def matvec(self):
+        return self._matvec
+
+    @property
+    def scalar_type(self):
+        return self._dtype
+
+    @property
+    def batch_offsets(self):
+        return self._batch_offsets
+
+    @property
+    def batch_count(self) -> int:
+        return 1 if self._batch_offsets is None else int(self._batch_offsets.shape[0]) - 1
+
+    @property
+    def max_batch_length(self):
+        return self._max_batch_length
+
+
+def _flat(t) -> torch.Tensor:
+    return A.as_tensor(t).reshape(-1)
+
+
+def aslinearoperator(Am, batch_offsets=None, max_batch_length=None) -> LinearOperator | None:
+    """Cast a BSR matrix, dense 2-D array or diagonal 1-D array (reference: ``linear.py:135-233``)."""
+    if Am is None or isinstance(Am, LinearOperator):
+        return Am
+    stream_of = A.stream
+    if isinstance(Am, sparse.BsrMatrix):
+
+        def bsr_mv(x, y, z, alpha, beta):
+            sparse.bsr_mv_into(Am, x, y, z, alpha, beta)
+
+        op = LinearOperator(Am.shape, Am.scalar_type, Am.device, bsr_mv, batch_offsets, max_batch_length)
+        op._bsr = Am
+        return op
+    t = A.as_tensor(Am)
+    if t.dim() == 2:
+        m, n = t.shape
+        tc = t.contiguous()
+
+        def dense_mv(x, y, z, alpha, beta):
+            N.check(N.lib().gb_dense_mv(A.gb_dtype(tc.dtype), m, n, A.ptr(tc), A.ptr(_flat(x)), A.ptr(_flat(y)),
+                                        A.ptr(_flat(z)), float(alpha), float(beta), stream_of()), "dense_mv")
+
+        return LinearOperator(tuple(t.shape), t.dtype, t.device, dense_mv, batch_offsets, max_batch_length)
+    if t.dim() in (1, 2) or t.dim() >= 1:
+        td = t.reshape(-1).contiguous()
+
+        def diag_mv(x, y, z, alpha, beta):
+            N.check(N.lib().gb_diag_mv(A.gb_dtype(td.dtype), td.numel(), A.ptr(td), A.ptr(_flat(x)),
+                                       A.ptr(_flat(y)), A.ptr(_flat(z)), float(alpha), float(beta), stream_of()),
+                    "diag_mv")
+
+        op = LinearOperator((td.numel(), td.numel()), t.dtype, t.device, diag_mv, batch_offsets, max_batch_length)
+        op._inv_diag = td
+        return op
+    raise ValueError(f"Unable to create LinearOperator from {Am}")
+
+
+def preconditioner(Am, ptype: str = "diag") -> LinearOperator | None:
+    """``"diag"`` (Jacobi), ``"diag_abs"`` or ``"id"`` (reference: ``linear.py:236-280``)."""
+    if ptype == "id":
+        return None
+    if ptype not in ("diag", "diag_abs"):
+        raise ValueError(f"Unsupported preconditioner type '{ptype}'")
+    use_abs = 1 if ptype == "diag_abs" else 0
+    if isinstance(Am, sparse.BsrMatrix):
+        br, bc = Am.block_shape
+        if br != bc:
+            raise ValueError("Jacobi preconditioner needs square blocks")
+        dt = Am.scalar_type if Am.scalar_type in (torch.float32, torch.float64) else torch.float32
+        vals = Am.values if Am.values.dtype == dt else Am.values.to(dt)
+        inv = A.empty(Am.nrow * br, dt)
+        N.check(N.lib().gb_bsr_inverse_diagonal(A.gb_dtype(dt), br, Am.nrow, A.ptr(Am.offsets),
+                                                A.ptr(Am.row_counts), A.ptr(Am.columns), A.ptr(vals), use_abs,
+                                                A.ptr(inv), A.stream()), "preconditioner")
+        return aslinearoperator(inv)
+    t = A.as_tensor(Am)
+    if t.dim() == 2:
+        d = torch.diagonal(t).clone()
+        d = d.abs() if use_abs else d
+        inv = torch.where(d == 0, torch.ones_like(d), 1.0 / d)
+        return aslinearoperator(inv.contiguous())
+    raise ValueError("Unsupported source matrix type for building diagonal preconditioner")
+
+
+def refresh_preconditioner(M: LinearOperator, Am, ptype: str = "diag") -> None:
+    """Recompute a Jacobi preconditioner in place after ``Am``'s values changed (same structure)."""
+    inv = M._inv_diag
+    br = Am.block_shape[0]
+    N.check(N.lib().gb_bsr_inverse_diagonal(A.gb_dtype(inv.dtype), br, Am.nrow, A.ptr(Am.offsets),
+                                            A.ptr(Am.row_counts), A.ptr(Am.columns), A.ptr(Am.values),
+                                            1 if ptype == "diag_abs" else 0, A.ptr(inv), A.stream()),
+            "refresh_preconditioner")
+
+
+# -------------------------------------------------------------------------------------------
+# tolerance rules (reference: linear.py:2010-2032)
+# -------------------------------------------------------------------------------------------
+def _dtype_epsilon(dtype) -> float:
+    if dtype == torch.float64:
+        return 1.0e-16
+    if dtype == torch.float16:
+        return 1.0e-4
+    return 1.0e-8
+
+
+def _get_tolerances(dtype, tol, atol):
+    eps = _dtype_epsilon(dtype)
+    default_tol = eps ** (3 / 4)
+    min_tol = eps ** (9 / 4)
+    if tol is None and atol is None:
+        tol = atol = default_tol
+    elif tol is None:
+        tol = atol
+    elif atol is None:
+        atol = tol
+    return tol, max(atol, min_tol)
+
+
+class _DevScalar:
+    """A device scalar exposed through ``__cuda_array_interface__`` (views into solver state)."""
+
+    def __init__(self, ptr: int, typestr: str, keep):
+        self.__cuda_array_interface__ = {"shape": (1,), "typestr": typestr, "data": (ptr, False), "version": 3,
+                                         "strides": None, "stream": None}
+        self._keep = keep
+
+
+# -------------------------------------------------------------------------------------------
+# solver state
+# -------------------------------------------------------------------------------------------
+class LinearSolverState:
+    """Pre-allocated solver (reference: ``linear.py:722-878``)."""
+
+    _kind = None
+
+    def __init__(self, A_, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_every=10,
+                 use_cuda_graph=True):
+        self._A = aslinearoperator(A_)
+        self._M = aslinearoperator(M)
+        self._b = A.as_tensor(b)
+        self._x = A.as_tensor(x)
+        self._tol = tol
+        self._atol = atol
+        self._callback = callback
+        self._check_every = int(check_every)
+        self._use_cuda_graph = bool(use_cuda_graph)
+        self._scalar_type = self._A.scalar_type
+        self._batch_count = self._A.batch_count
+        n = self._b.numel()
+        if maxiter is None or maxiter == 0:
+            maxiter = n // self._batch_count
+        self._maxiter = int(maxiter)
+        self._native = None
+        self._ws = None
+        self._fused = self._fused_eligible(self._A, self._M, self._b, self._x)
+        if self._fused:
+            self._create_native()
+
+    # -- fused path -----------------------------------------------------------------------
+    def _fused_eligible(self, Aop, Mop, b, x) -> bool:
+        bsr = getattr(Aop, "_bsr", None)
+        if bsr is None or Aop.batch_offsets is not None:
+            return False
+        if bsr.block_shape not in ((1, 1), (3, 3)) or bsr.row_counts is not None:
+            return False
+        if bsr.values.dtype not in (torch.float32, torch.bfloat16):
+            return False
+        if b.dtype != torch.float32 or x.dtype != torch.float32 or not b.is_contiguous() or not x.is_contiguous():
+            return False
+        if Mop is not None:
+            inv = getattr(Mop, "_inv_diag", None)
+            if inv is None or inv.dtype != torch.float32 or inv.numel() != b.numel():
+                return False
+        if bsr.columns.data_ptr() % 16 or bsr.values.data_ptr() % 16:
+            return False
+        return True
+
+    def _create_native(self):
+        bsr = self._A._bsr
+        L = N.lib()
+        nnz = bsr.nnz_sync()
+        bdim = bsr.block_shape[0]
+        vdt = A.gb_dtype(bsr.values.dtype)
+        ws_bytes = L.gb_krylov_workspace_bytes(self._kind, bdim, bsr.nrow, nnz, vdt)
+        self._ws = A.zeros(int(ws_bytes), torch.uint8)
+        h = ctypes.c_void_p()
+        N.check(L.gb_krylov_create(self._kind, bdim, bsr.nrow, nnz, bsr.capacity, vdt, 0, 0, 0,
+                                   self._ws.data_ptr(), self._ws.numel(), ctypes.byref(h)), "krylov_create")
+        self._native = h
+        self._native_key = (bsr.nrow, nnz, bdim, vdt)
+        it = ctypes.c_void_p()
+        rr = ctypes.c_void_p()
+        at = ctypes.c_void_p()
+        st = ctypes.c_void_p()
+        N.check(L.gb_krylov_scalars(h, ctypes.byref(it), ctypes.byref(rr), ctypes.byref(at), ctypes.byref(st)))
+        self._dev_iter = torch.as_tensor(_DevScalar(it.value, "<i4", self._ws), device="cuda")
+        self._dev_rr = torch.as_tensor(_DevScalar(rr.value, "<f8", self._ws), device="cuda")
+        self._dev_atol_sq = torch.as_tensor(_DevScalar(at.value, "<f8", self._ws), device="cuda")
+        self._dev_status = torch.as_tensor(_DevScalar(st.value, "<i4", self._ws), device="cuda")
+        self._host_i = torch.zeros(3, dtype=torch.int32, pin_memory=True)
+        self._host_d = torch.zeros(3, dtype=torch.float64, pin_memory=True)
+
+    def __del__(self):
+        try:
+            if self._native is not None:
+                N.lib().gb_krylov_destroy(self._native)
+                self._native = None
+        except Exception:
+            pass
+
+    def _read(self):
+        N.check(N.lib().gb_krylov_read(self._native, self._host_i.data_ptr(), self._host_d.data_ptr(), A.stream()))
+        torch.cuda.current_stream().synchronize()
+        it, cond, status = (int(v) for v in self._host_i.tolist())
+        rr, atol_sq, bb = (float(v) for v in self._host_d.tolist())
+        return it, cond, status, rr, atol_sq
+
+    def _run_fused(self, Aop, b, x, Mop, x_is_zero=False):
+        bsr = Aop._bsr
+        L = N.lib()
+        key = (bsr.nrow, bsr.nnz if bsr._nnz_exact and bsr._nnz_event is None else bsr.nnz_sync(),
+               bsr.block_shape[0], A.gb_dtype(bsr.values.dtype))
+        if key != self._native_key:
+            raise ValueError("operator shape changed since the solver was created")
+        rtol, atol = _get_tolerances(torch.float32, self._tol, self._atol)
+        dinv = None if Mop is None else Mop._inv_diag
+        stream = A.stream()
+        N.check(L.gb_krylov_set_operands(self._native, A.ptr(bsr.offsets), None, A.ptr(bsr.columns),
+                                         A.ptr(bsr.values), A.ptr(dinv), A.ptr(b), A.ptr(x), 1 if x_is_zero else 0,
+                                         float(rtol), float(atol), self._maxiter,
+                                         1 if getattr(self, "_is_left_preconditioner", False) else 0, stream),
+                "krylov_set_operands")
+        self._keep = (b, x, dinv, bsr)
+        if self._check_every == 0:
+            mode = 0 if self._use_cuda_graph else None
+            if mode == 0:
+                N.check(L.gb_krylov_launch(self._native, 0, 0, stream), "krylov_launch")
+            else:
+                N.check(L.gb_krylov_launch(self._native, 4, 0, stream), "krylov_launch")
+                for _ in range(self._maxiter):
+                    N.check(L.gb_krylov_launch(self._native, 3, 0, stream), "krylov_launch")
+            return self._dev_iter, self._dev_rr, self._dev_atol_sq
+        # host-checked loop
+        graph = self._use_cuda_graph
+        N.check(L.gb_krylov_launch(self._native, 1 if graph else 4, 0, stream), "krylov_launch")
+        it, cond, status, rr, atol_sq = self._read()
+        atol_v = math.sqrt(atol_sq)
+        if self._callback is not None:
+            self._callback(0, math.sqrt(rr), atol_v)
+        chunk = max(1, self._check_every)
+        while cond and it < self._maxiter:
+            n = min(chunk, self._maxiter - it)
+            if graph:
+                N.check(L.gb_krylov_launch(self._native, 2, n, stream), "krylov_launch")
+            else:
+                for _ in range(n):
+                    N.check(L.gb_krylov_launch(self._native, 3, 0, stream), "krylov_launch")
+            it, cond, status, rr, atol_sq = self._read()
+            if self._callback is not None:
+                self._callback(it, math.sqrt(rr), atol_v)
+        self.last_status = status
+        return it, math.sqrt(rr), atol_v
+
+    # -- public ---------------------------------------------------------------------------
+    def __call__(self, A_=None, b=None, x=None, M=None):
+        Aop = aslinearoperator(A_) if A_ is not None else self._A
+        Mop = aslinearoperator(M) if M is not None else self._M
+        b_t = A.as_tensor(b) if b is not None else self._b
+        x_t = A.as_tensor(x) if x is not None else self._x
+        if Aop is not self._A and tuple(Aop.shape) != tuple(self._A.shape):
+            raise ValueError(f"Incompatible A.shape: expected {self._A.shape}, got {Aop.shape}")
+        if b_t.shape != self._b.shape:
+            raise ValueError(f"Incompatible b.shape: expected {tuple(self._b.shape)}, got {tuple(b_t.shape)}")
+        if x_t.shape != self._x.shape:
+            raise ValueError(f"Incompatible x.shape: expected {tuple(self._x.shape)}, got {tuple(x_t.shape)}")
+        if self._fused and self._fused_eligible(Aop, Mop, b_t, x_t):
+            return self._run_fused(Aop, b_t, x_t, Mop)
+        return self._run_generic(Aop, b_t.reshape(-1), x_t.reshape(-1), Mop)
+
+    # -- generic path (any LinearOperator) ------------------------------------------------
+    def _dots(self, pairs):
+        L = N.lib()
+        if not hasattr(self, "_dot_ws"):
+            self._dot_ws = A.zeros(int(L.gb_dots_workspace_bytes()), torch.uint8)
+            self._dot_out = A.zeros(4, torch.float64)
+        xs = (ctypes.c_void_p * 4)(*[p[0].data_ptr() for p in pairs])
+        ys = (ctypes.c_void_p * 4)(*[p[1].data_ptr() for p in pairs])
+        dt = A.gb_dtype(pairs[0][0].dtype)
+        N.check(L.gb_dots(dt, pairs[0][0].numel(), len(pairs), xs, ys, self._dot_out.data_ptr(),
+                          self._dot_ws.data_ptr(), A.stream()), "dots")
+        return [float(v) for v in self._dot_out[: len(pairs)].tolist()]
+
+    def _axpby(self, alpha, x, beta, y, out):
+        N.check(N.lib().gb_axpby(A.gb_dtype(x.dtype), x.numel(), float(alpha), x.data_ptr(), float(beta),
+                                 y.data_ptr(), out.data_ptr(), A.stream()), "axpby")
+
+
+class CG(LinearSolverState):
+    """Pre-allocated Conjugate Gradient solver (reference: ``linear.py:893-1032``)."""
+
+    _kind = N.KRYLOV_CG
+
+    def __init__(self, A_, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_every=10,
+                 use_cuda_graph=True, restart=None):
+        if restart is not None:
+            if isinstance(restart, bool) or not isinstance(restart, int):
+                raise TypeError("restart must be an integer or None")
+            if restart < 1:
+                raise ValueError("restart must be positive")
+        self._restart = restart
+        super().__init__(A_, b, x, tol, atol, maxiter, M, callback, check_every, use_cuda_graph)
+        if restart is not None:
+            self._fused = False
+
+    def _run_generic(self, Aop, b, x, Mop):
+        dt = b.dtype
+        rtol, atol = _get_tolerances(dt, self._tol, self._atol)
+        n = b.numel()
+        r = torch.empty_like(b)
+        z = torch.empty_like(b) if Mop is not None else r
+        p = torch.empty_like(b)
+        Ap = torch.zeros_like(b)
+        (bb,) = self._dots([(b, b)])
+        atol_v = max(rtol * math.sqrt(bb), atol)
+        atol_sq = atol_v * atol_v
+        Aop.matvec(x, b, r, -1.0, 1.0)
+        if Mop is not None:
+            Mop.matvec(r, z, z, 1.0, 0.0)
+        rr, rz = self._dots([(r, r), (r, z)])
+        p.copy_(z)
+        it = 0
+        if self._callback is not None and self._check_every > 0:
+            self._callback(0, math.sqrt(rr), atol_v)
+        while not (rr <= atol_sq) and it < self._maxiter:
+            Aop.matvec(p, Ap, Ap, 1.0, 0.0)
+            (pAp,) = self._dots([(p, Ap)])
+            alpha = rz / pAp if (rr > atol_sq and pAp != 0.0) else 0.0
+            self._axpby(alpha, p, 1.0, x, x)
+            self._axpby(-alpha, Ap, 1.0, r, r)
+            if Mop is not None:
+                Mop.matvec(r, z, z, 1.0, 0.0)
+            rz_new, rr = self._dots([(r, z), (r, r)])
+            beta = rz_new / rz if (rr > atol_sq and rz != 0.0) else 0.0
+            self._axpby(1.0, z, beta, p, p)
+            rz = rz_new
+            it += 1
+            if self._restart is not None and it % self._restart == 0:
+                Aop.matvec(x, b, r, -1.0, 1.0)
+                if Mop is not None:
+                    Mop.matvec(r, z, z, 1.0, 0.0)
+                rr, rz = self._dots([(r, r), (r, z)])
+                p.copy_(z)
+            if self._callback is not None and self._check_every > 0 and it % self._check_every == 0:
+                self._callback(it, math.sqrt(rr), atol_v)
+        if self._check_every == 0:
+            return (torch.tensor([it], dtype=torch.int32, device=b.device),
+                    torch.tensor([rr], dtype=torch.float64, device=b.device),
+                    torch.tensor([atol_sq], dtype=torch.float64, device=b.device))
+        return it, math.sqrt(rr), atol_v
+
+
+class BiCGSTAB(LinearSolverState):
+    """Pre-allocated BiCGSTAB solver (reference: ``linear.py:1377-1574``)."""
+
+    _kind = N.KRYLOV_BICGSTAB
+
+    def __init__(self, A_, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_every=10,
+                 use_cuda_graph=True, is_left_preconditioner=False):
+        self._is_left_preconditioner = bool(is_left_preconditioner)
+        super().__init__(A_, b, x, tol, atol, maxiter, M, callback, check_every, use_cuda_graph)
+
+    def _run_generic(self, Aop, b, x, Mop):
+        dt = b.dtype
+        rtol, atol = _get_tolerances(dt, self._tol, self._atol)
+        r = torch.empty_like(b)
+        v = torch.zeros_like(b)
+        t = torch.zeros_like(b)
+        y = torch.zeros_like(b) if Mop is not None else None
+        z = torch.zeros_like(b) if Mop is not None else None
+        (bb,) = self._dots([(b, b)])
+        atol_v = max(rtol * math.sqrt(bb), atol)
+        atol_sq = atol_v * atol_v
+        Aop.matvec(x, b, r, -1.0, 1.0)
+        (rr,) = self._dots([(r, r)])
+        p = r.clone()
+        r0 = r.clone()
+        rho = rr
+        it = 0
+        left = self._is_left_preconditioner
+        while not (rr <= atol_sq) and it < self._maxiter:
+            yv = p
+            if Mop is not None:
+                Mop.matvec(p, y, y, 1.0, 0.0)
+                yv = y
+            Aop.matvec(yv, v, v, 1.0, 0.0)
+            (r0v,) = self._dots([(r0, v)])
+            alpha = rho / r0v if (rr > atol_sq and r0v != 0.0) else 0.0
+            self._axpby(alpha, yv, 1.0, x, x)
+            self._axpby(-alpha, v, 1.0, r, r)
+            (rr,) = self._dots([(r, r)])
+            zv = r
+            if Mop is not None:
+                Mop.matvec(r, z, z, 1.0, 0.0)
+                zv = z
+            Aop.matvec(zv, t, t, 1.0, 0.0)
+            if Mop is not None and left:
+                Mt = torch.empty_like(t)
+                Mop.matvec(t, Mt, Mt, 1.0, 0.0)
+                st, tt = self._dots([(zv, Mt), (Mt, Mt)])
+            else:
+                st, tt = self._dots([(r, t), (t, t)])
+            omega = st / tt if (rr > atol_sq and tt != 0.0) else 0.0
+            self._axpby(omega, zv, 1.0, x, x)
+            self._axpby(-omega, t, 1.0, r, r)
+            rr, rho_new = self._dots([(r, r), (r0, r)])
+            active = rr > atol_sq and r0v != 0.0 and st != 0.0
+            beta = rho_new * tt / (r0v * st) if active else 0.0
+            beta_omega = rho_new / r0v if active else 0.0
+            # p = r + beta p - beta_omega v
+            self._axpby(beta, p, -beta_omega, v, p)
+            self._axpby(1.0, r, 1.0, p, p)
+            rho = rho_new
+            it += 1
+            if self._callback is not None and self._check_every > 0 and it % self._check_every == 0:
+                self._callback(it, math.sqrt(rr), atol_v)
+        if self._check_every == 0:
+            return (torch.tensor([it], dtype=torch.int32, device=b.device),
+                    torch.tensor([rr], dtype=torch.float64, device=b.device),
+                    torch.tensor([atol_sq], dtype=torch.float64, device=b.device))
+        return it, math.sqrt(rr), atol_v
+
+
+def cg(A_, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_every=10, use_cuda_graph=True,
+       run=True, *, restart=None):
+    """Preconditioned Conjugate Gradient (reference: ``linear.py:1035-1121``)."""
+    state = CG(A_, b, x, tol=tol, atol=atol, maxiter=maxiter, M=M, callback=callback, check_every=check_every,
+               use_cuda_graph=use_cuda_graph, restart=restart)
+    if run:
+        return state()
+    return state
+
+
+def bicgstab(A_, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_every=10, use_cuda_graph=True,
+             is_left_preconditioner=False, run=True):
+    """BiCGSTAB (reference: ``linear.py:1577-1650``)."""
+    state = BiCGSTAB(A_, b, x, tol=tol, atol=atol, maxiter=maxiter, M=M, callback=callback,
+                     check_every=check_every, use_cuda_graph=use_cuda_graph,
+                     is_left_preconditioner=is_left_preconditioner)
+    if run:
+        return state()
+    return state
+
+
+# -------------------------------------------------------------------------------------------
+# FP64 iterative refinement around the fused FP32 Krylov solver
+# -------------------------------------------------------------------------------------------
+class RefinedSolver:
+    """Mixed-precision solve: FP32 Jacobi-PCG (or BiCGSTAB) inner loop inside FP64 refinement.
+
+    Each outer step computes the FP64 true residual r = b - A x (fp32 values promoted, fp64
+    accumulation), solves A d = r in FP32 to ``inner_tol`` relative residual with the fused
+    graph solver, and updates x += d in FP64.  Convergence is tested on ||b - A x|| / ||b|| in
+    FP64.  ``values`` may be a bfloat16 copy of the matrix values for the inner loop only.
+    """
+
+    def __init__(self, Am: sparse.BsrMatrix, M: LinearOperator | None = None, method: str = "cg",
+                 inner_tol: float = 1e-4, inner_maxiter: int = 0, inner_values: torch.Tensor | None = None):
+        self.A = Am
+        self.M = M
+        self.n = Am.nrow * Am.block_shape[0]
+        self.inner_tol = float(inner_tol)
+        self.inner_maxiter = int(inner_maxiter) if inner_maxiter else self.n
+        self._r32 = A.zeros(self.n, torch.float32)
+        self._d = A.zeros(self.n, torch.float32)
+        self._inner_A = Am
+        if inner_values is not None:
+            self._inner_A = sparse.BsrMatrix(Am.nrow, Am.ncol, Am.block_shape, inner_values.dtype)
+            self._inner_A.offsets, self._inner_A.columns = Am.offsets, Am.columns
+            self._inner_A.values, self._inner_A.nnz = inner_values, Am.nnz
+        cls = CG if method == "cg" else BiCGSTAB
+        self.inner = cls(self._inner_A, self._r32, self._d, tol=self.inner_tol, atol=0.0,
+                         maxiter=self.inner_maxiter, M=M, check_every=0, use_cuda_graph=True)
+        if not self.inner._fused:
+            raise ValueError("solve_refined needs a BSR operator with 1x1/3x3 float32 blocks and a Jacobi or no "
+                             "preconditioner")
+        L = N.lib()
+        nnz = Am.nnz_sync()
+        self._res_ws = A.zeros(int(L.gb_residual_f64_workspace_bytes(Am.block_shape[0], Am.nrow, nnz,
+                                                                      A.gb_dtype(Am.values.dtype))), torch.uint8)
+        self._norms = A.zeros(2, torch.float64)
+        self._status = A.zeros(1, torch.int32)
+        self._host = torch.zeros(2, dtype=torch.float64, pin_memory=True)
+
+    def residual(self, x64: torch.Tensor, b: torch.Tensor, sync: bool = True):
+        """FP64 true residual; writes the fp32 copy used as the next inner right-hand side."""
+        Am = self.A
+        L = N.lib()
+        N.check(L.gb_residual_f64(Am.block_shape[0], Am.nrow, Am.nnz, Am.capacity, A.ptr(Am.offsets), None,
+                                  A.ptr(Am.columns), A.ptr(Am.values), A.gb_dtype(Am.values.dtype), A.ptr(x64),
+                                  A.ptr(b), None, A.ptr(self._r32), A.ptr(self._norms), self._res_ws.data_ptr(),
+                                  self._res_ws.numel(), A.ptr(self._status), A.stream()), "residual_f64")
+        if not sync:
+            return None
+        self._host.copy_(self._norms, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        rr, bb = self._host.tolist()
+        return math.sqrt(rr), math.sqrt(bb)
+
+    def solve(self, b, x64=None, tol: float = 1e-8, max_outer: int = 50, callback=None):
+        b = A.as_tensor(b).reshape(-1)
+        if b.dtype != torch.float32:
+            raise TypeError("right-hand side must be float32 (the system's scalar type)")
+        x64 = A.zeros(self.n, torch.float64) if x64 is None else A.as_tensor(x64).reshape(-1)
+        L = N.lib()
+        history = []
+        inner_iters = 0
+        rnorm, bnorm = self.residual(x64, b)
+        history.append(rnorm / bnorm if bnorm > 0 else 0.0)
+        outer = 0
+        Aop = self.inner._A
+        while bnorm > 0 and rnorm > tol * bnorm and outer < max_outer:
+            # the correction solve starts from d = 0 (init skips the product: r = b)
+            self._d.zero_()
+            self.inner._run_fused(Aop, self._r32, self._d, self.inner._M, x_is_zero=True)
+            # x64 += d  (the inner solve starts from d = 0 each time: x_is_zero path)
+            N.check(L.gb_axpy_f64_f32(self.n, A.ptr(x64), A.ptr(self._d), 1.0, A.stream()), "axpy_f64_f32")
+            it = int(self.inner._dev_iter.item())
+            inner_iters += it
+            rnorm, _ = self.residual(x64, b)
+            outer += 1
+            history.append(rnorm / bnorm)
+            if callback is not None:
+                callback(outer, it, rnorm / bnorm)
+            if it == 0:
+                break
+        return x64, dict(outer=outer, inner_iterations=inner_iters, rel_residual=history[-1], history=history,
+                         converged=bool(rnorm <= tol * bnorm))
+
+
+def solve_refined(A_: sparse.BsrMatrix, b, x64=None, tol: float = 1e-8, M=None, method: str = "cg",
+                  inner_tol: float = 1e-4, max_outer: int = 50):
+    """FP64-accurate solve of ``A x = b`` with an FP32 Krylov inner loop; returns ``(x64, info)``."""
+    solver = RefinedSolver(A_, M=M, method=method, inner_tol=inner_tol)
+    return solver.solve(b, x64=x64, tol=tol, max_outer=max_outer)
