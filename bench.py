@@ -194,6 +194,35 @@ def run_reference(args):
     return 0
 
 
+def run_profile(args):
+    """Kernel sequences for ncu (launch lists and single-kernel captures) on the bench workload."""
+    import torch
+
+    from warp_gb300 import problems, sparse
+    from warp_gb300.optim import linear
+
+    torch.cuda.set_device(0)
+    system = problems.diffusion(args.res, sigma=1.5, corr_length=0.1, seed=args.seed)
+    A = system.A
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()  # keep the device footprint of the capture small (assembly temporaries)
+    if args.profile == "spmv":
+        x = torch.randn(A.nrow, dtype=torch.float32, device="cuda")
+        y = torch.empty_like(x)
+        for _ in range(8):
+            sparse.bsr_mv(A, x, y)
+    elif args.profile == "cg":
+        x = torch.zeros_like(system.b)
+        linear.cg(A, system.b, x, tol=1e-12, atol=0.0, maxiter=30, M=linear.preconditioner(A, "diag"),
+                  check_every=30, use_cuda_graph=False)
+    else:
+        solver = linear.RefinedSolver(A, M=linear.preconditioner(A, "diag"), inner_tol=args.inner_tol)
+        solver.solve(system.b, tol=1e-8)
+    torch.cuda.synchronize()
+    print("profile run done", flush=True)
+    return 0
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -202,16 +231,22 @@ def main():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--res", type=int, nargs="+", default=[96, 96, 96])
     p.add_argument("--seed", type=int, default=0)
-    p.add_argument("--inner-tol", type=float, default=1e-4)
+    p.add_argument("--inner-tol", type=float, default=1e-5)
     p.add_argument("--mv-launches", type=int, default=50)
     p.add_argument("--ref-iters", type=int, default=50)
     p.add_argument("--ref-full-iters", type=int, default=2000)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--profile", choices=["spmv", "cg", "solve"], default=None,
+                   help="run a fixed kernel sequence for an ncu capture and exit (prints no bench line): "
+                        "spmv = 8 bsr_mv launches, cg = 30 eager (non-graph) Jacobi-CG iterations, "
+                        "solve = one refined solve")
     args = p.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile:
+        return run_profile(args)
 
     import numpy as np
     import torch
@@ -248,11 +283,13 @@ def main():
             torch.distributed.barrier()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        launches0 = solver.kernel_launches
         e0.record(stream)
         for _ in range(args.steps):
             x64, info = solver.solve(system.b, tol=1e-8)
             infos.append(info)
         e1.record(stream)
+        solver.kernel_launches_timed = solver.kernel_launches - launches0
         torch.cuda.synchronize()
         if ws > 1:
             torch.distributed.barrier()
@@ -329,8 +366,8 @@ def main():
 
     inner_iters = [i["inner_iterations"] for i in infos]
     outer = [i["outer"] for i in infos]
-    # per solve: 1 residual + per outer step (argument store, CG init, axpy, residual) + 3 per CG iteration
-    gpu_launches = int(sum(1 + 4 * o + 3 * it for o, it in zip(outer, inner_iters)))
+    # counted by the solver: residuals, argument stores, CG inits, solution updates, 3 per CG iteration
+    gpu_launches = int(solver.kernel_launches_timed)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

@@ -127,6 +127,26 @@ int gb_residual_f64(int block_dim, int nrow, int64_t nnz, int64_t ncap, const in
                     double* r64, float* r32, double* norms, void* workspace, size_t workspace_bytes, int* status,
                     gb_stream_t stream);
 int gb_axpy_f64_f32(int64_t n, double* x, const float* d, double alpha, gb_stream_t stream);
+/* same residual in double-float (two-fp32) arithmetic from the interleaved (hi, lo) split x2 of x */
+int gb_residual_df(int block_dim, int nrow, int64_t nnz, int64_t ncap, const int* offsets, const int* row_counts,
+                   const int* columns, const void* values, int val_dtype, const void* x2, const float* b, double* r64,
+                   float* r32, double* norms, void* workspace, size_t workspace_bytes, int* status,
+                   gb_stream_t stream);
+/* x += alpha * d (d may be null) and refresh the (hi, lo) split x2 (may be null) */
+int gb_update_solution(int64_t n, double* x, void* x2, const float* d, double alpha, gb_stream_t stream);
+
+/* ---- SpGEMM (bsr_mm) on the triplet assembly ----------------------------------------------------
+ * Replace the bsr_mm pipeline (warp/_src/sparse.py:4200-4624, kernels :3620-3917): per block of x
+ * count the product terms, emit (row, col, (x block, y block)) triplets (plus z's blocks when
+ * beta != 0), assemble with gb_bsr_matrix_from_triplets_device, then sum each run. */
+int gb_spgemm_count(int x_nrow, const int* x_offsets, const int* x_columns, const int* y_offsets, int x_nnz_cap,
+                    int* count, gb_stream_t stream);
+int gb_spgemm_emit(int x_nrow, const int* x_offsets, const int* x_columns, const int* y_offsets, const int* y_columns,
+                   int x_nnz_cap, const int* start, int z_nrow, const int* z_offsets, const int* z_columns,
+                   int z_nnz_cap, int z_base, int* rows, int* cols, void* pairs, gb_stream_t stream);
+int gb_spgemm_values(int dtype, int nrow, const int* out_offsets, const int* run_ends, const int* run_ids,
+                     const void* pairs, int br, int bk, int bc, const void* X, const void* Y, const void* Z,
+                     double alpha, double beta, void* out, int nnz_upper, gb_stream_t stream);
 
 /* ---- Q1 FEM assembly on regular grids ------------------------------------------------------------
  * gb_q1_assemble_triplets replaces fem.integrate's bilinear dispatch path for Q1 Grid2D/Grid3D

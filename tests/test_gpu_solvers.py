@@ -50,14 +50,17 @@ def _true_rel_residual(host, x, b):
 @pytest.mark.parametrize("check_every", [10, 0, 1])
 @pytest.mark.parametrize("use_graph", [True, False])
 def test_cg_fused_poisson(cuda, check_every, use_graph):
+    """Fused graph CG vs the oracle's restatement of CG._run on the same system."""
     from warp_gb300.optim import linear
 
     A, host, b = _poisson((24, 20, 16))
     M = linear.preconditioner(A, "diag")
     x = torch.zeros(A.nrow, dtype=torch.float32, device="cuda")
     bd = torch.from_numpy(b).cuda()
-    state = linear.cg(A, bd, x, tol=1e-6, maxiter=2000, M=M, check_every=check_every, use_cuda_graph=use_graph,
-                      run=False)
+    # atol=0: purely relative stopping rule (with atol=None the reference sets atol=tol, an absolute
+    # floor that dominates for this small-norm right-hand side)
+    state = linear.cg(A, bd, x, tol=1e-6, atol=0.0, maxiter=2000, M=M, check_every=check_every,
+                      use_cuda_graph=use_graph, run=False)
     assert state._fused
     out = state()
     if check_every == 0:
@@ -70,9 +73,25 @@ def test_cg_fused_poisson(cuda, check_every, use_graph):
     assert rel <= 32 * 1e-6, rel
     # oracle restatement of the same PCG (fp32 vectors): same iteration count within a few
     _, it_ref, err_ref, atol_ref = oracle.pcg_f32(host[0], host[1], host[2], b,
-                                                  inv_diag=oracle.inverse_diagonal_f32(*host), tol=1e-6,
+                                                  inv_diag=oracle.inverse_diagonal_f32(*host), tol=1e-6, atol=0.0,
                                                   maxiter=2000)
     assert abs(it - it_ref) <= max(3, 0.05 * it_ref), (it, it_ref)
+
+
+def test_cg_tolerance_rule_matches_reference(cuda):
+    """tol only -> atol = tol (absolute floor), as _get_tolerances (linear.py:2018-2032); the fused
+    solver stops exactly where the oracle restatement stops."""
+    from warp_gb300.optim import linear
+
+    A, host, b = _poisson((24, 20, 16))
+    x = torch.zeros(A.nrow, dtype=torch.float32, device="cuda")
+    it, err, atol = linear.cg(A, torch.from_numpy(b).cuda(), x, tol=1e-6, maxiter=2000,
+                              M=linear.preconditioner(A, "diag"), check_every=1)
+    xo, it_o, err_o, atol_o = oracle.pcg_f32(host[0], host[1], host[2], b, inv_diag=oracle.inverse_diagonal_f32(*host),
+                                             tol=1e-6, maxiter=2000)
+    assert atol == pytest.approx(1e-6) and atol_o == pytest.approx(1e-6)
+    assert abs(it - it_o) <= 1
+    np.testing.assert_allclose(x.cpu().numpy(), xo, rtol=1e-3, atol=1e-4 * np.abs(xo).max())
 
 
 def test_cg_capture_whole_solve_in_user_graph(cuda):
@@ -83,7 +102,7 @@ def test_cg_capture_whole_solve_in_user_graph(cuda):
     M = linear.preconditioner(A, "diag")
     x = torch.zeros(A.nrow, dtype=torch.float32, device="cuda")
     bd = torch.from_numpy(b).cuda()
-    state = linear.cg(A, bd, x, tol=1e-6, maxiter=1000, M=M, check_every=0, run=False)
+    state = linear.cg(A, bd, x, tol=1e-6, atol=0.0, maxiter=1000, M=M, check_every=0, run=False)
     g = torch.cuda.CUDAGraph()
     s = torch.cuda.Stream()
     with torch.cuda.stream(s):
@@ -106,7 +125,7 @@ def test_bicgstab_fused_poisson(cuda, left):
     A, host, b = _poisson((20, 18, 14), seed=5)
     M = linear.preconditioner(A, "diag")
     x = torch.zeros(A.nrow, dtype=torch.float32, device="cuda")
-    st = linear.bicgstab(A, torch.from_numpy(b).cuda(), x, tol=1e-6, maxiter=2000, M=M,
+    st = linear.bicgstab(A, torch.from_numpy(b).cuda(), x, tol=1e-6, atol=0.0, maxiter=2000, M=M,
                          is_left_preconditioner=left, run=False)
     assert st._fused
     it, err, atol = st()
@@ -208,3 +227,44 @@ def test_nonfinite_rhs_reports_status(cuda):
     it, err, atol = st()
     assert it == 0
     assert st.last_status & N.DEV_NONFINITE
+
+
+@pytest.mark.parametrize("bs", [1, 3])
+def test_residual_double_float_vs_fp64_oracle(cuda, bs):
+    """The refinement residual in double-float arithmetic matches the FP64 oracle to ~1e-12 of sum|A||x|."""
+    import warp_gb300._native as N
+    from warp_gb300 import sparse
+
+    rng = np.random.default_rng(bs)
+    nrow, n = 4000, 60000
+    rows = rng.integers(0, nrow, n).astype(np.int32)
+    cols = rng.integers(0, nrow, n).astype(np.int32)
+    vals = rng.standard_normal((n, bs, bs)).astype(np.float32)
+    A = sparse.bsr_zeros(nrow, nrow, torch.float32 if bs == 1 else ((3, 3), torch.float32))
+    sparse.bsr_set_from_triplets(A, torch.from_numpy(rows).cuda(), torch.from_numpy(cols).cuda(),
+                                 torch.from_numpy(vals.reshape(n) if bs == 1 else vals).cuda())
+    nnz = A.nnz_sync()
+    x = rng.standard_normal(nrow * bs)
+    b = rng.standard_normal(nrow * bs).astype(np.float32)
+    x64 = torch.from_numpy(x).cuda()
+    x2 = torch.zeros(2 * nrow * bs, dtype=torch.float32, device="cuda")
+    N.check(N.lib().gb_update_solution(nrow * bs, x64.data_ptr(), x2.data_ptr(), None, 0.0,
+                                       torch.cuda.current_stream().cuda_stream))
+    ws = torch.zeros(int(N.lib().gb_residual_f64_workspace_bytes(bs, nrow, nnz, 0)), dtype=torch.uint8, device="cuda")
+    norms = torch.zeros(2, dtype=torch.float64, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    off = A.offsets.cpu().numpy()
+    cs = A.columns[:nnz].cpu().numpy()
+    vs = A.values[:nnz].cpu().numpy()
+    exp = b.astype(np.float64) - oracle.bsr_mv_f64(off, cs, vs, x, block_shape=(bs, bs))
+    scale = oracle.bsr_abs_mv_f64(off, cs, vs, x, block_shape=(bs, bs)) + np.abs(b)
+    for fn, xin in (("gb_residual_df", x2), ("gb_residual_f64", x64)):
+        r64 = torch.zeros(nrow * bs, dtype=torch.float64, device="cuda")
+        N.check(getattr(N.lib(), fn)(bs, nrow, nnz, A.capacity, A.offsets.data_ptr(), None, A.columns.data_ptr(),
+                                     A.values.data_ptr(), N.GB_F32, xin.data_ptr(), torch.from_numpy(b).cuda().data_ptr(),
+                                     r64.data_ptr(), None, norms.data_ptr(), ws.data_ptr(), ws.numel(),
+                                     status.data_ptr(), torch.cuda.current_stream().cuda_stream))
+        err = np.abs(r64.cpu().numpy() - exp)
+        assert np.all(err <= 1e-12 * scale), (fn, float((err / scale).max()))
+        np.testing.assert_allclose(norms[0].item(), np.dot(exp, exp), rtol=1e-5)
+    assert int(status.item()) == 0

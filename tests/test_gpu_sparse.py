@@ -229,3 +229,41 @@ def test_bsr_mv_aliasing_and_transpose(cuda):
     D = oracle.bsr_to_dense(o["offsets"], o["columns"], o["values"], 500)
     yt = sparse.bsr_mv(A, torch.from_numpy(x).cuda(), transpose=True)
     np.testing.assert_allclose(yt.cpu().numpy(), D.T @ x, rtol=1e-4, atol=1e-3)
+
+
+@pytest.mark.parametrize("shapes", [((1, 1), (1, 1)), ((3, 3), (3, 3)), ((2, 3), (3, 1))])
+@pytest.mark.parametrize("alpha,beta", [(1.0, 0.0), (0.5, 2.0)])
+def test_bsr_mm_vs_dense(cuda, shapes, alpha, beta):
+    from warp_gb300 import sparse
+
+    (a, k), (k2, c) = shapes
+    X, ox = _random_bsr(60, 50, 400, (a, k), seed=1)
+    Y, oy = _random_bsr(50, 70, 500, (k2, c), seed=2)
+    Z, oz = _random_bsr(60, 70, 300, (a, c), seed=3)
+    Dx = oracle.bsr_to_dense(ox["offsets"], ox["columns"], ox["values"], 50, (a, k))
+    Dy = oracle.bsr_to_dense(oy["offsets"], oy["columns"], oy["values"], 70, (k2, c))
+    Dz = oracle.bsr_to_dense(oz["offsets"], oz["columns"], oz["values"], 70, (a, c))
+    out = sparse.bsr_mm(X, Y, Z, alpha=alpha, beta=beta)
+    exp = alpha * Dx @ Dy + beta * Dz
+    np.testing.assert_allclose(out.numpy_dense(), exp, rtol=1e-4, atol=1e-4 * np.abs(exp).max())
+    # topology = union of product pattern and z pattern when beta != 0
+    nnz = out.nnz_sync()
+    pat = (np.abs(Dx) > 0).astype(int) @ (np.abs(Dy) > 0).astype(int)
+    if beta != 0:
+        pat = pat + (np.abs(Dz) > 0)
+    blocks = (pat.reshape(60, a, 70, c).sum(axis=(1, 3)) > 0).sum()
+    assert nnz == blocks
+
+
+def test_bsr_mm_diagonal_projector_keeps_structure(cuda):
+    from warp_gb300 import fem, sparse
+
+    geo = fem.Grid3D(res=(5, 4, 3))
+    space = fem.make_polynomial_space(geo, degree=1)
+    A = fem.integrate(fem.diffusion_form, fields={"u": fem.make_trial(space), "v": fem.make_test(space)})
+    bd = fem.BoundarySides(geo)
+    P = fem.integrate(fem.boundary_projector_form, fields={"u": fem.make_trial(space, bd),
+                                                           "v": fem.make_test(space, bd)}, assembly="nodal")
+    D = A.numpy_dense()
+    PA = sparse.bsr_mm(P, A)
+    np.testing.assert_allclose(PA.numpy_dense(), P.numpy_dense() @ D, atol=1e-5)

@@ -13,6 +13,7 @@ from . import _native  # noqa: F401
 from . import sparse  # noqa: F401
 from . import optim  # noqa: F401
 from . import fem  # noqa: F401
+from . import spgemm  # noqa: F401
 
 __version__ = "1.0.0"
 

@@ -59,6 +59,9 @@ _SIGNATURES = {
     "gb_residual_f64": (_c_int, [_c_int, _c_int, _c_i64, _c_i64, _vp, _vp, _vp, _vp, _c_int, _vp, _vp, _vp, _vp,
                                  _vp, _vp, _c_sz, _vp, _vp]),
     "gb_axpy_f64_f32": (_c_int, [_c_i64, _vp, _vp, _c_dbl, _vp]),
+    "gb_residual_df": (_c_int, [_c_int, _c_int, _c_i64, _c_i64, _vp, _vp, _vp, _vp, _c_int, _vp, _vp, _vp, _vp,
+                                _vp, _vp, _c_sz, _vp, _vp]),
+    "gb_update_solution": (_c_int, [_c_i64, _vp, _vp, _vp, _c_dbl, _vp]),
     "gb_bsr_get_diag": (_c_int, [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gb_bsr_inverse_diagonal": (_c_int, [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_int, _vp, _vp]),
     "gb_diag_mv": (_c_int, [_c_int, _c_i64, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _vp]),

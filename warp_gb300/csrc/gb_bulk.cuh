@@ -1,6 +1,7 @@
 // gb_bulk.cuh -- 1-D bulk-copy (TMA, cp.async.bulk) and mbarrier helpers for sm_103a.
 //
-// Every wait is bounded: after kWaitLimit unsuccessful polls the caller gets `false`, ORs
+// Every wait is bounded in time: a non-blocking mbarrier.test_wait is polled with a short sleep
+// against the %globaltimer clock; after kWaitLimitNs the caller gets `false`, ORs
 // GB_DEV_WAIT_TIMEOUT into its status word and drains (again bounded) before returning, so a
 // kernel can never hang the GPU on a barrier.
 #pragma once
@@ -8,7 +9,14 @@
 
 namespace gb {
 
-constexpr uint32_t kWaitLimit = 1u << 24;
+constexpr uint64_t kWaitLimitNs = 100ull * 1000ull * 1000ull;  // 100 ms per wait
+
+__device__ __forceinline__ uint64_t globaltimer_ns()
+{
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p)
 {
@@ -49,19 +57,37 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
     return done != 0;
 }
 
-// Bounded wait on phase `parity`; returns false if the limit was reached.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity)
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity)
 {
-    for (uint32_t it = 0; it < kWaitLimit; ++it)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
 }
 
-// Global -> shared bulk copy completing on `bar` (dst, src 16-byte aligned; bytes % 16 == 0).
+// Wait on phase `parity`, bounded by kWaitLimitNs of wall time; false if the limit was reached.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity)
+{
+    if (mbar_test_wait(bar, parity)) return true;
+    const uint64_t t0 = globaltimer_ns();
+    for (;;) {
+        if (mbar_test_wait(bar, parity)) return true;
+        if (globaltimer_ns() - t0 > kWaitLimitNs) return false;
+        __nanosleep(64);
+    }
+}
+
+// Global -> shared bulk copy (1-D TMA) into this CTA's shared memory, completing on `bar`
+// (dst, src 16-byte aligned; bytes % 16 == 0).
 __device__ __forceinline__ void bulk_g2s(void* dst_smem, const void* src_gmem, uint32_t bytes, uint64_t* bar)
 {
     asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+        "cp.async.bulk.shared::cta.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
             smem_u32(dst_smem)),
         "l"(src_gmem), "r"(bytes), "r"(smem_u32(bar))
         : "memory");

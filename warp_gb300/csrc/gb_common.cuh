@@ -73,12 +73,14 @@ template <int G, typename T> __device__ __forceinline__ T group_sum(T v)
     return v;
 }
 
-// Block-wide sum of NV doubles; result valid in thread 0.  `scratch` holds >= 32*NV doubles.
-template <int NV> __device__ __forceinline__ void block_sum(double (&v)[NV], double* scratch)
+// Block-wide sum of NV values; result valid in thread 0.  `scratch` holds >= 32*NV doubles.
+// Per-warp sums run in the input type (fp32 per-thread partials keep the FP64 pipe, a small
+// fraction of the FP32 rate on GB300, out of the element loops); cross-warp sums in fp64.
+template <int NV, typename T> __device__ __forceinline__ void block_sum(T (&vin)[NV], double* scratch, double (&v)[NV])
 {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
-    for (int k = 0; k < NV; ++k) v[k] = warp_sum(v[k]);
+    for (int k = 0; k < NV; ++k) v[k] = (double)warp_sum(vin[k]);
     __syncthreads();
     if (lane == 0) {
 #pragma unroll
@@ -101,12 +103,13 @@ template <int NV> __device__ __forceinline__ void block_sum(double (&v)[NV], dou
 // same buffers serve every launch of a captured graph.  No CTA ever waits on another.
 // partials: [NV][gridDim.x] doubles; counter: one unsigned int, zero before the first launch.
 // ---------------------------------------------------------------------------------------------
-template <int NV, typename Finish>
-__device__ __forceinline__ void grid_reduce(double (&v)[NV], double* partials, unsigned int* counter,
+template <int NV, typename T, typename Finish>
+__device__ __forceinline__ void grid_reduce(T (&vin)[NV], double* partials, unsigned int* counter,
                                             double* scratch, Finish finish)
 {
     __shared__ bool s_last;
-    block_sum<NV>(v, scratch);
+    double v[NV];
+    block_sum<NV>(vin, scratch, v);
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) partials[(size_t)k * gridDim.x + blockIdx.x] = v[k];
@@ -124,10 +127,11 @@ __device__ __forceinline__ void grid_reduce(double (&v)[NV], double* partials, u
 #pragma unroll
         for (int k = 0; k < NV; ++k) acc[k] += __ldcg(&partials[(size_t)k * gridDim.x + i]);
     }
-    block_sum<NV>(acc, scratch);
+    double tot[NV];
+    block_sum<NV>(acc, scratch, tot);
     if (threadIdx.x == 0) {
         *counter = 0u;
-        finish(acc);
+        finish(tot);
     }
 }
 

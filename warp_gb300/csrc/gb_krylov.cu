@@ -69,7 +69,7 @@ template <int BR, typename AT> struct EpiCgInit {
     const float *b, *dinv;
     float *r, *p;
     AT sign;  // r = b - A x  (sign = -1) or r = b when x is zero (sign = 0)
-    double bb = 0, rr = 0, rz = 0;
+    float bb = 0.f, rr = 0.f, rz = 0.f;
     __device__ __forceinline__ void operator()(int row, const AT (&acc)[BR], int lane_g)
     {
         if (lane_g < BR) {
@@ -79,9 +79,9 @@ template <int BR, typename AT> struct EpiCgInit {
             const float zi = dinv ? dinv[i] * ri : ri;
             r[i] = ri;
             p[i] = zi;
-            bb += (double)bi * bi;
-            rr += (double)ri * ri;
-            rz += (double)ri * zi;
+            bb += bi * bi;
+            rr += ri * ri;
+            rz += ri * zi;
         }
     }
 };
@@ -116,20 +116,12 @@ __global__ __launch_bounds__(SPMV_THREADS) void k_cg_init(const SolveArgs* __res
     const SolveArgs a = *args;
     EpiCgInit<BR, float> epi{a.b, a.dinv, a.r, a.p, -1.0f};
     if (a.x_is_zero) {
-        // r = b: no product needed; same epilogue with a zero accumulator.
-        const int r0 = blockIdx.x * sh.rows, nr = min(sh.rows, nrow - r0);
-        const int lane_g = threadIdx.x & (sh.G - 1);
-        for (int k = threadIdx.x / sh.G; k < nr; k += blockDim.x / sh.G) {
-            float acc[BR];
-#pragma unroll
-            for (int q = 0; q < BR; ++q) acc[q] = 0.f;
-            epi(r0 + k, acc, lane_g);
-        }
+        rows_run<BR, float>(nrow, sh, epi);  // r = b: no product needed
     } else {
-        spmv_tile<BR, BR, VT, float, float>(nrow, sh, a.offsets, a.row_counts, a.columns, (const VT*)a.values, a.x,
-                                            smem, &a.S->status, epi);
+        spmv_run<BR, BR, VT, float, float>(nrow, sh, a.offsets, a.row_counts, a.columns, (const VT*)a.values, a.x,
+                                           smem, &a.S->status, epi);
     }
-    double v[3] = {epi.bb, epi.rr, epi.rz};
+    float v[3] = {epi.bb, epi.rr, epi.rz};
     grid_reduce<3>(v, a.partials, &a.S->counters[0], s_red,
                    [&](const double (&t)[3]) { cg_init_finish(a, t, h, has_cond); });
 }
@@ -137,14 +129,14 @@ __global__ __launch_bounds__(SPMV_THREADS) void k_cg_init(const SolveArgs* __res
 template <int BR, typename AT> struct EpiCgAp {
     float* Ap;
     const float* p;
-    double pAp = 0;
+    float pAp = 0.f;
     __device__ __forceinline__ void operator()(int row, const AT (&acc)[BR], int lane_g)
     {
         if (lane_g < BR) {
             const size_t i = (size_t)row * BR + lane_g;
             const float ap = pick<BR>(acc, lane_g);
             Ap[i] = ap;
-            pAp += (double)p[i] * ap;
+            pAp += p[i] * ap;
         }
     }
 };
@@ -158,9 +150,9 @@ __global__ __launch_bounds__(SPMV_THREADS) void k_cg_spmv(const SolveArgs* __res
     KrylovScalars* S = a.S;
     if (!S->cond) return;
     EpiCgAp<BR, float> epi{a.Ap, a.p};
-    spmv_tile<BR, BR, VT, float, float>(nrow, sh, a.offsets, a.row_counts, a.columns, (const VT*)a.values, a.p, smem,
+    spmv_run<BR, BR, VT, float, float>(nrow, sh, a.offsets, a.row_counts, a.columns, (const VT*)a.values, a.p, smem,
                                         &S->status, epi);
-    double v[1] = {epi.pAp};
+    float v[1] = {epi.pAp};
     grid_reduce<1>(v, a.partials, &S->counters[1], s_red, [&](const double (&t)[1]) {
         S->pAp = t[0];
         double alpha = 0.0;
@@ -187,7 +179,7 @@ __global__ __launch_bounds__(VEC_THREADS) void k_cg_update(const SolveArgs* __re
     const int64_t n = a.n;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    double rr = 0.0, rz = 0.0;
+    float rr = 0.f, rz = 0.f;
     const bool vec4 = ((((uintptr_t)a.x | (uintptr_t)a.r | (uintptr_t)a.p | (uintptr_t)a.Ap |
                          (uintptr_t)(a.dinv ? a.dinv : a.r)) & 15) == 0);
     int64_t done = 0;
@@ -210,8 +202,8 @@ __global__ __launch_bounds__(VEC_THREADS) void k_cg_update(const SolveArgs* __re
             }
             x4[i] = xv;
             r4[i] = rv;
-            rr += (double)rv.x * rv.x + (double)rv.y * rv.y + (double)rv.z * rv.z + (double)rv.w * rv.w;
-            rz += (double)rv.x * zv.x + (double)rv.y * zv.y + (double)rv.z * zv.z + (double)rv.w * zv.w;
+            rr += rv.x * rv.x + rv.y * rv.y + rv.z * rv.z + rv.w * rv.w;
+            rz += rv.x * zv.x + rv.y * zv.y + rv.z * zv.z + rv.w * zv.w;
         }
         done = n4 << 2;
     }
@@ -221,10 +213,10 @@ __global__ __launch_bounds__(VEC_THREADS) void k_cg_update(const SolveArgs* __re
         const float zi = a.dinv ? a.dinv[i] * ri : ri;
         a.x[i] = xi;
         a.r[i] = ri;
-        rr += (double)ri * ri;
-        rz += (double)ri * zi;
+        rr += ri * ri;
+        rz += ri * zi;
     }
-    double v[2] = {rr, rz};
+    float v[2] = {rr, rz};
     grid_reduce<2>(v, a.partials, &S->counters[2], s_red, [&](const double (&t)[2]) {
         const double rz_old = S->rz;
         S->rr = t[0];
@@ -290,7 +282,7 @@ template <int BR, typename AT> struct EpiBiInit {
     const float *b, *dinv;
     float *r, *r0, *p, *y;
     AT sign;
-    double bb = 0, rr = 0;
+    float bb = 0.f, rr = 0.f;
     __device__ __forceinline__ void operator()(int row, const AT (&acc)[BR], int lane_g)
     {
         if (lane_g < BR) {
@@ -301,8 +293,8 @@ template <int BR, typename AT> struct EpiBiInit {
             r0[i] = ri;
             p[i] = ri;
             y[i] = dinv ? dinv[i] * ri : ri;
-            bb += (double)bi * bi;
-            rr += (double)ri * ri;
+            bb += bi * bi;
+            rr += ri * ri;
         }
     }
 };
@@ -316,19 +308,12 @@ __global__ __launch_bounds__(SPMV_THREADS) void k_bi_init(const SolveArgs* __res
     const SolveArgs a = *args;
     EpiBiInit<BR, float> epi{a.b, a.dinv, a.r, a.r0, a.p, a.y, -1.0f};
     if (a.x_is_zero) {
-        const int r0 = blockIdx.x * sh.rows, nr = min(sh.rows, nrow - r0);
-        const int lane_g = threadIdx.x & (sh.G - 1);
-        for (int k = threadIdx.x / sh.G; k < nr; k += blockDim.x / sh.G) {
-            float acc[BR];
-#pragma unroll
-            for (int q = 0; q < BR; ++q) acc[q] = 0.f;
-            epi(r0 + k, acc, lane_g);
-        }
+        rows_run<BR, float>(nrow, sh, epi);
     } else {
-        spmv_tile<BR, BR, VT, float, float>(nrow, sh, a.offsets, a.row_counts, a.columns, (const VT*)a.values, a.x,
-                                            smem, &a.S->status, epi);
+        spmv_run<BR, BR, VT, float, float>(nrow, sh, a.offsets, a.row_counts, a.columns, (const VT*)a.values, a.x,
+                                           smem, &a.S->status, epi);
     }
-    double v[2] = {epi.bb, epi.rr};
+    float v[2] = {epi.bb, epi.rr};
     grid_reduce<2>(v, a.partials, &a.S->counters[0], s_red, [&](const double (&t)[2]) {
         KrylovScalars* S = a.S;
         const double at = fmax(a.tol * sqrt(t[0]), a.atol);
@@ -351,14 +336,14 @@ __global__ __launch_bounds__(SPMV_THREADS) void k_bi_init(const SolveArgs* __res
 template <int BR, typename AT> struct EpiBiV {
     float* v;
     const float* r0;
-    double r0v = 0;
+    float r0v = 0.f;
     __device__ __forceinline__ void operator()(int row, const AT (&acc)[BR], int lane_g)
     {
         if (lane_g < BR) {
             const size_t i = (size_t)row * BR + lane_g;
             const float vi = pick<BR>(acc, lane_g);
             v[i] = vi;
-            r0v += (double)r0[i] * vi;
+            r0v += r0[i] * vi;
         }
     }
 };
@@ -373,9 +358,9 @@ __global__ __launch_bounds__(SPMV_THREADS) void k_bi_spmv_v(const SolveArgs* __r
     KrylovScalars* S = a.S;
     if (!S->cond) return;
     EpiBiV<BR, float> epi{a.v, a.r0};
-    spmv_tile<BR, BR, VT, float, float>(nrow, sh, a.offsets, a.row_counts, a.columns, (const VT*)a.values, a.y, smem,
+    spmv_run<BR, BR, VT, float, float>(nrow, sh, a.offsets, a.row_counts, a.columns, (const VT*)a.values, a.y, smem,
                                         &S->status, epi);
-    double v[1] = {epi.r0v};
+    float v[1] = {epi.r0v};
     grid_reduce<1>(v, a.partials, &S->counters[1], s_red, [&](const double (&t)[1]) {
         S->r0v = t[0];
         double alpha = 0.0;
@@ -399,15 +384,15 @@ __global__ __launch_bounds__(VEC_THREADS) void k_bi_update1(const SolveArgs* __r
     if (!S->cond) return;
     const float alpha = (float)S->alpha;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    double rr = 0.0;
+    float rr = 0.f;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
         a.x[i] += alpha * a.y[i];
         const float ri = a.r[i] - alpha * a.v[i];
         a.r[i] = ri;
         a.z[i] = a.dinv ? a.dinv[i] * ri : ri;
-        rr += (double)ri * ri;
+        rr += ri * ri;
     }
-    double v[1] = {rr};
+    float v[1] = {rr};
     grid_reduce<1>(v, a.partials, &S->counters[2], s_red, [&](const double (&t)[1]) { S->rr = t[0]; });
 }
 
@@ -416,7 +401,7 @@ template <int BR, typename AT> struct EpiBiT {
     float* t;
     const float *r, *z, *dinv;
     int left;
-    double st = 0, tt = 0;
+    float st = 0.f, tt = 0.f;
     __device__ __forceinline__ void operator()(int row, const AT (&acc)[BR], int lane_g)
     {
         if (lane_g < BR) {
@@ -425,11 +410,11 @@ template <int BR, typename AT> struct EpiBiT {
             t[i] = ti;
             if (left) {
                 const float mt = dinv ? dinv[i] * ti : ti;
-                st += (double)z[i] * mt;
-                tt += (double)mt * mt;
+                st += z[i] * mt;
+                tt += mt * mt;
             } else {
-                st += (double)r[i] * ti;
-                tt += (double)ti * ti;
+                st += r[i] * ti;
+                tt += ti * ti;
             }
         }
     }
@@ -445,9 +430,9 @@ __global__ __launch_bounds__(SPMV_THREADS) void k_bi_spmv_t(const SolveArgs* __r
     KrylovScalars* S = a.S;
     if (!S->cond) return;
     EpiBiT<BR, float> epi{a.t, a.r, a.z, a.dinv, a.left_precond};
-    spmv_tile<BR, BR, VT, float, float>(nrow, sh, a.offsets, a.row_counts, a.columns, (const VT*)a.values, a.z, smem,
+    spmv_run<BR, BR, VT, float, float>(nrow, sh, a.offsets, a.row_counts, a.columns, (const VT*)a.values, a.z, smem,
                                         &S->status, epi);
-    double v[2] = {epi.st, epi.tt};
+    float v[2] = {epi.st, epi.tt};
     grid_reduce<2>(v, a.partials, &S->counters[3], s_red, [&](const double (&t)[2]) {
         S->st = t[0];
         S->tt = t[1];
@@ -473,15 +458,15 @@ __global__ __launch_bounds__(VEC_THREADS) void k_bi_update2(const SolveArgs* __r
     if (!S->cond) return;
     const float omega = (float)S->omega;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    double rr = 0.0, rho = 0.0;
+    float rr = 0.f, rho = 0.f;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
         a.x[i] += omega * a.z[i];
         const float ri = a.r[i] - omega * a.t[i];
         a.r[i] = ri;
-        rr += (double)ri * ri;
-        rho += (double)a.r0[i] * ri;
+        rr += ri * ri;
+        rho += a.r0[i] * ri;
     }
-    double v[2] = {rr, rho};
+    float v[2] = {rr, rho};
     grid_reduce<2>(v, a.partials, &S->counters[4], s_red, [&](const double (&t)[2]) {
         S->rr = t[0];
         const bool active = t[0] > S->atol_sq;
@@ -714,11 +699,9 @@ using namespace gb;
 
 GB_API size_t gb_krylov_workspace_bytes(int kind, int block_dim, int nrow, int64_t nnz, int val_dtype)
 {
-    SpmvShape sh = default_shape(block_dim, block_dim, val_dtype, nrow, nnz, nnz, true);
     const int64_t n = (int64_t)nrow * block_dim;
-    const int spmv_grid = ceil_div(std::max(nrow, 1), sh.rows);
-    const int vec_grid = kSmCount * 4;
-    return ws_layout(kind, n, spmv_grid, vec_grid).total;
+    const int grid = std::max(sm_count(), kSmCount) * 4;  // upper bound of both persistent grids
+    return ws_layout(kind, n, grid, grid).total;
 }
 
 // Creates a solver handle for a BSR system with block_dim x block_dim blocks (1 or 3) and values
@@ -747,14 +730,21 @@ GB_API int gb_krylov_create(int kind, int block_dim, int nrow, int64_t nnz, int6
     if (lanes_per_row > 0) s->sh.G = lanes_per_row;
     if (cap_blocks > 0) s->sh.cap = cap_blocks & ~(SPMV_ALIGN - 1);
     s->sh.ncap = ncap;
-    s->spmv_grid = ceil_div(nrow, s->sh.rows);
-    s->vec_grid = kSmCount * 4;
+    s->sh.rows = std::max(4, (s->sh.rows + 3) & ~3);
     s->spmv_smem = (block_dim == 1)
-                       ? (val_dtype == GB_BF16 ? spmv_smem_bytes<1, 1, __nv_bfloat16>(s->sh.rows, s->sh.cap)
-                                               : spmv_smem_bytes<1, 1, float>(s->sh.rows, s->sh.cap))
-                       : (val_dtype == GB_BF16 ? spmv_smem_bytes<3, 3, __nv_bfloat16>(s->sh.rows, s->sh.cap)
-                                               : spmv_smem_bytes<3, 3, float>(s->sh.rows, s->sh.cap));
-    WsLayout L = ws_layout(kind, s->n, s->spmv_grid, s->vec_grid);
+                       ? (val_dtype == GB_BF16 ? spmv_smem_bytes<1, 1, __nv_bfloat16>(s->sh.rows, s->sh.cap, s->sh.stages)
+                                               : spmv_smem_bytes<1, 1, float>(s->sh.rows, s->sh.cap, s->sh.stages))
+                       : (val_dtype == GB_BF16 ? spmv_smem_bytes<3, 3, __nv_bfloat16>(s->sh.rows, s->sh.cap, s->sh.stages)
+                                               : spmv_smem_bytes<3, 3, float>(s->sh.rows, s->sh.cap, s->sh.stages));
+    if (s->spmv_smem > 227 * 1024) {
+        gb::set_error("krylov: tile shape needs %zu bytes of shared memory", s->spmv_smem);
+        delete s;
+        return GB_ERR_INVALID;
+    }
+    finalize_shape(s->sh, nrow, s->spmv_smem, nullptr);  // offsets alignment is set per operand
+    s->spmv_grid = s->sh.grid;
+    s->vec_grid = sm_count() * 4;
+    WsLayout L = ws_layout(kind, s->n, std::max(sm_count(), kSmCount) * 4, std::max(sm_count(), kSmCount) * 4);
     if (workspace_bytes < L.total) {
         gb::set_error("krylov: workspace too small (%zu < %zu)", workspace_bytes, L.total);
         delete s;
@@ -844,6 +834,16 @@ GB_API int gb_krylov_set_operands(void* handle, const int* offsets, const int* r
     if (!aligned && s->sh.cap != 0) {
         gb::set_error("krylov_set_operands: columns/values must be 16-byte aligned");
         return GB_ERR_INVALID;
+    }
+    const int off_bulk = ((uintptr_t)offsets % 16 == 0) ? 1 : 0;
+    if (off_bulk != s->sh.off_bulk) {
+        // the shape is baked into the cached graphs: rebuild them for the new alignment
+        s->sh.off_bulk = off_bulk;
+        if (s->exec_while) cudaGraphExecDestroy(s->exec_while);
+        if (s->exec_init) cudaGraphExecDestroy(s->exec_init);
+        if (s->exec_chunk) cudaGraphExecDestroy(s->exec_chunk);
+        s->exec_while = s->exec_init = s->exec_chunk = nullptr;
+        s->chunk_iters = 0;
     }
     k_store_args<<<1, 1, 0, stream>>>(s->d_args, s->host, 1);
     GB_CHECK_CUDA(cudaGetLastError());

@@ -103,13 +103,13 @@ template <typename T>
 __global__ void k_dots(int64_t n, int ncols, DotPtrs P, double* partials, unsigned int* counter, double* out)
 {
     __shared__ double s_red[32 * 4];
-    double acc[4] = {0, 0, 0, 0};
+    T acc[4] = {T(0), T(0), T(0), T(0)};  // per-thread partials in T, fp64 across warps
     for (int k = 0; k < ncols; ++k) {
         const T* x = static_cast<const T*>(P.x[k]);
         const T* y = static_cast<const T*>(P.y[k]);
-        double a = 0.0;
+        T a = T(0);
         for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-            a += (double)x[i] * (double)y[i];
+            a += x[i] * y[i];
         acc[k] = a;
     }
     grid_reduce<4>(acc, partials, counter, s_red, [&](const double (&t)[4]) {

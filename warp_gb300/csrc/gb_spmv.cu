@@ -33,7 +33,7 @@ __global__ __launch_bounds__(SPMV_THREADS) void k_bsr_mv(int nrow, SpmvShape sh,
 {
     extern __shared__ __align__(16) unsigned char smem[];
     EpiAxpby<BR, XT, AT> epi{y_out, y_in, alpha, beta};
-    spmv_tile<BR, BC, VT, XT, AT>(nrow, sh, offsets, row_counts, columns, values, x, smem, status, epi);
+    spmv_run<BR, BC, VT, XT, AT>(nrow, sh, offsets, row_counts, columns, values, x, smem, status, epi);
 }
 
 // alpha == 0: y_out = beta * y_in without reading A or x (reference semantics, sparse.py:4649).
@@ -90,38 +90,78 @@ static int launch_mv(int nrow, SpmvShape sh, const int* offsets, const int* row_
                      const void* values, const void* x, const void* y_in, void* y_out, double alpha, double beta,
                      int* status, cudaStream_t stream)
 {
-    const size_t smem = spmv_smem_bytes<BR, BC, VT>(sh.rows, sh.cap);
+    const size_t smem = spmv_smem_bytes<BR, BC, VT>(sh.rows, sh.cap, sh.stages);
+    finalize_shape(sh, nrow, smem, offsets);
     auto kern = k_bsr_mv<BR, BC, VT, XT, AT>;
     if (smem > 48 * 1024) GB_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int grid = ceil_div(nrow, sh.rows);
-    kern<<<grid, SPMV_THREADS, smem, stream>>>(nrow, sh, offsets, row_counts, columns, (const VT*)values,
+    kern<<<sh.grid, SPMV_THREADS, smem, stream>>>(nrow, sh, offsets, row_counts, columns, (const VT*)values,
                                                (const XT*)x, (const XT*)y_in, (XT*)y_out, (AT)alpha, (AT)beta, status);
     GB_CHECK_CUDA(cudaGetLastError());
     return GB_OK;
 }
 
-// Default tile shape (the autotuner in warp_gb300.tuning may override it per matrix).
+int sm_count()
+{
+    static int count = 0;
+    if (count == 0) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || count <= 0)
+            count = kSmCount;
+    }
+    return count;
+}
+
+// Default tile shape (the autotuner in warp_gb300.tuning may override it per matrix): G lanes per
+// block row so that each lane handles ~3-4 blocks; tiles of ~24-32 KB of staged data; 3 stages.
 SpmvShape default_shape(int br, int bc, int val_dtype, int nrow, int64_t nnzb, int64_t ncap, bool aligned)
 {
     SpmvShape sh;
     const double avg = nrow > 0 ? (double)nnzb / (double)nrow : 0.0;
     const int bb = br * bc;
     const int vbytes = (val_dtype == GB_F64) ? 8 : (val_dtype == GB_BF16 ? 2 : 4);
-    // lanes per row: about 3-4 blocks per lane
-    int G = 1;
-    while (G < 32 && G * 4 < avg) G <<= 1;
-    if (br > 1 && G < 4) G = 4;
+    // lanes per block row: scalar blocks use one thread per row (8-deep predicated gather
+    // batches, no shuffles) up to ~48 blocks per row; larger blocks use 8 lanes (4-block batches)
+    int G;
+    if (bb == 1) {
+        G = 1;
+        while (G < 32 && avg > 48.0 * G) G <<= 1;
+    } else {
+        G = 8;
+        while (G < 32 && avg > 8.0 * G) G <<= 1;
+    }
     sh.G = G;
-    // rows per CTA so that a tile stages ~24-40 KB
-    const double bytes_per_row = avg * (4.0 + bb * vbytes);
-    int rows = 256 / G;
-    while (rows * 2 <= 1024 && (rows * 2) * bytes_per_row <= 28 * 1024) rows *= 2;
+    const double bytes_per_row = std::max(avg, 1.0) * (4.0 + bb * vbytes);
+    // one row per lane group (SPMV_CONSUMERS / G rows), shrunk while a tile stages > 104 KB so a
+    // 2-deep ring fits the 227 KB a CTA may use (one 17-warp CTA per SM, ~200 KB of copies in flight)
+    int rows = std::max(4, SPMV_CONSUMERS / G);
+    while (rows > 4 && rows * bytes_per_row * 1.05 > 104 * 1024) rows >>= 1;
+    // keep every lane busy: at least one group per row of the tile
+    while (G < 32 && rows * G < SPMV_CONSUMERS) G <<= 1;
+    sh.G = G;
     sh.rows = rows;
-    int cap = (int)(avg * rows * 1.25) + 2 * SPMV_ALIGN + 16;
+    int cap = (int)(avg * rows * 1.05) + 2 * SPMV_ALIGN + 16;
     cap = (cap + SPMV_ALIGN - 1) & ~(SPMV_ALIGN - 1);
     sh.cap = aligned ? cap : 0;
+    const size_t stage = align16((size_t)(rows + 8) * 4) + align16((size_t)cap * 4) + align16((size_t)cap * bb * vbytes);
+    sh.stages = (3 * stage <= 220 * 1024) ? 3 : 2;
+    sh.grid = 0;
+    sh.off_bulk = 0;
     sh.ncap = ncap;
     return sh;
+}
+
+void finalize_shape(SpmvShape& sh, int nrow, size_t smem_bytes, const int* offsets)
+{
+    sh.rows = std::max(4, (sh.rows + 3) & ~3);
+    sh.cap = std::max(0, sh.cap & ~(SPMV_ALIGN - 1));
+    sh.stages = std::min(std::max(sh.stages, 1), SPMV_MAX_STAGES);
+    sh.off_bulk = ((uintptr_t)offsets % 16 == 0) ? 1 : 0;
+    const int ntiles = std::max(1, ceil_div(nrow, sh.rows));
+    int per_sm = (int)std::max<size_t>(1, (size_t)(227 * 1024) / std::max<size_t>(smem_bytes + 1024, 1));
+    per_sm = std::min(per_sm, 2048 / SPMV_THREADS);
+    per_sm = std::min(per_sm, 4);
+    sh.grid = std::min(ntiles, sm_count() * per_sm);
 }
 
 }  // namespace gb
@@ -181,6 +221,14 @@ GB_API int gb_bsr_mv(int block_rows, int block_cols, int nrow, int ncol, int64_t
     if (cap_blocks >= 0 && (rows_per_cta > 0 || cap_blocks > 0)) sh.cap = aligned ? (cap_blocks & ~(SPMV_ALIGN - 1)) : 0;
     GB_REQUIRE(sh.G >= 1 && sh.G <= 32 && (sh.G & (sh.G - 1)) == 0, "bsr_mv: lanes_per_row must be a power of two <= 32");
     GB_REQUIRE(sh.rows >= 1 && sh.rows <= 4096, "bsr_mv: rows_per_cta out of range");
+    {
+        const int vb = (val_dtype == GB_F64) ? 8 : (val_dtype == GB_BF16 ? 2 : 4);
+        const size_t stage = align16((size_t)(sh.rows + 8) * 4) + align16((size_t)sh.cap * 4) +
+                             align16((size_t)sh.cap * br * bc * vb);
+        // ring of up to 3 stages within the 227 KB per-CTA limit
+        sh.stages = (int)std::min<size_t>((size_t)sh.stages, (227 * 1024 - 256) / std::max<size_t>(stage, 1));
+        GB_REQUIRE(sh.stages >= 1, "bsr_mv: tile does not fit shared memory (rows %d, cap %d)", sh.rows, sh.cap);
+    }
 
     if (br == 1 && bc == 1) {
         if (val_dtype == GB_F32 && vec_dtype == GB_F32)
@@ -234,6 +282,7 @@ int gb_bsr_mv_internal(int bdim, int nrow, const int* offsets, const int* column
     sh.rows = 64;
     sh.G = 8;
     sh.cap = 0;
+    sh.stages = 1;
     if (bdim == 1)
         return launch_mv<1, 1, float, float, float>(nrow, sh, offsets, nullptr, columns, values, x, y, y, -1.0, 1.0,
                                                    nullptr, stream);
@@ -246,6 +295,7 @@ GB_API int gb_bsr_mv_default_shape(int block_rows, int block_cols, int val_dtype
                                    int* rows_per_cta, int* lanes_per_row, int* cap_blocks)
 {
     SpmvShape sh = default_shape(block_rows, block_cols, val_dtype, nrow, nnz, nnz, true);
+    sh.rows = std::max(4, (sh.rows + 3) & ~3);
     *rows_per_cta = sh.rows;
     *lanes_per_row = sh.G;
     *cap_blocks = sh.cap;
