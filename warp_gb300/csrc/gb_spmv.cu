@@ -120,24 +120,23 @@ SpmvShape default_shape(int br, int bc, int val_dtype, int nrow, int64_t nnzb, i
     const double avg = nrow > 0 ? (double)nnzb / (double)nrow : 0.0;
     const int bb = br * bc;
     const int vbytes = (val_dtype == GB_F64) ? 8 : (val_dtype == GB_BF16 ? 2 : 4);
-    // lanes per block row: scalar blocks use one thread per row (8-deep predicated gather
-    // batches, no shuffles) up to ~48 blocks per row; larger blocks use 8 lanes (4-block batches)
-    int G;
-    if (bb == 1) {
-        G = 1;
-        while (G < 32 && avg > 48.0 * G) G <<= 1;
-    } else {
-        G = 8;
-        while (G < 32 && avg > 8.0 * G) G <<= 1;
-    }
-    sh.G = G;
+    // Tile shapes measured on GB300 (sweep over lanes per row x rows per tile on the 96^3 Q1
+    // scalar and 64^3 Q1 vector matrices): scalar blocks run best with ~28 KB tiles (two CTAs of
+    // 17 warps per SM, 3-deep rings) and 4 lanes per row; 3x3 blocks with 8 lanes per block row
+    // and ~70 KB tiles (one CTA per SM).  Long rows get more lanes (<= 8 blocks per lane).
+    int G, rows;
     const double bytes_per_row = std::max(avg, 1.0) * (4.0 + bb * vbytes);
-    // one row per lane group (SPMV_CONSUMERS / G rows), shrunk while a tile stages > 104 KB so a
-    // 2-deep ring fits the 227 KB a CTA may use (one 17-warp CTA per SM, ~200 KB of copies in flight)
-    int rows = std::max(4, SPMV_CONSUMERS / G);
-    while (rows > 4 && rows * bytes_per_row * 1.05 > 104 * 1024) rows >>= 1;
-    // keep every lane busy: at least one group per row of the tile
-    while (G < 32 && rows * G < SPMV_CONSUMERS) G <<= 1;
+    if (bb == 1) {
+        rows = 128;
+        while (rows > 4 && rows * bytes_per_row * 1.05 > 36 * 1024) rows >>= 1;
+        G = std::max(1, SPMV_CONSUMERS / rows);
+    } else {
+        rows = 64;
+        while (rows > 4 && rows * bytes_per_row * 1.05 > 104 * 1024) rows >>= 1;
+        G = std::max(8, SPMV_CONSUMERS / (rows * 2));
+    }
+    while (G < 32 && avg > 8.0 * G) G <<= 1;
+    G = std::min(G, 32);
     sh.G = G;
     sh.rows = rows;
     int cap = (int)(avg * rows * 1.05) + 2 * SPMV_ALIGN + 16;
