@@ -43,6 +43,14 @@ size_t gb_scan_i32_workspace_bytes(int64_t n);
 int gb_scan_i32(const int* in, int* out, int64_t n, int inclusive, void* workspace, size_t workspace_bytes,
                 gb_stream_t stream);
 
+/* Allocation-free variant of gb_scan_i32 (no counterpart in the reference): for callers that must
+ * not allocate device memory (a host arena owning all device memory, or offsets built during a
+ * stream capture).  Its scratch is a fixed ~256 KB device array inside the library, shared by all
+ * calls: n <= gb_scan_i32_noalloc_max_n() (2^28) or GB_ERR_CAPACITY; calls that overlap on the GPU
+ * race on the array; the first call on a device looks the array up (make it outside a capture). */
+int64_t gb_scan_i32_noalloc_max_n(void);
+int gb_scan_i32_noalloc(const int* in, int* out, int64_t n, int inclusive, gb_stream_t stream);
+
 /* ---- triplets -> BSR -------------------------------------------------------------------------
  * gb_bsr_matrix_from_triplets_device replaces wp_bsr_matrix_from_triplets_device
  * (warp/native/warp.h:583-602; warp/native/sparse.cu:1168-1325): same arguments and semantics

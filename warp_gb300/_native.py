@@ -32,6 +32,8 @@ _SIGNATURES = {
     "gb_device_arch": (_c_int, []),
     "gb_scan_i32_workspace_bytes": (_c_sz, [_c_i64]),
     "gb_scan_i32": (_c_int, [_vp, _vp, _c_i64, _c_int, _vp, _c_sz, _vp]),
+    "gb_scan_i32_noalloc_max_n": (_c_i64, []),
+    "gb_scan_i32_noalloc": (_c_int, [_vp, _vp, _c_i64, _c_int, _vp]),
     "gb_bsr_from_triplets_workspace_bytes": (_c_sz, [_c_int, _c_int, _c_int]),
     "gb_bsr_matrix_from_triplets_device": (
         _c_int,
