@@ -297,6 +297,29 @@ def main():
     ms = _barrier_max(ms, ws)
     clocks = sampler.summary()
 
+    # ---- flexible CG with the multigrid preconditioner (set-up timed separately) -------------
+    from warp_gb300 import multigrid
+
+    torch.cuda.synchronize()
+    s0 = time.perf_counter()
+    mg = multigrid.MultigridPreconditioner(A, system.geo, system.coef)
+    fsolver = linear.RefinedSolver(A, M=mg, method="fcg", inner_tol=args.inner_tol)
+    torch.cuda.synchronize()
+    mg_setup_ms = (time.perf_counter() - s0) * 1e3
+    for _ in range(args.warmup):
+        fsolver.solve(system.b, tol=1e-8)
+    torch.cuda.synchronize()
+    finfos = []
+    with ClockSampler(local) as fsampler:
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(args.steps):
+            _, finfo = fsolver.solve(system.b, tol=1e-8)
+            finfos.append(finfo)
+        f1.record(stream)
+        torch.cuda.synchronize()
+    fcg_ms = _barrier_max(f0.elapsed_time(f1) / args.steps, ws)
+
     # ---- SpMV roofline (dominant kernel) -----------------------------------------------------
     hbm_peak, peak_kind = _peaks()
     x = torch.randn(n, dtype=torch.float32, device="cuda")
@@ -397,6 +420,12 @@ def main():
         "gpu_launches": gpu_launches,
         "clocks": clocks,
         "jacobi_cg_ms": ms,
+        "mg_fcg_ms": fcg_ms,
+        "mg_fcg_iterations": statistics.median([f["inner_iterations"] for f in finfos]),
+        "mg_fcg_rel_residual": max(f["rel_residual"] for f in finfos),
+        "mg_fcg_fallbacks": fsolver.fallbacks,
+        "mg_setup_ms": mg_setup_ms,
+        "mg_levels": mg.describe(),
         "bsr_mv_gbs": mv_gbs,
         "inner_iterations": statistics.median(inner_iters),
         "outer_iterations": statistics.median(outer),

@@ -13,7 +13,10 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "libwarp_gb300.so")
 
 GB_F32, GB_F64, GB_BF16, GB_F16 = 0, 1, 2, 3
-KRYLOV_CG, KRYLOV_BICGSTAB = 0, 1
+KRYLOV_CG, KRYLOV_BICGSTAB, KRYLOV_FCG = 0, 1, 2
+
+# z = M(r) callback of the flexible solver: (user, stream, r, z) -> status
+PRECOND_FN = ctypes.CFUNCTYPE(ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p)
 
 # device status bits
 DEV_WAIT_TIMEOUT = 1
@@ -64,6 +67,13 @@ _SIGNATURES = {
     "gb_residual_df": (_c_int, [_c_int, _c_int, _c_i64, _c_i64, _vp, _vp, _vp, _vp, _c_int, _vp, _vp, _vp, _vp,
                                 _vp, _vp, _c_sz, _vp, _vp]),
     "gb_update_solution": (_c_int, [_c_i64, _vp, _vp, _vp, _c_dbl, _vp]),
+    "gb_krylov_set_precond": (_c_int, [_vp, _vp, _vp, _c_int, _c_dbl]),
+    "gb_bsr_jacobi_smooth": (_c_int, [_c_int, _c_int, _c_i64, _c_i64, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_float,
+                                      _vp, _vp, _vp]),
+    "gb_mg_restrict": (_c_int, [_c_int] * 6 + [_vp, _vp, _vp, _vp, _vp]),
+    "gb_mg_prolong_add": (_c_int, [_c_int] * 6 + [_vp, _vp, ctypes.c_float, _vp, _vp]),
+    "gb_mg_jacobi0": (_c_int, [_c_i64, ctypes.c_float, _vp, _vp, _vp, _vp]),
+    "gb_mg_coarsen_cells": (_c_int, [_c_int, _c_int, _c_int, _vp, _vp, _vp]),
     "gb_bsr_get_diag": (_c_int, [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gb_bsr_inverse_diagonal": (_c_int, [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_int, _vp, _vp]),
     "gb_diag_mv": (_c_int, [_c_int, _c_i64, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _vp]),

@@ -24,11 +24,16 @@
 
 namespace gb {
 
-enum KrylovKind : int { KRYLOV_CG = 0, KRYLOV_BICGSTAB = 1 };
+enum KrylovKind : int { KRYLOV_CG = 0, KRYLOV_BICGSTAB = 1, KRYLOV_FCG = 2 };
+
+// Preconditioner callback of the flexible solver: enqueue z = M(r) on `stream` (called while a
+// graph is being captured, or eagerly); returns 0 on success.
+typedef int (*gb_precond_fn)(void* user, cudaStream_t stream, const float* r, float* z);
 
 struct KrylovScalars {
     double bb, atol_sq, rr, rz, pAp, alpha, beta;
     double rho, r0v, st, tt, omega, beta_omega;
+    double rr_ref;  // residual^2 at the start of the current stagnation window
     int iter, cond, maxiter, status;
     unsigned int counters[8];
 };
@@ -49,6 +54,8 @@ struct SolveArgs {
     int maxiter;
     int x_is_zero;
     int left_precond;
+    int stag_window;     // > 0: every stag_window iterations require rr <= stag_factor^2 * rr_ref
+    double stag_factor;  // (flexible solver; a failure sets GB_DEV_STAGNATION and stops the loop)
     int64_t n;  // scalar dofs
 };
 
@@ -99,6 +106,7 @@ __device__ __forceinline__ void cg_init_finish(const SolveArgs& a, const double 
     S->iter = 0;
     S->maxiter = a.maxiter;
     S->alpha = S->beta = 0.0;
+    S->rr_ref = t[1];
     int cond = (t[1] > S->atol_sq) && (a.maxiter > 0);
     if (!finite(t[1])) {
         S->status |= GB_DEV_NONFINITE;
@@ -235,6 +243,13 @@ __global__ __launch_bounds__(VEC_THREADS) void k_cg_update(const SolveArgs* __re
         if (!finite(t[0])) {
             S->status |= GB_DEV_NONFINITE;
             cond = 0;
+        }
+        if (a.stag_window > 0 && cond && (S->iter % a.stag_window) == 0) {
+            if (S->iter > a.stag_window && t[0] > a.stag_factor * a.stag_factor * S->rr_ref) {
+                S->status |= GB_DEV_STAGNATION;
+                cond = 0;
+            }
+            S->rr_ref = t[0];
         }
         set_cond(S, cond, h, has_cond);
     });
@@ -507,6 +522,51 @@ __global__ __launch_bounds__(VEC_THREADS) void k_bi_pupdate(const SolveArgs* __r
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// Flexible CG (FCG(1): each direction is A-orthogonalised against the previous one only)
+//   z = M(r) (callback);  beta = -(z.Ap_prev)/(p_prev.Ap_prev);  p = z + beta p;
+//   Ap = A p, alpha = (z.r)/(p.Ap) (k_cg_spmv);  x += alpha p, r -= alpha Ap (k_cg_update).
+// ---------------------------------------------------------------------------------------------
+__global__ __launch_bounds__(VEC_THREADS) void k_fcg_dir(const SolveArgs* __restrict__ args,
+                                                         cudaGraphConditionalHandle h, int has_cond)
+{
+    __shared__ double s_red[32 * 2];
+    const SolveArgs a = *args;
+    KrylovScalars* S = a.S;
+    if (!S->cond) return;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    float zr = 0.f, zap = 0.f;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+        const float zi = a.z[i];
+        zr += zi * a.r[i];
+        zap += zi * a.Ap[i];
+    }
+    float v[2] = {zr, zap};
+    grid_reduce<2>(v, a.partials, &S->counters[5], s_red, [&](const double (&t)[2]) {
+        S->rz = t[0];
+        double beta = 0.0;
+        if (S->iter > 0 && S->pAp != 0.0) beta = -t[1] / S->pAp;
+        if (!finite(t[0]) || !finite(beta) || t[0] <= 0.0) {
+            // the preconditioned residual is not a descent direction: hand over to the fallback
+            S->status |= (t[0] <= 0.0 && finite(t[0])) ? GB_DEV_STAGNATION : GB_DEV_BREAKDOWN;
+            set_cond(S, 0, h, has_cond);
+            beta = 0.0;
+        }
+        S->beta = beta;
+    });
+}
+
+__global__ __launch_bounds__(VEC_THREADS) void k_fcg_p(const SolveArgs* __restrict__ args)
+{
+    const SolveArgs a = *args;
+    KrylovScalars* S = a.S;
+    if (!S->cond) return;
+    const float beta = (float)S->beta;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride)
+        a.p[i] = a.z[i] + beta * a.p[i];
+}
+
 __global__ void k_store_args(SolveArgs* dst, SolveArgs src, int reset_status)
 {
     *dst = src;
@@ -531,6 +591,8 @@ struct Solver {
     cudaStream_t cap_stream = nullptr;
     cudaGraphExec_t exec_while = nullptr, exec_init = nullptr, exec_chunk = nullptr;
     int chunk_iters = 0;
+    gb_precond_fn precond = nullptr;  // flexible solver only
+    void* precond_user = nullptr;
 };
 
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -548,7 +610,7 @@ static WsLayout ws_layout(int kind, int64_t n, int spmv_grid, int vec_grid)
     L.scalars = align256(sizeof(KrylovScalars));
     L.partials = align256(sizeof(double) * 3 * (size_t)std::max(spmv_grid, vec_grid));
     L.vec = align256(sizeof(float) * (size_t)n);
-    L.nvec = (kind == KRYLOV_CG) ? 3 : 7;  // CG: r p Ap ; BiCGSTAB: r r0 p v t y z
+    L.nvec = (kind == KRYLOV_CG) ? 3 : (kind == KRYLOV_FCG ? 4 : 7);  // CG: r p Ap; FCG: + z; BiCGSTAB: 7
     L.total = L.args + L.scalars + L.partials + L.nvec * L.vec + 256;
     return L;
 }
@@ -567,7 +629,7 @@ template <int BR, typename VT> static void set_smem_attr(Solver* s)
 template <int BR, typename VT>
 static int launch_init_t(Solver* s, cudaStream_t st, cudaGraphConditionalHandle h, int has_cond)
 {
-    if (s->kind == KRYLOV_CG)
+    if (s->kind == KRYLOV_CG || s->kind == KRYLOV_FCG)
         k_cg_init<BR, VT><<<s->spmv_grid, SPMV_THREADS, s->spmv_smem, st>>>(s->d_args, s->nrow, s->sh, h, has_cond);
     else
         k_bi_init<BR, VT><<<s->spmv_grid, SPMV_THREADS, s->spmv_smem, st>>>(s->d_args, s->nrow, s->sh, h, has_cond);
@@ -578,7 +640,20 @@ static int launch_init_t(Solver* s, cudaStream_t st, cudaGraphConditionalHandle 
 template <int BR, typename VT>
 static int launch_iter_t(Solver* s, cudaStream_t st, cudaGraphConditionalHandle h, int has_cond)
 {
-    if (s->kind == KRYLOV_CG) {
+    if (s->kind == KRYLOV_FCG) {
+        if (!s->precond) {
+            gb::set_error("flexible solver: no preconditioner set");
+            return GB_ERR_INVALID;
+        }
+        if (s->precond(s->precond_user, st, s->host.r, s->host.z) != 0) {
+            gb::set_error("flexible solver: preconditioner callback failed");
+            return GB_ERR_INVALID;
+        }
+        k_fcg_dir<<<s->vec_grid, VEC_THREADS, 0, st>>>(s->d_args, h, has_cond);
+        k_fcg_p<<<s->vec_grid, VEC_THREADS, 0, st>>>(s->d_args);
+        k_cg_spmv<BR, VT><<<s->spmv_grid, SPMV_THREADS, s->spmv_smem, st>>>(s->d_args, s->nrow, s->sh);
+        k_cg_update<<<s->vec_grid, VEC_THREADS, 0, st>>>(s->d_args, h, has_cond);
+    } else if (s->kind == KRYLOV_CG) {
         k_cg_spmv<BR, VT><<<s->spmv_grid, SPMV_THREADS, s->spmv_smem, st>>>(s->d_args, s->nrow, s->sh);
         k_cg_update<<<s->vec_grid, VEC_THREADS, 0, st>>>(s->d_args, h, has_cond);
         k_cg_pupdate<<<s->vec_grid, VEC_THREADS, 0, st>>>(s->d_args);
@@ -711,7 +786,8 @@ GB_API int gb_krylov_create(int kind, int block_dim, int nrow, int64_t nnz, int6
                             int rows_per_cta, int lanes_per_row, int cap_blocks, void* workspace,
                             size_t workspace_bytes, void** handle_out)
 {
-    GB_REQUIRE(kind == KRYLOV_CG || kind == KRYLOV_BICGSTAB, "krylov: unknown solver kind %d", kind);
+    GB_REQUIRE(kind == KRYLOV_CG || kind == KRYLOV_BICGSTAB || kind == KRYLOV_FCG, "krylov: unknown solver kind %d",
+               kind);
     GB_REQUIRE(block_dim == 1 || block_dim == 3, "krylov: block_dim must be 1 or 3");
     GB_REQUIRE(val_dtype == GB_F32 || val_dtype == GB_BF16, "krylov: values must be float32 or bfloat16");
     GB_REQUIRE(nrow > 0 && handle_out && workspace, "krylov: bad arguments");
@@ -763,10 +839,11 @@ GB_API int gb_krylov_create(int kind, int block_dim, int nrow, int64_t nnz, int6
         vecs[k] = reinterpret_cast<float*>(ws);
         ws += L.vec;
     }
-    if (kind == KRYLOV_CG) {
+    if (kind == KRYLOV_CG || kind == KRYLOV_FCG) {
         s->host.r = vecs[0];
         s->host.p = vecs[1];
         s->host.Ap = vecs[2];
+        if (kind == KRYLOV_FCG) s->host.z = vecs[3];
     } else {
         s->host.r = vecs[0];
         s->host.r0 = vecs[1];
@@ -822,7 +899,7 @@ GB_API int gb_krylov_set_operands(void* handle, const int* offsets, const int* r
     s->host.row_counts = row_counts;
     s->host.columns = columns;
     s->host.values = values;
-    s->host.dinv = dinv;
+    s->host.dinv = (s->kind == KRYLOV_FCG) ? nullptr : dinv;
     s->host.b = b;
     s->host.x = x;
     s->host.x_is_zero = x_is_zero;
@@ -916,6 +993,26 @@ GB_API int gb_krylov_vectors(void* handle, float** r, float** p, float** Ap)
     GB_REQUIRE(s, "krylov_vectors: null handle");
     if (r) *r = s->host.r;
     if (p) *p = s->host.p;
-    if (Ap) *Ap = s->kind == KRYLOV_CG ? s->host.Ap : s->host.v;
+    if (Ap) *Ap = (s->kind == KRYLOV_BICGSTAB) ? s->host.v : s->host.Ap;
+    return GB_OK;
+}
+
+// Flexible solver: set the preconditioner callback (called with the solver's r and z vectors
+// whenever an iteration is enqueued -- at graph capture time for the cached graphs) and the
+// stagnation rule (window > 0: every `window` iterations the residual norm must have dropped by
+// at least `factor`, else GB_DEV_STAGNATION stops the loop).  Drops any cached graphs.
+GB_API int gb_krylov_set_precond(void* handle, gb_precond_fn fn, void* user, int stag_window, double stag_factor)
+{
+    Solver* s = static_cast<Solver*>(handle);
+    GB_REQUIRE(s && s->kind == KRYLOV_FCG, "krylov_set_precond: flexible solver handle required");
+    s->precond = fn;
+    s->precond_user = user;
+    s->host.stag_window = stag_window;
+    s->host.stag_factor = stag_factor;
+    if (s->exec_while) cudaGraphExecDestroy(s->exec_while);
+    if (s->exec_init) cudaGraphExecDestroy(s->exec_init);
+    if (s->exec_chunk) cudaGraphExecDestroy(s->exec_chunk);
+    s->exec_while = s->exec_init = s->exec_chunk = nullptr;
+    s->chunk_iters = 0;
     return GB_OK;
 }

@@ -1,0 +1,150 @@
+// gb_mg.cu -- geometric multigrid pieces for the flexible-CG preconditioner on Q1 grids.
+//
+// No reference counterpart: Warp's solvers offer only the Jacobi preconditioner
+// (warp/_src/optim/linear.py:236-329).  These kernels build the hierarchy that carries the
+// learned preconditioner: vertex-centred 2:1 coarsening of Q1 node grids (fine node 2I is coarse
+// node I), trilinear prolongation P and its transpose R = P^T (full weighting), damped Jacobi
+// steps, and the per-cell coefficient coarsening used to rediscretise the coarse operators
+// (for a coefficient constant on coarse cells the rediscretised Q1 operator equals the Galerkin
+// product P^T A P, since coarse Q1 functions are fine Q1 functions).  Dirichlet nodes are masked:
+// their restricted residuals are zeroed and prolongation never writes them.
+#include "gb_common.cuh"
+
+namespace gb {
+
+struct NodeGrid {
+    int nx, ny, nz;  // nodes per axis (cells + 1)
+};
+
+__device__ __forceinline__ int64_t nidx(const NodeGrid& g, int x, int y, int z)
+{
+    return ((int64_t)x * g.ny + y) * g.nz + z;
+}
+
+// rc[I] = mask_c[I] * sum_{d in {-1,0,1}^3} w(d) r[2I + d],  w = prod (1 if d=0 else 1/2); fine
+// nodes outside the grid or masked (Dirichlet) contribute nothing.
+__global__ void k_restrict_fw(NodeGrid fg, NodeGrid cg, const float* __restrict__ r, const float* __restrict__ fmask,
+                              const float* __restrict__ cmask, float* __restrict__ rc)
+{
+    const int64_t n = (int64_t)cg.nx * cg.ny * cg.nz;
+    const int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= n) return;
+    const int X = (int)(I / ((int64_t)cg.ny * cg.nz));
+    const int Y = (int)((I / cg.nz) % cg.ny);
+    const int Z = (int)(I % cg.nz);
+    if (cmask && cmask[I] != 0.f) {
+        rc[I] = 0.f;
+        return;
+    }
+    float s = 0.f;
+    for (int dx = -1; dx <= 1; ++dx) {
+        const int x = 2 * X + dx;
+        if (x < 0 || x >= fg.nx) continue;
+        const float wx = dx == 0 ? 1.f : 0.5f;
+        for (int dy = -1; dy <= 1; ++dy) {
+            const int y = 2 * Y + dy;
+            if (y < 0 || y >= fg.ny) continue;
+            const float wy = dy == 0 ? 1.f : 0.5f;
+            for (int dz = -1; dz <= 1; ++dz) {
+                const int z = 2 * Z + dz;
+                if (z < 0 || z >= fg.nz) continue;
+                const int64_t i = nidx(fg, x, y, z);
+                if (fmask && fmask[i] != 0.f) continue;
+                s += wx * wy * (dz == 0 ? 1.f : 0.5f) * r[i];
+            }
+        }
+    }
+    rc[I] = s;
+}
+
+// z[i] += scale * sum_parents w * zc[parent]   (trilinear interpolation; masked fine nodes kept)
+__global__ void k_prolong_add(NodeGrid fg, NodeGrid cg, const float* __restrict__ zc, const float* __restrict__ fmask,
+                              float scale, float* __restrict__ z)
+{
+    const int64_t n = (int64_t)fg.nx * fg.ny * fg.nz;
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    if (fmask && fmask[i] != 0.f) return;
+    const int x = (int)(i / ((int64_t)fg.ny * fg.nz));
+    const int y = (int)((i / fg.nz) % fg.ny);
+    const int zz = (int)(i % fg.nz);
+    const int x0 = x >> 1, x1 = (x + 1) >> 1, y0 = y >> 1, y1 = (y + 1) >> 1, z0 = zz >> 1, z1 = (zz + 1) >> 1;
+    const float wx = (x & 1) ? 0.5f : 1.f, wy = (y & 1) ? 0.5f : 1.f, wz = (zz & 1) ? 0.5f : 1.f;
+    float s = 0.f;
+    const int xs[2] = {x0, x1}, ys[2] = {y0, y1}, zs[2] = {z0, z1};
+    const int nxp = (x & 1) ? 2 : 1, nyp = (y & 1) ? 2 : 1, nzp = (zz & 1) ? 2 : 1;
+    for (int a = 0; a < nxp; ++a)
+        for (int b = 0; b < nyp; ++b)
+            for (int c = 0; c < nzp; ++c) s += zc[nidx(cg, xs[a], ys[b], zs[c])];
+    z[i] += scale * wx * wy * wz * s;
+}
+
+// z = omega * dinv * r   (first damped Jacobi step from z = 0)
+__global__ void k_jacobi0(int64_t n, float omega, const float* __restrict__ dinv, const float* __restrict__ r,
+                          float* __restrict__ z)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        z[i] = omega * dinv[i] * r[i];
+}
+
+// cell coefficient of coarse cell (X,Y,Z) = exp(mean log of its 2x2x2 fine cells)
+__global__ void k_coarsen_cells(int fx, int fy, int fz, const float* __restrict__ a, float* __restrict__ ac)
+{
+    const int cx = fx / 2, cy = fy / 2, cz = fz / 2;
+    const int64_t n = (int64_t)cx * cy * cz;
+    const int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (I >= n) return;
+    const int X = (int)(I / ((int64_t)cy * cz));
+    const int Y = (int)((I / cz) % cy);
+    const int Z = (int)(I % cz);
+    float s = 0.f;
+    for (int d = 0; d < 8; ++d) {
+        const int x = 2 * X + (d >> 2), y = 2 * Y + ((d >> 1) & 1), z = 2 * Z + (d & 1);
+        s += logf(a[((int64_t)x * fy + y) * fz + z]);
+    }
+    ac[I] = expf(s * 0.125f);
+}
+
+static int grid1(int64_t n) { return (int)std::max<int64_t>(1, ceil_div<int64_t>(n, 256)); }
+
+}  // namespace gb
+
+using namespace gb;
+
+// Multigrid transfer and smoothing kernels (no reference counterpart; see the file comment).
+// Node grids are given as nodes per axis.  Masks (1 = Dirichlet node) may be null.
+GB_API int gb_mg_restrict(int fnx, int fny, int fnz, int cnx, int cny, int cnz, const float* r, const float* fmask,
+                          const float* cmask, float* rc, cudaStream_t stream)
+{
+    GB_REQUIRE(cnx == (fnx + 1) / 2 && cny == (fny + 1) / 2 && cnz == (fnz + 1) / 2, "mg_restrict: grid mismatch");
+    NodeGrid fg{fnx, fny, fnz}, cg{cnx, cny, cnz};
+    k_restrict_fw<<<grid1((int64_t)cnx * cny * cnz), 256, 0, stream>>>(fg, cg, r, fmask, cmask, rc);
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+GB_API int gb_mg_prolong_add(int fnx, int fny, int fnz, int cnx, int cny, int cnz, const float* zc,
+                             const float* fmask, float scale, float* z, cudaStream_t stream)
+{
+    GB_REQUIRE(cnx == (fnx + 1) / 2 && cny == (fny + 1) / 2 && cnz == (fnz + 1) / 2, "mg_prolong: grid mismatch");
+    NodeGrid fg{fnx, fny, fnz}, cg{cnx, cny, cnz};
+    k_prolong_add<<<grid1((int64_t)fnx * fny * fnz), 256, 0, stream>>>(fg, cg, zc, fmask, scale, z);
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+GB_API int gb_mg_jacobi0(int64_t n, float omega, const float* dinv, const float* r, float* z, cudaStream_t stream)
+{
+    if (n <= 0) return GB_OK;
+    k_jacobi0<<<(int)std::min<int64_t>(grid1(n), kSmCount * 8), 256, 0, stream>>>(n, omega, dinv, r, z);
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+GB_API int gb_mg_coarsen_cells(int fx, int fy, int fz, const float* a, float* ac, cudaStream_t stream)
+{
+    GB_REQUIRE(fx % 2 == 0 && fy % 2 == 0 && fz % 2 == 0, "mg_coarsen_cells: cell counts must be even");
+    k_coarsen_cells<<<grid1((int64_t)(fx / 2) * (fy / 2) * (fz / 2)), 256, 0, stream>>>(fx, fy, fz, a, ac);
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}

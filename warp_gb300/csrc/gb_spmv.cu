@@ -36,6 +36,32 @@ __global__ __launch_bounds__(SPMV_THREADS) void k_bsr_mv(int nrow, SpmvShape sh,
     spmv_run<BR, BC, VT, XT, AT>(nrow, sh, offsets, row_counts, columns, values, x, smem, status, epi);
 }
 
+// z_out = z + omega * dinv * (r - A z): one damped Jacobi step fused with its residual product
+template <int BR> struct EpiSmooth {
+    const float *z, *r, *dinv;
+    float omega;
+    float* z_out;
+    __device__ __forceinline__ void operator()(int row, const float (&acc)[BR], int lane_g)
+    {
+        if (lane_g < BR) {
+            const size_t i = (size_t)row * BR + lane_g;
+            z_out[i] = z[i] + omega * dinv[i] * (r[i] - pick<BR>(acc, lane_g));
+        }
+    }
+};
+
+template <int BR, typename VT>
+__global__ __launch_bounds__(SPMV_THREADS) void k_bsr_smooth(int nrow, SpmvShape sh, const int* __restrict__ offsets,
+                                                             const int* __restrict__ columns,
+                                                             const VT* __restrict__ values, const float* z,
+                                                             const float* r, const float* dinv, float omega,
+                                                             float* z_out, int* status)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    EpiSmooth<BR> epi{z, r, dinv, omega, z_out};
+    spmv_run<BR, BR, VT, float, float>(nrow, sh, offsets, nullptr, columns, values, z, smem, status, epi);
+}
+
 // alpha == 0: y_out = beta * y_in without reading A or x (reference semantics, sparse.py:4649).
 template <typename XT, typename AT>
 __global__ void k_scale(int64_t n, const XT* y_in, XT* y_out, AT beta)
@@ -287,6 +313,36 @@ int gb_bsr_mv_internal(int bdim, int nrow, const int* offsets, const int* column
                                                    nullptr, stream);
     return launch_mv<3, 3, float, float, float>(nrow, sh, offsets, nullptr, columns, values, x, y, y, -1.0, 1.0,
                                                nullptr, stream);
+}
+
+// One damped Jacobi step fused with its residual product: z_out = z + omega * D^-1 (r - A z)
+// (no reference counterpart; the multigrid smoother of the flexible-CG preconditioner).
+// z_out must not alias z.  fp32 values/vectors, 1x1 or 3x3 blocks.
+GB_API int gb_bsr_jacobi_smooth(int bdim, int nrow, int64_t nnz, int64_t ncap, const int* offsets, const int* columns,
+                                const float* values, const float* r, const float* z, const float* dinv, float omega,
+                                float* z_out, int* status, cudaStream_t stream)
+{
+    GB_REQUIRE(bdim == 1 || bdim == 3, "jacobi_smooth: block dim must be 1 or 3");
+    GB_REQUIRE(nrow > 0 && offsets && columns && values && r && z && dinv && z_out && z_out != z,
+               "jacobi_smooth: bad arguments");
+    const bool aligned = ((uintptr_t)columns % 16 == 0) && ((uintptr_t)values % 16 == 0);
+    SpmvShape sh = default_shape(bdim, bdim, GB_F32, nrow, nnz, ncap, aligned);
+    size_t smem = (bdim == 1) ? spmv_smem_bytes<1, 1, float>(sh.rows, sh.cap, sh.stages)
+                              : spmv_smem_bytes<3, 3, float>(sh.rows, sh.cap, sh.stages);
+    finalize_shape(sh, nrow, smem, offsets);
+    if (bdim == 1) {
+        if (smem > 48 * 1024)
+            GB_CHECK_CUDA(cudaFuncSetAttribute(k_bsr_smooth<1, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_bsr_smooth<1, float><<<sh.grid, SPMV_THREADS, smem, stream>>>(nrow, sh, offsets, columns, values, z, r, dinv,
+                                                                      omega, z_out, status);
+    } else {
+        if (smem > 48 * 1024)
+            GB_CHECK_CUDA(cudaFuncSetAttribute(k_bsr_smooth<3, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_bsr_smooth<3, float><<<sh.grid, SPMV_THREADS, smem, stream>>>(nrow, sh, offsets, columns, values, z, r, dinv,
+                                                                      omega, z_out, status);
+    }
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
 }
 
 // Reports the tile shape the heuristic picks (for the autotuner and the roofline accounting).

@@ -1,0 +1,157 @@
+"""Geometric multigrid V-cycle on Q1 grids: the global part of the flexible-CG preconditioner.
+
+Warp's solvers offer only the Jacobi preconditioner (``warp/_src/optim/linear.py:236-329``); the
+learned preconditioner of this package needs a carrier with global reach, since a 4-layer
+3x3x3 convolution only sees 9 nodes.  This module provides it:
+
+* hierarchy: vertex-centred 2:1 coarsening of the node grid (fine node 2I = coarse node I), per-cell
+  coefficient coarsened by geometric mean (``gb_mg_coarsen_cells``), coarse operators
+  rediscretised with the same Q1 assembly kernels and Dirichlet projection as the fine one;
+* transfers: trilinear prolongation P and full weighting R = P^T (``gb_mg_prolong_add`` /
+  ``gb_mg_restrict``), matrix-free, Dirichlet nodes masked;
+* smoothing: damped Jacobi, the post-smoothing step fused with its residual product
+  (``gb_bsr_jacobi_smooth``); the coarsest level (<= ``coarsest_nodes`` nodes) is solved with a
+  dense inverse computed once at set-up;
+* an optional learned fine-level smoother (``warp_gb300.learned``) replaces the first Jacobi step.
+
+Every launch goes to the stream the caller passes, so the flexible solver can capture a whole
+V-cycle into its CUDA graph.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _arrays as A
+from . import _native as N
+from . import fem, sparse
+
+
+class _Level:
+    pass
+
+
+class MultigridPreconditioner:
+    """z = V(r): symmetric V(1,1)-cycle (damped Jacobi, exact coarsest solve).
+
+    Args:
+        A: the fine system (compact BSR, 1x1 fp32, Dirichlet rows already projected).
+        geo: the fem.Grid3D / Grid2D it was assembled on.
+        coef: per-cell diffusion coefficient (host array or device tensor).
+        faces: Dirichlet faces (default: the whole boundary).
+        omega: Jacobi damping.
+        coarsest_nodes: stop coarsening at or below this many nodes.
+    """
+
+    def __init__(self, Am: sparse.BsrMatrix, geo, coef, faces=("x-", "x+", "y-", "y+", "z-", "z+"), omega: float = 0.6,
+                 coarsest_nodes: int = 400, max_levels: int = 12):
+        if Am.block_shape != (1, 1) or Am.scalar_type != torch.float32:
+            raise ValueError("multigrid preconditioner: scalar fp32 BSR matrix required")
+        self.omega = float(omega)
+        self.faces = tuple(faces)
+        self.smoother = None  # learned fine-level smoother (set by warp_gb300.learned)
+        self.status = A.zeros(1, torch.int32)
+        L = N.lib()
+        stream = A.stream()
+        levels = []
+        coef_t = coef if isinstance(coef, torch.Tensor) else A.from_numpy(np.asarray(coef, np.float32).reshape(-1))
+        coef_t = coef_t.reshape(-1).to(torch.float32).contiguous()
+        cur_geo, cur_A, cur_coef = geo, Am, coef_t
+        while True:
+            lv = _Level()
+            lv.geo = cur_geo
+            lv.A = cur_A
+            lv.nnz = cur_A.nnz_sync()
+            lv.dims = tuple(r + 1 for r in cur_geo.res) + ((1,) if cur_geo.dimension == 2 else ())
+            lv.n = cur_A.nrow
+            lv.mask = A.empty(lv.n, torch.float32)
+            nx, ny, nz = cur_geo._dims()
+            bits = fem.BoundarySides(cur_geo, self.faces).face_bits()
+            N.check(L.gb_grid_boundary_mask(cur_geo.dimension, nx, ny, nz, bits, 1, 1, A.ptr(lv.mask), stream), "mask")
+            lv.dinv = A.empty(lv.n, torch.float32)
+            N.check(L.gb_bsr_inverse_diagonal(N.GB_F32, 1, lv.n, A.ptr(cur_A.offsets), None, A.ptr(cur_A.columns),
+                                              A.ptr(cur_A.values), 0, A.ptr(lv.dinv), stream), "dinv")
+            lv.w = A.zeros(lv.n, torch.float32)
+            lv.t = A.zeros(lv.n, torch.float32)
+            levels.append(lv)
+            res = cur_geo.res
+            if lv.n <= coarsest_nodes or any(r % 2 for r in res) or len(levels) >= max_levels:
+                break
+            cres = tuple(r // 2 for r in res)
+            ccoef = A.empty(int(np.prod(cres)), torch.float32)
+            fx, fy, fz = (res[0], res[1], res[2]) if cur_geo.dimension == 3 else (res[0], res[1], 2)
+            if cur_geo.dimension == 2:
+                raise NotImplementedError("2-D hierarchy: use Grid3D problems")
+            N.check(L.gb_mg_coarsen_cells(fx, fy, fz, A.ptr(cur_coef), A.ptr(ccoef), stream), "coarsen")
+            cgeo = fem.Grid3D(res=cres, bounds_lo=cur_geo.bounds_lo, bounds_hi=cur_geo.bounds_hi)
+            space = fem.make_polynomial_space(cgeo, degree=1)
+            cA = fem.integrate(fem.diffusion_form, fields={"u": fem.make_trial(space), "v": fem.make_test(space)},
+                               values={"nu": ccoef})
+            rhs = A.zeros(cgeo.node_count(), torch.float32)
+            bd = fem.BoundarySides(cgeo, self.faces)
+            P = fem.integrate(fem.boundary_projector_form,
+                              fields={"u": fem.make_trial(space, bd), "v": fem.make_test(space, bd)}, assembly="nodal")
+            fem.project_linear_system(cA, rhs, P)
+            cur_geo, cur_A, cur_coef = cgeo, cA, ccoef
+        # coarsest level: dense inverse (set-up only; a few hundred unknowns)
+        last = levels[-1]
+        dense = last.A.numpy_dense()
+        last.inv = A.from_numpy(np.linalg.inv(dense).astype(np.float32))
+        for lv in levels[1:]:  # right-hand side / correction buffers of the coarse levels
+            lv.rhs = A.zeros(lv.n, torch.float32)
+            lv.sol = A.zeros(lv.n, torch.float32)
+        self.levels = levels
+        torch.cuda.current_stream().synchronize()
+
+    @property
+    def n(self) -> int:
+        return self.levels[0].n
+
+    @property
+    def kernels_per_apply(self) -> int:
+        """Kernel launches of one V-cycle (5 per level above the coarsest + the coarse solve)."""
+        extra = getattr(self.smoother, "kernels_per_apply", 0) - 1 if self.smoother is not None else 0
+        return 5 * (len(self.levels) - 1) + 1 + max(extra, 0)
+
+    def describe(self) -> str:
+        return " -> ".join(f"{'x'.join(str(d) for d in lv.dims)}" for lv in self.levels)
+
+    # z = M r on `stream` (device pointers r, z of the fine level)
+    def launch(self, stream, r_ptr: int, z_ptr: int) -> None:
+        self._vcycle(0, int(r_ptr), int(z_ptr), stream)
+
+    def _vcycle(self, li: int, r: int, z: int, stream) -> None:
+        L = N.lib()
+        lv = self.levels[li]
+        if li == len(self.levels) - 1:
+            N.check(L.gb_dense_mv(N.GB_F32, lv.n, lv.n, A.ptr(lv.inv), r, None, z, 1.0, 0.0, stream), "coarse")
+            return
+        nxt = self.levels[li + 1]
+        w, t = A.ptr(lv.w), A.ptr(lv.t)
+        Am = lv.A
+        # pre-smoothing from zero: learned step on the fine level when available, else Jacobi
+        if li == 0 and self.smoother is not None:
+            self.smoother.launch(stream, r, w)
+        else:
+            N.check(L.gb_mg_jacobi0(lv.n, self.omega, A.ptr(lv.dinv), r, w, stream), "jacobi0")
+        # t = r - A w
+        N.check(L.gb_bsr_mv(1, 1, lv.n, lv.n, lv.nnz, Am.capacity, A.ptr(Am.offsets), None, A.ptr(Am.columns),
+                            A.ptr(Am.values), N.GB_F32, w, r, t, N.GB_F32, -1.0, 1.0, 0, 0, 0, -1, A.ptr(self.status),
+                            stream), "residual")
+        fx, fy, fz = lv.dims
+        cx, cy, cz = nxt.dims
+        rc, zc = A.ptr(nxt.rhs), A.ptr(nxt.sol)  # the coarse level's own w/t are its work vectors
+        N.check(L.gb_mg_restrict(fx, fy, fz, cx, cy, cz, t, A.ptr(lv.mask), A.ptr(nxt.mask), rc, stream), "restrict")
+        self._vcycle(li + 1, rc, zc, stream)
+        N.check(L.gb_mg_prolong_add(fx, fy, fz, cx, cy, cz, zc, A.ptr(lv.mask), 1.0, w, stream), "prolong")
+        # post-smoothing fused with its residual: z = w + omega D^-1 (r - A w)
+        N.check(L.gb_bsr_jacobi_smooth(1, lv.n, lv.nnz, Am.capacity, A.ptr(Am.offsets), A.ptr(Am.columns),
+                                       A.ptr(Am.values), r, w, A.ptr(lv.dinv), self.omega, z, A.ptr(self.status),
+                                       stream), "smooth")
+
+    def apply(self, r: torch.Tensor, z: torch.Tensor | None = None) -> torch.Tensor:
+        """Eager z = M r on the current stream (tests / diagnostics)."""
+        z = torch.empty_like(r) if z is None else z
+        self.launch(A.stream(), r.data_ptr(), z.data_ptr())
+        return z

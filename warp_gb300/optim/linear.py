@@ -35,6 +35,8 @@ from .. import _native as N
 from .. import sparse
 
 __all__ = [
+    "FCG",
+    "fcg",
     "LinearOperator",
     "aslinearoperator",
     "preconditioner",
@@ -516,6 +518,62 @@ class BiCGSTAB(LinearSolverState):
         return it, math.sqrt(rr), atol_v
 
 
+class FCG(LinearSolverState):
+    """Flexible CG, FCG(1) (Notay's truncated variant): each new direction z = M(r) is
+    A-orthogonalised against the previous direction only, so M may change from one application to
+    the next (a nonlinear / learned preconditioner).  Same interface and return conventions as
+    ``CG``; ``M`` is an object with ``launch(stream, r_ptr, z_ptr)`` that enqueues z = M(r) on the
+    given stream (e.g. ``MultigridPreconditioner``).  A stagnation rule (every
+    ``stagnation_window`` iterations the residual norm must drop by ``stagnation_factor``) or a
+    non-descent direction (z.r <= 0) stops the loop with a status bit so that the caller can fall
+    back to Jacobi-CG.  No reference counterpart (Warp has CG/CR/BiCGSTAB/GMRES only).
+    """
+
+    _kind = N.KRYLOV_FCG
+
+    def __init__(self, A_, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_every=10,
+                 use_cuda_graph=True, stagnation_window: int = 25, stagnation_factor: float = 0.9):
+        if M is None or not hasattr(M, "launch"):
+            raise ValueError("FCG needs a preconditioner object with launch(stream, r_ptr, z_ptr)")
+        self._precond_obj = M
+        self._stag = (int(stagnation_window), float(stagnation_factor))
+        super().__init__(A_, b, x, tol, atol, maxiter, None, callback, check_every, use_cuda_graph)
+        if not self._fused:
+            raise ValueError("FCG needs a BSR operator with 1x1/3x3 fp32 blocks and fp32 vectors")
+        self._M = None
+        self._install_precond(M)
+
+    def _install_precond(self, M):
+        import traceback
+
+        def _cb(user, stream, r, z):
+            try:
+                M.launch(stream, r, z)
+                return 0
+            except Exception:  # reported through the solver's status
+                traceback.print_exc()
+                return 1
+
+        self._cb = N.PRECOND_FN(_cb)
+        N.check(N.lib().gb_krylov_set_precond(self._native, ctypes.cast(self._cb, ctypes.c_void_p), None,
+                                              self._stag[0], self._stag[1]), "krylov_set_precond")
+        self._precond_obj = M
+
+    def _run_generic(self, Aop, b, x, Mop):
+        raise ValueError("FCG runs on the fused path only")
+
+
+def fcg(A_, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_every=10, use_cuda_graph=True,
+        run=True, stagnation_window: int = 25, stagnation_factor: float = 0.9):
+    """Flexible CG with a (possibly nonlinear) preconditioner object; see ``FCG``."""
+    state = FCG(A_, b, x, tol=tol, atol=atol, maxiter=maxiter, M=M, callback=callback, check_every=check_every,
+                use_cuda_graph=use_cuda_graph, stagnation_window=stagnation_window,
+                stagnation_factor=stagnation_factor)
+    if run:
+        return state()
+    return state
+
+
 def cg(A_, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_every=10, use_cuda_graph=True,
        run=True, *, restart=None):
     """Preconditioned Conjugate Gradient (reference: ``linear.py:1035-1121``)."""
@@ -570,9 +628,20 @@ class RefinedSolver:
             self._inner_A = sparse.BsrMatrix(Am.nrow, Am.ncol, Am.block_shape, inner_values.dtype)
             self._inner_A.offsets, self._inner_A.columns = Am.offsets, Am.columns
             self._inner_A.values, self._inner_A.nnz = inner_values, Am.nnz
-        cls = CG if method == "cg" else BiCGSTAB
-        self.inner = cls(self._inner_A, self._r32, self._d, tol=self.inner_tol, atol=0.0,
-                         maxiter=self.inner_maxiter, M=M, check_every=0, use_cuda_graph=True)
+        self.method = method
+        self.fallbacks = 0
+        self._jacobi = None
+        if method == "fcg":
+            self.inner = FCG(self._inner_A, self._r32, self._d, tol=self.inner_tol, atol=0.0,
+                             maxiter=self.inner_maxiter, M=M, check_every=0, use_cuda_graph=True)
+            # Jacobi-CG: the fallback when the flexible solve stagnates
+            self._jacobi_M = preconditioner(self._inner_A, "diag")
+            self._jacobi = CG(self._inner_A, self._r32, self._d, tol=self.inner_tol, atol=0.0,
+                              maxiter=self.inner_maxiter, M=self._jacobi_M, check_every=0, use_cuda_graph=True)
+        else:
+            cls = CG if method == "cg" else BiCGSTAB
+            self.inner = cls(self._inner_A, self._r32, self._d, tol=self.inner_tol, atol=0.0,
+                             maxiter=self.inner_maxiter, M=M, check_every=0, use_cuda_graph=True)
         if not self.inner._fused:
             raise ValueError("solve_refined needs a BSR operator with 1x1/3x3 float32 blocks and a Jacobi or no "
                              "preconditioner")
@@ -632,11 +701,23 @@ class RefinedSolver:
             self.inner._tol = min(max(self.inner_tol, need), 0.5)
             self._d.zero_()
             self.inner._run_fused(Aop, self._r32, self._d, self.inner._M, x_is_zero=True)
+            it = int(self.inner._dev_iter.item())
+            per_it = 3 if self.method != "fcg" else 4 + getattr(self.inner._precond_obj, "kernels_per_apply", 0)
+            self.kernel_launches += 2 + per_it * it  # argument store, init, kernels per iteration
+            if self.method == "fcg":
+                status = int(self.inner._dev_status.item())
+                if status & (N.DEV_STAGNATION | N.DEV_BREAKDOWN | N.DEV_NONFINITE):
+                    # the flexible solve stalled: finish this correction with Jacobi-CG (the judge)
+                    self.fallbacks += 1
+                    self._jacobi._tol = self.inner._tol
+                    self._jacobi._run_fused(Aop, self._r32, self._d, self._jacobi_M, x_is_zero=False)
+                    jt = int(self._jacobi._dev_iter.item())
+                    it += jt
+                    self.kernel_launches += 2 + 3 * jt
             N.check(L.gb_update_solution(self.n, A.ptr(x64), A.ptr(self._x2), A.ptr(self._d), 1.0, A.stream()),
                     "update_solution")
-            it = int(self.inner._dev_iter.item())
+            self.kernel_launches += 1
             inner_iters += it
-            self.kernel_launches += 3 + 3 * it  # argument store, CG init, update + 3 per iteration
             rnorm, _ = self.residual(x64, b)
             outer += 1
             history.append(rnorm / bnorm)
@@ -650,6 +731,7 @@ class RefinedSolver:
 
 def solve_refined(A_: sparse.BsrMatrix, b, x64=None, tol: float = 1e-8, M=None, method: str = "cg",
                   inner_tol: float = 1e-5, max_outer: int = 50, residual: str = "df32"):
+    """method: "cg" / "bicgstab" (M = Jacobi or None) or "fcg" (M = a preconditioner object)."""
     """FP64-accurate solve of ``A x = b`` with an FP32 Krylov inner loop; returns ``(x64, info)``."""
     solver = RefinedSolver(A_, M=M, method=method, inner_tol=inner_tol, residual=residual)
     return solver.solve(b, x64=x64, tol=tol, max_outer=max_outer)
