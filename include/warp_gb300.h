@@ -173,6 +173,48 @@ int gb_grid_boundary_mask(int dim, int nx, int ny, int nz, int face_bits, int nc
 int gb_dirichlet_project(int bdim, int nrow, const int* offsets, const int* columns, float* values, const float* mask,
                          float* rhs, const float* fixed, float* tmp, int project_matrix, gb_stream_t stream);
 
+/* ---- Flexible CG preconditioner, multigrid carrier, learned smoother ------------------------------
+ * No counterparts in the reference (its only preconditioner is Jacobi, warp/_src/optim/linear.py:236-329).
+ * gb_krylov_set_precond: installs z = M(r) for a KRYLOV_FCG handle; fn is called on the host while the
+ * solver records its launches (eagerly or into its CUDA graphs) and must enqueue M's kernels on the
+ * given stream.  Stagnation (residual not reduced by stag_factor over stag_window iterations, or
+ * r.z <= 0) stops the loop with GB_DEV_STAGNATION so the caller can fall back to Jacobi-CG. */
+typedef int (*gb_precond_fn)(void* user, gb_stream_t stream, const float* r, float* z);
+int gb_krylov_set_precond(void* handle, gb_precond_fn fn, void* user, int stag_window, double stag_factor);
+/* z_out = z + omega * dinv * (r - A z) (fused Jacobi smoothing step; z_out may not alias z). */
+int gb_bsr_jacobi_smooth(int bdim, int nrow, int64_t nnz, int64_t ncap, const int* offsets, const int* columns,
+                         const float* values, const float* r, const float* z, const float* dinv, float omega,
+                         float* z_out, int* status, gb_stream_t stream);
+/* Vertex-centred 2:1 transfers on Q1 node grids (nodes per axis; masks 1 = Dirichlet, may be NULL). */
+int gb_mg_restrict(int fnx, int fny, int fnz, int cnx, int cny, int cnz, const float* r, const float* fmask,
+                   const float* cmask, float* rc, gb_stream_t stream);
+int gb_mg_prolong_add(int fnx, int fny, int fnz, int cnx, int cny, int cnz, const float* zc, const float* fmask,
+                      float scale, float* z, gb_stream_t stream);
+int gb_mg_jacobi0(int64_t n, float omega, const float* dinv, const float* r, float* z, gb_stream_t stream);
+int gb_mg_coarsen_cells(int fx, int fy, int fz, const float* a, float* ac, gb_stream_t stream);
+/* 3x3x3 convolutions on a node grid, channels-last activations act[v][C], v = (x*ny + y)*nz + z,
+ * weights W[t][ci][co] (t = 9(dx+1) + 3(dy+1) + (dz+1)), zero padding.  fp32 training kernels
+ * (gb_conv3_bwd_weight_f32 accumulates into gW, deterministic), Adam, and the bf16 tensor-core
+ * forward (Wt[t][co][16] bf16, cout 16 or 8, fp32 accumulation). */
+int gb_conv3_fwd_f32(int nx, int ny, int nz, int cin, int cout, const float* in, const float* W, int relu, float* out,
+                     gb_stream_t stream);
+int gb_conv3_bwd_data_f32(int nx, int ny, int nz, int cin, int cout, const float* gout, const float* W, float* gin,
+                          gb_stream_t stream);
+size_t gb_conv3_bwd_weight_workspace_bytes(int nx, int ny, int nz, int cin, int cout);
+int gb_conv3_bwd_weight_f32(int nx, int ny, int nz, int cin, int cout, const float* in, const float* gout, float* gW,
+                            void* workspace, size_t workspace_bytes, gb_stream_t stream);
+int gb_relu_bwd(int64_t n, const float* out, float* g, gb_stream_t stream);
+int gb_adam_step(int n, float* w, const float* g, float* m, float* v, float lr, float b1, float b2, float eps, int step,
+                 void* w_bf16, gb_stream_t stream);
+int gb_net_features(int dtype, int64_t n, const float* r, const float* dinv, const float* chat, const float* mask,
+                    void* out, gb_stream_t stream);
+int gb_net_cell_features(int nx, int ny, int nz, const float* cell_coef, float mean_log, float inv_std, float* chat,
+                         gb_stream_t stream);
+int gb_net_combine(int dtype, int64_t n, int stride, const void* act, const float* mask, float omega, const float* dinv,
+                   const float* r, float* out, gb_stream_t stream);
+int gb_conv3_fwd_bf16(int nx, int ny, int nz, int cout, int relu, const void* in, const void* Wt, void* out,
+                      gb_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -81,6 +81,17 @@ _SIGNATURES = {
     "gb_dots_workspace_bytes": (_c_sz, []),
     "gb_dots": (_c_int, [_c_int, _c_i64, _c_int, ctypes.POINTER(_vp), ctypes.POINTER(_vp), _vp, _vp, _vp]),
     "gb_axpby": (_c_int, [_c_int, _c_i64, _c_dbl, _vp, _c_dbl, _vp, _vp, _vp]),
+    "gb_conv3_fwd_f32": (_c_int, [_c_int] * 5 + [_vp, _vp, _c_int, _vp, _vp]),
+    "gb_conv3_bwd_data_f32": (_c_int, [_c_int] * 5 + [_vp, _vp, _vp, _vp]),
+    "gb_conv3_bwd_weight_workspace_bytes": (_c_sz, [_c_int] * 5),
+    "gb_conv3_bwd_weight_f32": (_c_int, [_c_int] * 5 + [_vp, _vp, _vp, _vp, _c_sz, _vp]),
+    "gb_relu_bwd": (_c_int, [_c_i64, _vp, _vp, _vp]),
+    "gb_adam_step": (_c_int, [_c_int, _vp, _vp, _vp, _vp, ctypes.c_float, ctypes.c_float, ctypes.c_float,
+                              ctypes.c_float, _c_int, _vp, _vp]),
+    "gb_net_features": (_c_int, [_c_int, _c_i64, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "gb_net_cell_features": (_c_int, [_c_int, _c_int, _c_int, _vp, ctypes.c_float, ctypes.c_float, _vp, _vp]),
+    "gb_net_combine": (_c_int, [_c_int, _c_i64, _c_int, _vp, _vp, ctypes.c_float, _vp, _vp, _vp, _vp]),
+    "gb_conv3_fwd_bf16": (_c_int, [_c_int] * 5 + [_vp, _vp, _vp, _vp]),
 }
 
 _LIB = None

@@ -1,0 +1,511 @@
+// gb_convnet.cu -- the learned smoother: a 4-layer 3x3x3 convolutional network on the Q1 node grid.
+//
+// No reference counterpart (Warp's preconditioners are Jacobi only).  Layout: activations are
+// channels-last over the node grid, act[v][C] with v = (x * ny + y) * nz + z and C = 16; taps
+// t = (dx+1)*9 + (dy+1)*3 + (dz+1) for dx, dy, dz in {-1, 0, 1}; neighbours outside the grid read
+// as zero; weights W[t][ci][co]:
+//     out[v][co] = sum_t sum_ci W[t][ci][co] * in[v + off(t)][ci]        (no bias: the network is
+// positively homogeneous, N(c x) = c N(x) for c > 0, so no residual normalisation is needed).
+//
+// Training (fp32, CUDA cores): k_conv_fwd_f32, k_conv_bwd_data_f32 (gradient w.r.t. the input =
+// correlation with the flipped, transposed kernel), k_conv_bwd_weight_f32 (per-CTA partial sums
+// reduced in a fixed order: deterministic), ReLU backward and Adam.  Inference (bf16 operands,
+// fp32 accumulation): k_conv_fwd_bf16_mma, an implicit GEMM on the tensor cores -- a CTA owns a
+// 2 x 4 x 16 voxel brick, stages its halo (4 x 6 x 18 voxels x 16 channels, swizzled so that
+// ldmatrix reads are bank-conflict free) and the layer's weights in shared memory, and each warp
+// accumulates 32 voxels x 16 output channels over the 27 taps with m16n8k16 MMAs.
+#include "gb_common.cuh"
+
+namespace gb {
+
+constexpr int CN = 16;  // channels of the hidden layers (and of the padded input)
+
+struct Grid3 {
+    int nx, ny, nz;
+};
+
+__device__ __forceinline__ bool tap_neighbor(const Grid3& g, int x, int y, int z, int t, int64_t& nb)
+{
+    const int dx = t / 9 - 1, dy = (t / 3) % 3 - 1, dz = t % 3 - 1;
+    const int xx = x + dx, yy = y + dy, zz = z + dz;
+    if (xx < 0 || yy < 0 || zz < 0 || xx >= g.nx || yy >= g.ny || zz >= g.nz) return false;
+    nb = ((int64_t)xx * g.ny + yy) * g.nz + zz;
+    return true;
+}
+
+__device__ __forceinline__ void decode(const Grid3& g, int64_t v, int& x, int& y, int& z)
+{
+    x = (int)(v / ((int64_t)g.ny * g.nz));
+    y = (int)((v / g.nz) % g.ny);
+    z = (int)(v % g.nz);
+}
+
+// ---------------------------------------------------------------------------------------------
+// fp32 training kernels
+// ---------------------------------------------------------------------------------------------
+// out[v][co] = sum W * in ; cin, cout <= 16; relu: out = max(out, 0)
+__global__ __launch_bounds__(256) void k_conv_fwd_f32(Grid3 g, int cin, int cout, const float* __restrict__ in,
+                                                      const float* __restrict__ W, int relu, float* __restrict__ out)
+{
+    __shared__ float s_w[27 * CN * CN];
+    for (int i = threadIdx.x; i < 27 * cin * cout; i += blockDim.x) s_w[i] = W[i];
+    __syncthreads();
+    const int64_t n = (int64_t)g.nx * g.ny * g.nz;
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    int x, y, z;
+    decode(g, v, x, y, z);
+    float acc[CN];
+#pragma unroll
+    for (int c = 0; c < CN; ++c) acc[c] = 0.f;
+    for (int t = 0; t < 27; ++t) {
+        int64_t nb;
+        if (!tap_neighbor(g, x, y, z, t, nb)) continue;
+        const float* src = in + nb * cin;
+        for (int ci = 0; ci < cin; ++ci) {
+            const float a = src[ci];
+            const float* w = s_w + (t * cin + ci) * cout;
+#pragma unroll
+            for (int co = 0; co < CN; ++co)
+                if (co < cout) acc[co] += a * w[co];
+        }
+    }
+#pragma unroll
+    for (int co = 0; co < CN; ++co)
+        if (co < cout) out[v * cout + co] = relu ? fmaxf(acc[co], 0.f) : acc[co];
+}
+
+// gin[v][ci] = sum_t sum_co W[t][ci][co] * gout[v - off(t)][co]
+__global__ __launch_bounds__(256) void k_conv_bwd_data_f32(Grid3 g, int cin, int cout, const float* __restrict__ gout,
+                                                           const float* __restrict__ W, float* __restrict__ gin)
+{
+    __shared__ float s_w[27 * CN * CN];
+    for (int i = threadIdx.x; i < 27 * cin * cout; i += blockDim.x) s_w[i] = W[i];
+    __syncthreads();
+    const int64_t n = (int64_t)g.nx * g.ny * g.nz;
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    int x, y, z;
+    decode(g, v, x, y, z);
+    float acc[CN];
+#pragma unroll
+    for (int c = 0; c < CN; ++c) acc[c] = 0.f;
+    for (int t = 0; t < 27; ++t) {
+        int64_t nb;
+        if (!tap_neighbor(g, x, y, z, 26 - t, nb)) continue;  // v - off(t) = v + off(26 - t)
+        const float* src = gout + nb * cout;
+        for (int co = 0; co < cout; ++co) {
+            const float gv = src[co];
+#pragma unroll
+            for (int ci = 0; ci < CN; ++ci)
+                if (ci < cin) acc[ci] += gv * s_w[(t * cin + ci) * cout + co];
+        }
+    }
+#pragma unroll
+    for (int ci = 0; ci < CN; ++ci)
+        if (ci < cin) gin[v * cin + ci] = acc[ci];
+}
+
+// partial[cta][t][ci][co] = sum over the CTA's voxels v of in[v + off(t)][ci] * gout[v][co].
+// Persistent CTAs walk tiles of WG_VOX voxels; thread (ci, co) keeps the 27 tap sums in registers; the
+// tile's neighbour table and output gradients are staged in shared memory.
+constexpr int WG_VOX = 64;
+constexpr int WG_CTAS = 2 * kSmCount;
+__global__ __launch_bounds__(256) void k_conv_bwd_weight_f32(Grid3 g, int cin, int cout, const float* __restrict__ in,
+                                                             const float* __restrict__ gout,
+                                                             float* __restrict__ partial)
+{
+    __shared__ float s_g[WG_VOX * CN];
+    __shared__ int64_t s_nb[WG_VOX * 27];
+    const int64_t n = (int64_t)g.nx * g.ny * g.nz;
+    const int64_t ntiles = ceil_div<int64_t>(n, WG_VOX);
+    const int ci = threadIdx.x / cout, co = threadIdx.x % cout;
+    const bool active = threadIdx.x < cin * cout;
+    float acc[27];
+#pragma unroll
+    for (int t = 0; t < 27; ++t) acc[t] = 0.f;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int64_t v0 = tile * WG_VOX;
+        __syncthreads();
+        for (int i = threadIdx.x; i < WG_VOX * cout; i += blockDim.x) {
+            const int64_t v = v0 + i / cout;
+            s_g[i] = (v < n) ? gout[v * cout + (i % cout)] : 0.f;
+        }
+        for (int i = threadIdx.x; i < WG_VOX * 27; i += blockDim.x) {
+            const int64_t v = v0 + i / 27;
+            int64_t nb = -1;
+            if (v < n) {
+                int x, y, z;
+                decode(g, v, x, y, z);
+                if (!tap_neighbor(g, x, y, z, i % 27, nb)) nb = -1;
+            }
+            s_nb[i] = nb;
+        }
+        __syncthreads();
+        if (!active) continue;
+        for (int j = 0; j < WG_VOX; ++j) {
+            const float gv = s_g[j * cout + co];
+#pragma unroll
+            for (int t = 0; t < 27; ++t) {
+                const int64_t nb = s_nb[j * 27 + t];
+                if (nb >= 0) acc[t] += __ldg(in + nb * cin + ci) * gv;
+            }
+        }
+    }
+    if (active) {
+        const int nw = 27 * cin * cout;
+#pragma unroll
+        for (int t = 0; t < 27; ++t) partial[(int64_t)blockIdx.x * nw + (t * cin + ci) * cout + co] = acc[t];
+    }
+}
+
+// gW[k] += sum_cta partial[cta][k]  (fixed order)
+__global__ void k_reduce_partials(int nparts, int nw, const float* __restrict__ partial, float* __restrict__ gW)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nw) return;
+    float s = 0.f;
+    for (int p = 0; p < nparts; ++p) s += partial[(int64_t)p * nw + k];
+    gW[k] += s;
+}
+
+// g *= (out > 0)
+__global__ void k_relu_bwd(int64_t n, const float* __restrict__ out, float* __restrict__ g)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if (out[i] <= 0.f) g[i] = 0.f;
+}
+
+// Adam (Kingma & Ba): m = b1 m + (1-b1) g; v = b2 v + (1-b2) g^2; w -= lr mhat / (sqrt(vhat) + eps);
+// also writes the bf16 copy used by the tensor-core forward.
+__global__ void k_adam(int n, float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, float lr, float b1, float b2, float eps, float c1, float c2,
+                       __nv_bfloat16* __restrict__ wb)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float gi = g[i];
+    const float mi = b1 * m[i] + (1.f - b1) * gi;
+    const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+    m[i] = mi;
+    v[i] = vi;
+    const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+    w[i] = wi;
+    if (wb) wb[i] = __float2bfloat16(wi);
+}
+
+// Input features: ch0 = x = dinv * r; ch1..8 = x * chat[v][k] (normalised log-coefficient of the
+// k-th adjacent cell, 0 outside the grid); ch9..15 = 0; masked (Dirichlet) nodes are all zero.
+// fp32 (training) or bf16 (inference) output.
+template <typename OT>
+__global__ void k_features(int64_t n, const float* __restrict__ r, const float* __restrict__ dinv,
+                           const float* __restrict__ chat, const float* __restrict__ mask, OT* __restrict__ out)
+{
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const float xm = (mask && mask[v] != 0.f) ? 0.f : dinv[v] * r[v];
+        float f[CN];
+        f[0] = xm;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) f[1 + k] = xm * chat[v * 8 + k];
+#pragma unroll
+        for (int k = 9; k < CN; ++k) f[k] = 0.f;
+        if constexpr (sizeof(OT) == 2) {
+            __nv_bfloat162* o = reinterpret_cast<__nv_bfloat162*>(out + v * CN);
+#pragma unroll
+            for (int k = 0; k < CN / 2; ++k) o[k] = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
+        } else {
+#pragma unroll
+            for (int k = 0; k < CN; ++k) out[v * CN + k] = f[k];
+        }
+    }
+}
+
+// per-node normalised log-coefficients of the 8 adjacent cells (set-up)
+__global__ void k_cell_features(Grid3 g, const float* __restrict__ cell_coef, float mean_log, float inv_std,
+                                float* __restrict__ chat)
+{
+    const int64_t n = (int64_t)g.nx * g.ny * g.nz;
+    const int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= n) return;
+    int x, y, z;
+    decode(g, v, x, y, z);
+    const int cx = g.nx - 1, cy = g.ny - 1, cz = g.nz - 1;
+    for (int k = 0; k < 8; ++k) {
+        const int ax = x - 1 + (k >> 2), ay = y - 1 + ((k >> 1) & 1), az = z - 1 + (k & 1);
+        float val = 0.f;
+        if (ax >= 0 && ay >= 0 && az >= 0 && ax < cx && ay < cy && az < cz)
+            val = (logf(cell_coef[((int64_t)ax * cy + ay) * cz + az]) - mean_log) * inv_std;
+        chat[v * 8 + k] = val;
+    }
+}
+
+// out[v] = omega * dinv[v] * r[v] + (mask[v] ? 0 : act[v][0]): the Jacobi step plus the network's
+// single output channel (dinv may be null: network only).
+template <typename T>
+__global__ void k_net_combine(int64_t n, int stride, const T* __restrict__ act, const float* __restrict__ mask,
+                              float omega, const float* __restrict__ dinv, const float* __restrict__ r,
+                              float* __restrict__ out)
+{
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        float a;
+        if constexpr (sizeof(T) == 2) a = __bfloat162float(act[v * stride]); else a = act[v * stride];
+        if (mask && mask[v] != 0.f) a = 0.f;
+        if (dinv) a += omega * dinv[v] * r[v];
+        out[v] = a;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// bf16 tensor-core forward (m16n8k16, fp32 accumulation)
+// ---------------------------------------------------------------------------------------------
+constexpr int BX = 2, BY = 4, BZ = 16;                         // brick of 128 voxels
+constexpr int HX = BX + 2, HY = BY + 2, HZ = BZ + 2;           // halo 4 x 6 x 18
+constexpr int HVOX = HX * HY * HZ;                             // 432 voxels, 32 B each
+
+// shared-memory byte offset of 16-byte chunk h (0/1) of halo voxel hv, swizzled: chunk h of voxel
+// hv lives in slot h ^ ((hv >> 2) & 1), so the 8 rows of an ldmatrix phase (8 consecutive z, 32 B
+// apart) cover all 32 banks.
+__device__ __forceinline__ uint32_t halo_off(int hv, int h) { return (uint32_t)(hv * 32 + ((h ^ ((hv >> 2) & 1)) << 4)); }
+
+__device__ __forceinline__ void ldmatrix_x4(uint32_t addr, uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3)
+{
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];"
+                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+                 : "r"(addr));
+}
+
+__device__ __forceinline__ void mma_bf16_16816(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                               uint32_t b0, uint32_t b1)
+{
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+        "{%0, %1, %2, %3};"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+}
+
+// in: [V][16] bf16; Wt: [27][cout][16] bf16 (co-major, ci contiguous); out: [V][cout_store] bf16
+// (cout = 16 with ReLU for hidden layers; cout = 8 for the last layer, only channel 0 meaningful).
+template <int COUT, bool RELU>
+__global__ __launch_bounds__(128) void k_conv_fwd_bf16_mma(Grid3 g, const __nv_bfloat16* __restrict__ in,
+                                                           const __nv_bfloat16* __restrict__ Wt,
+                                                           __nv_bfloat16* __restrict__ out)
+{
+    __shared__ __align__(128) unsigned char s_halo[HVOX * 32];
+    __shared__ __align__(16) __nv_bfloat16 s_w[27 * COUT * CN];
+    const int bx = blockIdx.x, by = blockIdx.y, bz = blockIdx.z;
+    const int x0 = bx * BX, y0 = by * BY, z0 = bz * BZ;
+    // stage weights
+    for (int i = threadIdx.x; i < 27 * COUT * CN / 8; i += blockDim.x)
+        reinterpret_cast<uint4*>(s_w)[i] = reinterpret_cast<const uint4*>(Wt)[i];
+    // stage the halo brick (zero outside the grid)
+    for (int i = threadIdx.x; i < HVOX * 2; i += blockDim.x) {
+        const int hv = i >> 1, h = i & 1;
+        const int hz = hv % HZ, hy = (hv / HZ) % HY, hx = hv / (HZ * HY);
+        const int x = x0 + hx - 1, y = y0 + hy - 1, z = z0 + hz - 1;
+        uint4 val = make_uint4(0u, 0u, 0u, 0u);
+        if (x >= 0 && y >= 0 && z >= 0 && x < g.nx && y < g.ny && z < g.nz)
+            val = reinterpret_cast<const uint4*>(in + (((int64_t)x * g.ny + y) * g.nz + z) * CN)[h];
+        *reinterpret_cast<uint4*>(s_halo + halo_off(hv, h)) = val;
+    }
+    __syncthreads();
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t halo_base = static_cast<uint32_t>(__cvta_generic_to_shared(s_halo));
+    // warp w owns the two z-lines (hx = 1 + w/2, hy = 1 + 2*(w%2) + {0, 1}) of the brick
+    const int lx = warp >> 1;
+    float acc[2][COUT / 8][4];
+#pragma unroll
+    for (int m = 0; m < 2; ++m)
+#pragma unroll
+        for (int nt = 0; nt < COUT / 8; ++nt)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) acc[m][nt][q] = 0.f;
+    // ldmatrix.x4 row assignment: lanes 0-15 -> rows 0-15 of chunk 0, lanes 16-31 -> rows 0-15 of chunk 1
+    const int arow = lane & 15, achunk = lane >> 4;
+#pragma unroll 1
+    for (int t = 0; t < 27; ++t) {
+        const int dx = t / 9 - 1, dy = (t / 3) % 3 - 1, dz = t % 3 - 1;
+        // B fragments for this tap: b0,b1 = W[t][co = n0 + lane/4][ci = 2*(lane%4) .. +1 and +8 ..]
+        uint32_t b[COUT / 8][2];
+#pragma unroll
+        for (int nt = 0; nt < COUT / 8; ++nt) {
+            const __nv_bfloat16* wrow = s_w + ((size_t)t * COUT + nt * 8 + (lane >> 2)) * CN;
+            b[nt][0] = *reinterpret_cast<const uint32_t*>(wrow + 2 * (lane & 3));
+            b[nt][1] = *reinterpret_cast<const uint32_t*>(wrow + 8 + 2 * (lane & 3));
+        }
+#pragma unroll
+        for (int m = 0; m < 2; ++m) {
+            const int ly = 2 * (warp & 1) + m;
+            const int hv = ((1 + lx + dx) * HY + (1 + ly + dy)) * HZ + (1 + arow + dz);
+            uint32_t a0, a1, a2, a3;
+            ldmatrix_x4(halo_base + halo_off(hv, achunk), a0, a1, a2, a3);
+            // x4 order: (rows 0-7, k 0-7), (rows 8-15, k 0-7), (rows 0-7, k 8-15), (rows 8-15, k 8-15)
+#pragma unroll
+            for (int nt = 0; nt < COUT / 8; ++nt) mma_bf16_16816(acc[m][nt], a0, a1, a2, a3, b[nt][0], b[nt][1]);
+        }
+    }
+    // epilogue: c0,c1 -> (row lane/4, cols 2*(lane%4), +1); c2,c3 -> row + 8
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+        const int ly = 2 * (warp & 1) + m;
+        const int x = x0 + lx, y = y0 + ly;
+        if (x >= g.nx || y >= g.ny) continue;
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            const int z = z0 + (lane >> 2) + 8 * half;
+            if (z >= g.nz) continue;
+            const int64_t v = ((int64_t)x * g.ny + y) * g.nz + z;
+#pragma unroll
+            for (int nt = 0; nt < COUT / 8; ++nt) {
+                float c0 = acc[m][nt][2 * half], c1 = acc[m][nt][2 * half + 1];
+                if (RELU) {
+                    c0 = fmaxf(c0, 0.f);
+                    c1 = fmaxf(c1, 0.f);
+                }
+                *reinterpret_cast<__nv_bfloat162*>(out + v * COUT + nt * 8 + 2 * (lane & 3)) =
+                    __floats2bfloat162_rn(c0, c1);
+            }
+        }
+    }
+}
+
+static int g1(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(n, 256), kSmCount * 16)); }
+
+}  // namespace gb
+
+using namespace gb;
+
+GB_API int gb_conv3_fwd_f32(int nx, int ny, int nz, int cin, int cout, const float* in, const float* W, int relu,
+                            float* out, cudaStream_t stream)
+{
+    GB_REQUIRE(cin >= 1 && cin <= CN && cout >= 1 && cout <= CN, "conv3_fwd_f32: channels must be 1..16");
+    Grid3 g{nx, ny, nz};
+    const int64_t n = (int64_t)nx * ny * nz;
+    k_conv_fwd_f32<<<(int)ceil_div<int64_t>(n, 256), 256, 0, stream>>>(g, cin, cout, in, W, relu, out);
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+GB_API int gb_conv3_bwd_data_f32(int nx, int ny, int nz, int cin, int cout, const float* gout, const float* W,
+                                 float* gin, cudaStream_t stream)
+{
+    GB_REQUIRE(cin >= 1 && cin <= CN && cout >= 1 && cout <= CN, "conv3_bwd_data: channels must be 1..16");
+    Grid3 g{nx, ny, nz};
+    const int64_t n = (int64_t)nx * ny * nz;
+    k_conv_bwd_data_f32<<<(int)ceil_div<int64_t>(n, 256), 256, 0, stream>>>(g, cin, cout, gout, W, gin);
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+static int bwd_weight_ctas(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(n, WG_VOX), WG_CTAS)); }
+
+GB_API size_t gb_conv3_bwd_weight_workspace_bytes(int nx, int ny, int nz, int cin, int cout)
+{
+    const int64_t n = (int64_t)nx * ny * nz;
+    return sizeof(float) * (size_t)bwd_weight_ctas(n) * 27 * cin * cout;
+}
+
+// gW += dL/dW (accumulates, so several samples can be summed before an optimiser step)
+GB_API int gb_conv3_bwd_weight_f32(int nx, int ny, int nz, int cin, int cout, const float* in, const float* gout,
+                                   float* gW, void* workspace, size_t workspace_bytes, cudaStream_t stream)
+{
+    GB_REQUIRE(cin >= 1 && cin <= CN && cout >= 1 && cout <= CN, "conv3_bwd_weight: channels must be 1..16");
+    GB_REQUIRE(workspace_bytes >= gb_conv3_bwd_weight_workspace_bytes(nx, ny, nz, cin, cout),
+               "conv3_bwd_weight: workspace too small");
+    Grid3 g{nx, ny, nz};
+    const int64_t n = (int64_t)nx * ny * nz;
+    const int parts = bwd_weight_ctas(n);
+    float* partial = static_cast<float*>(workspace);
+    k_conv_bwd_weight_f32<<<parts, 256, 0, stream>>>(g, cin, cout, in, gout, partial);
+    const int nw = 27 * cin * cout;
+    k_reduce_partials<<<ceil_div(nw, 256), 256, 0, stream>>>(parts, nw, partial, gW);
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+GB_API int gb_relu_bwd(int64_t n, const float* out, float* g, cudaStream_t stream)
+{
+    if (n <= 0) return GB_OK;
+    k_relu_bwd<<<g1(n), 256, 0, stream>>>(n, out, g);
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+GB_API int gb_adam_step(int n, float* w, const float* g, float* m, float* v, float lr, float b1, float b2, float eps,
+                        int step, void* w_bf16, cudaStream_t stream)
+{
+    GB_REQUIRE(n > 0 && step >= 1, "adam: bad arguments");
+    const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+    k_adam<<<ceil_div(n, 256), 256, 0, stream>>>(n, w, g, m, v, lr, b1, b2, eps, c1, c2,
+                                                 static_cast<__nv_bfloat16*>(w_bf16));
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+// features: dtype GB_F32 -> fp32 [n][16], GB_BF16 -> bf16 [n][16]
+GB_API int gb_net_features(int dtype, int64_t n, const float* r, const float* dinv, const float* chat,
+                           const float* mask, void* out, cudaStream_t stream)
+{
+    if (n <= 0) return GB_OK;
+    if (dtype == GB_F32)
+        k_features<float><<<g1(n), 256, 0, stream>>>(n, r, dinv, chat, mask, static_cast<float*>(out));
+    else if (dtype == GB_BF16)
+        k_features<__nv_bfloat16><<<g1(n), 256, 0, stream>>>(n, r, dinv, chat, mask, static_cast<__nv_bfloat16*>(out));
+    else {
+        gb::set_error("net_features: dtype must be f32 or bf16");
+        return GB_ERR_UNSUPPORTED;
+    }
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+GB_API int gb_net_cell_features(int nx, int ny, int nz, const float* cell_coef, float mean_log, float inv_std,
+                                float* chat, cudaStream_t stream)
+{
+    Grid3 g{nx, ny, nz};
+    const int64_t n = (int64_t)nx * ny * nz;
+    k_cell_features<<<(int)ceil_div<int64_t>(n, 256), 256, 0, stream>>>(g, cell_coef, mean_log, inv_std, chat);
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+GB_API int gb_net_combine(int dtype, int64_t n, int stride, const void* act, const float* mask, float omega,
+                          const float* dinv, const float* r, float* out, cudaStream_t stream)
+{
+    if (n <= 0) return GB_OK;
+    if (dtype == GB_F32)
+        k_net_combine<float><<<g1(n), 256, 0, stream>>>(n, stride, static_cast<const float*>(act), mask, omega, dinv, r,
+                                                        out);
+    else
+        k_net_combine<__nv_bfloat16><<<g1(n), 256, 0, stream>>>(n, stride, static_cast<const __nv_bfloat16*>(act), mask,
+                                                                omega, dinv, r, out);
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+// bf16 tensor-core layer: cout 16 (hidden, ReLU) or 8 (last layer, linear).
+// in [V][16] bf16, Wt [27][cout][16] bf16 (16-byte aligned), out [V][cout] bf16.
+GB_API int gb_conv3_fwd_bf16(int nx, int ny, int nz, int cout, int relu, const void* in, const void* Wt, void* out,
+                             cudaStream_t stream)
+{
+    GB_REQUIRE(((uintptr_t)in % 16 == 0) && ((uintptr_t)Wt % 16 == 0) && ((uintptr_t)out % 4 == 0),
+               "conv3_fwd_bf16: misaligned arrays");
+    Grid3 g{nx, ny, nz};
+    dim3 grid(ceil_div(nx, BX), ceil_div(ny, BY), ceil_div(nz, BZ));
+    const __nv_bfloat16* i = static_cast<const __nv_bfloat16*>(in);
+    const __nv_bfloat16* w = static_cast<const __nv_bfloat16*>(Wt);
+    __nv_bfloat16* o = static_cast<__nv_bfloat16*>(out);
+    if (cout == 16 && relu)
+        k_conv_fwd_bf16_mma<16, true><<<grid, 128, 0, stream>>>(g, i, w, o);
+    else if (cout == 16)
+        k_conv_fwd_bf16_mma<16, false><<<grid, 128, 0, stream>>>(g, i, w, o);
+    else if (cout == 8 && !relu)
+        k_conv_fwd_bf16_mma<8, false><<<grid, 128, 0, stream>>>(g, i, w, o);
+    else {
+        gb::set_error("conv3_fwd_bf16: cout must be 16 (hidden) or 8 (last layer, linear)");
+        return GB_ERR_UNSUPPORTED;
+    }
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
