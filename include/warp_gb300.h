@@ -214,6 +214,15 @@ int gb_net_combine(int dtype, int64_t n, int stride, const void* act, const floa
                    const float* r, float* out, gb_stream_t stream);
 int gb_conv3_fwd_bf16(int nx, int ny, int nz, int cout, int relu, const void* in, const void* Wt, void* out,
                       gb_stream_t stream);
+/* tcgen05 implicit-GEMM layers on the planar padded layout: the grid padded by one zero voxel per side,
+ * row p = ((x+1)(ny+2) + (y+1))(nz+2) + (z+1), channels 0-7 in plane 0 and 8-15 in plane 1 (16 B per row),
+ * planes gb_conv3_planar_rows() rows apart, border rows zero.  last = 0: ReLU layer, planar bf16 out;
+ * last = 1: w = omega dinv r + (mask ? 0 : channel 0) in fp32.  Wt: [27][16][16] bf16. */
+int64_t gb_conv3_planar_rows(int nx, int ny, int nz);
+int gb_net_features_planar(int nx, int ny, int nz, const float* r, const float* dinv, const float* chat,
+                           const float* mask, void* out, gb_stream_t stream);
+int gb_conv3_fwd_tc(int nx, int ny, int nz, int last, const void* in, const void* Wt, void* out, float* w,
+                    const float* r, const float* dinv, const float* mask, float omega, int* status, gb_stream_t stream);
 
 #ifdef __cplusplus
 }

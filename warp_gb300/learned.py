@@ -84,12 +84,12 @@ class ConvNet:
         net.step_count = int(d["steps"])
         return net
 
-    def bf16_weights(self) -> list[torch.Tensor]:
-        """Inference layout Wt[t][co_pad][ci] bf16 (co padded to 8 for the last layer)."""
+    def bf16_weights(self, last_cout: int = 8) -> list[torch.Tensor]:
+        """Inference layout Wt[t][co_pad][ci] bf16 (co padded to ``last_cout`` for the last layer)."""
         out = []
         for (ci, co, _), w in zip(LAYERS, self.W):
             wt = w.reshape(27, ci, co).permute(0, 2, 1)  # [t][co][ci]
-            cop = 16 if co == 16 else 8
+            cop = 16 if co == 16 else last_cout
             full = torch.zeros(27, cop, CH, device=w.device, dtype=torch.float32)
             full[:, :co, :ci] = wt
             out.append(full.to(torch.bfloat16).contiguous())
@@ -153,29 +153,80 @@ def cell_features(dims, coef: torch.Tensor, mean_log: float, inv_std: float) -> 
     return chat
 
 
+def planar_rows(dims) -> int:
+    return int(N.lib().gb_conv3_planar_rows(*dims))
+
+
+def to_planar(act: torch.Tensor, dims) -> torch.Tensor:
+    """[n, 16] activations -> planar padded bf16 buffer [2, rows, 8] (border rows zero)."""
+    nx, ny, nz = dims
+    rows = planar_rows(dims)
+    buf = torch.zeros(2, rows, 8, dtype=torch.bfloat16, device=act.device)
+    p = padded_rows(dims, act.device)
+    a = act.reshape(-1, 16).to(torch.bfloat16)
+    buf[0, p] = a[:, :8]
+    buf[1, p] = a[:, 8:]
+    return buf
+
+
+def from_planar(buf: torch.Tensor, dims) -> torch.Tensor:
+    p = padded_rows(dims, buf.device)
+    return torch.cat([buf[0, p], buf[1, p]], dim=1)
+
+
+def padded_rows(dims, device) -> torch.Tensor:
+    nx, ny, nz = dims
+    v = torch.arange(nx * ny * nz, device=device)
+    x, y, z = v // (ny * nz), (v // nz) % ny, v % nz
+    return ((x + 1) * (ny + 2) + (y + 1)) * (nz + 2) + (z + 1)
+
+
 class LearnedSmoother:
-    """The inference smoother plugged into ``MultigridPreconditioner.smoother``: bf16 tensor-core
-    layers, 6 launches (features, 4 convolutions, combine)."""
+    """The inference smoother plugged into ``MultigridPreconditioner.smoother``.
 
-    kernels_per_apply = 6
+    backend "tc": tcgen05 implicit-GEMM layers on the planar padded layout (features + 4 layers, the
+    last one fused with the Jacobi step: 5 launches); backend "mma": the legacy mma.sync layers on
+    the plain channels-last layout (features, 4 layers, combine: 6 launches)."""
 
-    def __init__(self, net: ConvNet, mg: multigrid.MultigridPreconditioner, coef):
+    def __init__(self, net: ConvNet, mg: multigrid.MultigridPreconditioner, coef, backend: str = "tc"):
         lv = mg.levels[0]
         if len(lv.dims) != 3:
             raise ValueError("learned smoother: 3-D grids only")
+        if backend not in ("tc", "mma"):
+            raise ValueError(f"unknown backend {backend!r}")
+        self.backend = backend
         self.mg = mg
         self.dims = lv.dims
         self.n = lv.n
         self.omega = mg.omega
         self.mask, self.dinv = lv.mask, lv.dinv
+        self.status = mg.status
         coef_t = coef if isinstance(coef, torch.Tensor) else A.from_numpy(np.asarray(coef, np.float32).reshape(-1))
         self.chat = cell_features(self.dims, coef_t.reshape(-1).float().contiguous(), net.mean_log, net.inv_std)
-        self.Wt = net.bf16_weights()
-        self.buf = [A.empty(self.n * CH, torch.bfloat16), A.empty(self.n * CH, torch.bfloat16)]
-        self.out8 = self.buf[1]  # the last layer (8 channels) writes into the second buffer
+        if backend == "tc":
+            self.Wt = net.bf16_weights(last_cout=16)
+            rows = planar_rows(self.dims)
+            self.buf = [A.zeros(2 * rows * 8, torch.bfloat16), A.zeros(2 * rows * 8, torch.bfloat16)]
+            self.kernels_per_apply = 5
+        else:
+            self.Wt = net.bf16_weights(last_cout=8)
+            self.buf = [A.empty(self.n * CH, torch.bfloat16), A.empty(self.n * CH, torch.bfloat16)]
+            self.kernels_per_apply = 6
 
     def launch(self, stream, r: int, w: int) -> None:
         L = N.lib()
+        if self.backend == "tc":
+            N.check(L.gb_net_features_planar(*self.dims, r, A.ptr(self.dinv), A.ptr(self.chat), A.ptr(self.mask),
+                                             A.ptr(self.buf[0]), stream), "features")
+            src, dst = self.buf[0], self.buf[1]
+            for li, wt in enumerate(self.Wt):
+                last = li == len(self.Wt) - 1
+                N.check(L.gb_conv3_fwd_tc(*self.dims, int(last), A.ptr(src), A.ptr(wt), None if last else A.ptr(dst),
+                                          w if last else None, r if last else None, A.ptr(self.dinv) if last else None,
+                                          A.ptr(self.mask) if last else None, self.omega, A.ptr(self.status), stream),
+                        "conv tc")
+                src, dst = dst, src
+            return
         N.check(L.gb_net_features(N.GB_BF16, self.n, r, A.ptr(self.dinv), A.ptr(self.chat), A.ptr(self.mask),
                                   A.ptr(self.buf[0]), stream), "features")
         src, dst = self.buf[0], self.buf[1]

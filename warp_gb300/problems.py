@@ -26,15 +26,18 @@ class System:
 
 
 def diffusion(res, sigma: float = 1.5, corr_length: float = 0.1, seed: int = 0, lognormal: bool = True,
-              constant: float | None = None, field_cell_size: float | None = None) -> System:
+              constant: float | None = None, field_cell_size: float | None = None, coef=None) -> System:
     """-div(a grad u) = f, Q1 on a unit Grid2D/Grid3D, a = exp(g) with g a squared-exponential GRF
     (correlation ``corr_length``, std ``sigma``) per cell, f ~ U[-1, 1] per node, u = 0 on the whole
     boundary imposed by projection.  ``field_cell_size`` samples the field as if the cells had that
-    size (a sub-block of a finer grid: same correlation length in cells)."""
+    size (a sub-block of a finer grid: same correlation length in cells); ``coef`` gives the per-cell
+    coefficient directly."""
     res = tuple(int(r) for r in res)
     geo = fem.Grid2D(res=res) if len(res) == 2 else fem.Grid3D(res=res)
     rng = np.random.default_rng(seed)
-    if constant is not None:
+    if coef is not None:
+        coef = np.asarray(coef, np.float64).reshape(-1)
+    elif constant is not None:
         coef = np.full(geo.cell_count(), float(constant))
     elif lognormal:
         cs = None if field_cell_size is None else (float(field_cell_size),) * len(res)
