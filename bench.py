@@ -3,14 +3,19 @@
 Workload (default): 96^3 Q1 scalar diffusion, a = exp(g) with g a squared-exponential Gaussian
 random field (correlation 0.1, sigma 1.5), f ~ U[-1,1] per node, zero Dirichlet boundary by
 projection: n = 912,673 dofs, 24,137,569 nonzeros.  A step is one solve from x = 0 to an FP64
-relative residual ||b - A x|| / ||b|| <= 1e-8 (FP32 Jacobi-CG inner loop, FP64 iterative
-refinement), inputs resident in HBM.  The matrix (204 MB of values + columns) is larger than the
-129 MB L2, so no L2 flush is needed between steps.
+relative residual ||b - A x|| / ||b|| <= 1e-8 with the learned preconditioner: flexible CG in FP32
+whose preconditioner is a multigrid V-cycle with the trained conv-net fine-level smoother (bf16
+tcgen05 layers), inside FP64 iterative refinement; operator and preconditioner resident in HBM
+(their set-up is timed separately).  The matrix (204 MB of values + columns) is larger than the
+129 MB L2, so no L2 flush is needed between steps.  The same system is also solved by the plain
+Jacobi-CG drop-in (the judge of the learned method) and by flexible CG with the Jacobi-smoothed
+V-cycle (the method without the network).
 
-Printed (rank 0, one JSON line): value = solve time (ms), e2e = the same solve through the public
-API with host-resident inputs (matrix + rhs copied in, solution copied out, inside the timed
-region), roofline of the dominant kernel (the BSR SpMV) against the measured HBM copy peak,
-cpu_baseline = the oracle's FP64 Jacobi-PCG on the host cores (bounded sample).
+Printed (rank 0, one JSON line): value = learned-FCG solve time (ms); e2e = the same solve through
+the public API with the right-hand side copied in from pinned host memory and the FP64 solution
+copied out inside the timed region (e2e_with_setup adds the matrix and coefficient copies and the
+whole preconditioner set-up); roofline of the dominant kernel (the BSR SpMV) against the measured
+HBM copy peak; cpu_baseline = the oracle's FP64 Jacobi-PCG on the host cores (bounded sample).
 
 ``--impl reference`` times the reference's CPU implementation of this path (the oracle port of
 Warp's CG; the reference's own CPU build needs its LLVM JIT, which is not available here) on all
@@ -33,7 +38,8 @@ sys.path.insert(0, ROOT)
 
 METRIC = "Solve time to 1e-8 rel. residual: learned-FCG vs Jacobi-CG; bsr_mv HBM GB/s"
 WORKLOAD = ("96^3 Q1 lognormal diffusion (GRF l=0.1, sigma=1.5), 912,673 dofs, 24.1M nnz; "
-            "Jacobi-CG FP32 inner + FP64 refinement to 1e-8 FP64 relative residual")
+            "learned-preconditioned FCG (multigrid V-cycle + trained conv-net smoother) FP32 inner + FP64 "
+            "refinement to 1e-8 FP64 relative residual")
 
 
 def _peaks():
@@ -215,9 +221,19 @@ def run_profile(args):
         x = torch.zeros_like(system.b)
         linear.cg(A, system.b, x, tol=1e-12, atol=0.0, maxiter=30, M=linear.preconditioner(A, "diag"),
                   check_every=30, use_cuda_graph=False)
-    else:
+    elif args.profile == "jacobi_solve":
         solver = linear.RefinedSolver(A, M=linear.preconditioner(A, "diag"), inner_tol=args.inner_tol)
         solver.solve(system.b, tol=1e-8)
+    else:  # the learned-FCG solve of the bench line (set-up, one warm-up solve, one solve)
+        from warp_gb300 import learned, multigrid
+
+        net = learned.ConvNet.load(args.weights)
+        mg = multigrid.MultigridPreconditioner(A, system.geo, system.coef)
+        mg.smoother = learned.LearnedSmoother(net, mg, system.coef, backend="tc")
+        # eager launches (host check per iteration) so that every kernel of the solve is listed
+        solver = linear.RefinedSolver(A, M=mg, method="fcg", inner_tol=args.inner_tol, use_cuda_graph=False)
+        for _ in range(2):
+            solver.solve(system.b, tol=1e-8)
     torch.cuda.synchronize()
     print("profile run done", flush=True)
     return 0
@@ -236,10 +252,11 @@ def main():
     p.add_argument("--ref-iters", type=int, default=50)
     p.add_argument("--ref-full-iters", type=int, default=2000)
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--profile", choices=["spmv", "cg", "solve"], default=None,
+    p.add_argument("--weights", default=os.path.join(ROOT, "warp_gb300", "data", "smoother_q1_diffusion.npz"))
+    p.add_argument("--profile", choices=["spmv", "cg", "jacobi_solve", "solve"], default=None,
                    help="run a fixed kernel sequence for an ncu capture and exit (prints no bench line): "
                         "spmv = 8 bsr_mv launches, cg = 30 eager (non-graph) Jacobi-CG iterations, "
-                        "solve = one refined solve")
+                        "jacobi_solve = one refined Jacobi-CG solve, solve = two learned-FCG solves (eager launches)")
     args = p.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 
@@ -266,59 +283,77 @@ def main():
     A = system.A
     n = A.nrow
     nnz = A.nnz_sync()
-    M = linear.preconditioner(A, "diag")
-    solver = linear.RefinedSolver(A, M=M, inner_tol=args.inner_tol)
     stream = torch.cuda.current_stream()
+    from warp_gb300 import learned, multigrid
 
-    # ---- warm-up -----------------------------------------------------------------------------
-    for _ in range(args.warmup):
-        x64, info = solver.solve(system.b, tol=1e-8)
-    torch.cuda.synchronize()
-
-    # ---- timed solves (inputs resident) ------------------------------------------------------
-    infos = []
-    sampler = ClockSampler(local)
-    with sampler:
+    def timed(solver, b, steps, sample_clocks=False):
+        for _ in range(args.warmup):
+            solver.solve(b, tol=1e-8)
+        torch.cuda.synchronize()
+        infos = []
+        sampler = ClockSampler(local) if sample_clocks else None
+        if sampler:
+            sampler.__enter__()
         if ws > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         launches0 = solver.kernel_launches
         e0.record(stream)
-        for _ in range(args.steps):
-            x64, info = solver.solve(system.b, tol=1e-8)
+        for _ in range(steps):
+            _, info = solver.solve(b, tol=1e-8)
             infos.append(info)
         e1.record(stream)
-        solver.kernel_launches_timed = solver.kernel_launches - launches0
         torch.cuda.synchronize()
+        launches = solver.kernel_launches - launches0
         if ws > 1:
             torch.distributed.barrier()
-    ms = e0.elapsed_time(e1) / args.steps
-    ms = _barrier_max(ms, ws)
-    clocks = sampler.summary()
+        if sampler:
+            sampler.__exit__(None, None, None)
+        ms_ = _barrier_max(e0.elapsed_time(e1) / steps, ws)
+        return ms_, infos, launches, (sampler.summary() if sampler else None)
 
-    # ---- flexible CG with the multigrid preconditioner (set-up timed separately) -------------
-    from warp_gb300 import multigrid
+    # ---- learned preconditioner: set-up (timed separately) and the headline solve -------------
+    torch.cuda.synchronize()
+    s0 = time.perf_counter()
+    net = learned.ConvNet.load(args.weights)
+    lmg = multigrid.MultigridPreconditioner(A, system.geo, system.coef)
+    lmg.smoother = learned.LearnedSmoother(net, lmg, system.coef, backend="tc")
+    lsolver = linear.RefinedSolver(A, M=lmg, method="fcg", inner_tol=args.inner_tol)
+    torch.cuda.synchronize()
+    setup_ms = (time.perf_counter() - s0) * 1e3
+    ms, linfos, llaunch, clocks = timed(lsolver, system.b, args.steps, sample_clocks=True)
 
+    # ---- plain Jacobi-CG drop-in (the judge) -------------------------------------------------
+    M = linear.preconditioner(A, "diag")
+    jsolver = linear.RefinedSolver(A, M=M, inner_tol=args.inner_tol)
+    jms, jinfos, _, jclocks = timed(jsolver, system.b, args.steps, sample_clocks=True)
+
+    # ---- the same flexible CG without the network (Jacobi-smoothed V-cycle) -------------------
     torch.cuda.synchronize()
     s0 = time.perf_counter()
     mg = multigrid.MultigridPreconditioner(A, system.geo, system.coef)
     fsolver = linear.RefinedSolver(A, M=mg, method="fcg", inner_tol=args.inner_tol)
     torch.cuda.synchronize()
     mg_setup_ms = (time.perf_counter() - s0) * 1e3
-    for _ in range(args.warmup):
-        fsolver.solve(system.b, tol=1e-8)
+    fcg_ms, finfos, _, _ = timed(fsolver, system.b, args.steps)
+
+    # ---- the learned smoother's layers (tensor-core roofline) ----------------------------------
+    sm = lmg.smoother
+    r_t = torch.randn(n, device="cuda") * (1 - lmg.levels[0].mask)
+    w_t = torch.empty_like(r_t)
+    for _ in range(3):
+        sm.launch(stream.cuda_stream, r_t.data_ptr(), w_t.data_ptr())
     torch.cuda.synchronize()
-    finfos = []
-    with ClockSampler(local) as fsampler:
-        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        f0.record(stream)
-        for _ in range(args.steps):
-            _, finfo = fsolver.solve(system.b, tol=1e-8)
-            finfos.append(finfo)
-        f1.record(stream)
-        torch.cuda.synchronize()
-    fcg_ms = _barrier_max(f0.elapsed_time(f1) / args.steps, ws)
+    c0, c1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    c0.record(stream)
+    for _ in range(20):
+        sm.launch(stream.cuda_stream, r_t.data_ptr(), w_t.data_ptr())
+    c1.record(stream)
+    torch.cuda.synchronize()
+    smoother_us = c0.elapsed_time(c1) / 20 * 1e3
+    net_flop = 2.0 * 27 * (16 * 16 * 3 + 16 * 1) * n  # useful MACs x 2 of the four layers
+    net_tflops = net_flop / (smoother_us * 1e-6) / 1e12
 
     # ---- SpMV roofline (dominant kernel) -----------------------------------------------------
     hbm_peak, peak_kind = _peaks()
@@ -346,33 +381,14 @@ def main():
         pass
 
     # ---- end to end through the public API with host-resident inputs -------------------------
-    off_h = A.offsets.cpu().pin_memory()
-    col_h = A.columns[:nnz].cpu().pin_memory()
-    val_h = A.values[:nnz].cpu().pin_memory()
     b_h = system.b.cpu().pin_memory()
     x_h = torch.empty(n, dtype=torch.float64).pin_memory()
-    h2d = off_h.numel() * 4 + col_h.numel() * 4 + val_h.numel() * 4 + b_h.numel() * 4
-    d2h = n * 8
-    E = sparse.bsr_zeros(n, n, torch.float32)
-    E.offsets = torch.empty_like(A.offsets)
-    E.columns = torch.empty(nnz, dtype=torch.int32, device="cuda")
-    E.values = torch.empty(nnz, dtype=torch.float32, device="cuda")
-    E.nnz = nnz
     bE = torch.empty(n, dtype=torch.float32, device="cuda")
-    E.offsets.copy_(off_h)
-    E.columns.copy_(col_h)
-    E.values.copy_(val_h)
-    ME = linear.preconditioner(E, "diag")
-    solverE = linear.RefinedSolver(E, M=ME, inner_tol=args.inner_tol)
 
     def e2e_step():
-        # a user's repeated solve: new matrix values / rhs arrive from the host every step
-        E.offsets.copy_(off_h, non_blocking=True)
-        E.columns.copy_(col_h, non_blocking=True)
-        E.values.copy_(val_h, non_blocking=True)
+        # a user's solve: the right-hand side arrives from the host, the solution goes back
         bE.copy_(b_h, non_blocking=True)
-        linear.refresh_preconditioner(ME, E)
-        xs, inf = solverE.solve(bE, tol=1e-8)
+        xs, inf = lsolver.solve(bE, tol=1e-8)
         x_h.copy_(xs, non_blocking=True)
         return inf
 
@@ -386,15 +402,50 @@ def main():
     g1.record(stream)
     torch.cuda.synchronize()
     e2e_ms = _barrier_max(g0.elapsed_time(g1) / args.steps, ws)
+    h2d, d2h = n * 4, n * 8
 
-    inner_iters = [i["inner_iterations"] for i in infos]
-    outer = [i["outer"] for i in infos]
-    # counted by the solver: residuals, argument stores, CG inits, solution updates, 3 per CG iteration
-    gpu_launches = int(solver.kernel_launches_timed)
+    # with set-up: matrix, coefficient field and rhs from the host, preconditioner rebuilt, solve
+    off_h = A.offsets.cpu().pin_memory()
+    col_h = A.columns[:nnz].cpu().pin_memory()
+    val_h = A.values[:nnz].cpu().pin_memory()
+    coef_h = torch.from_numpy(np.asarray(system.coef, np.float32).reshape(-1)).pin_memory()
+    E = sparse.bsr_zeros(n, n, torch.float32)
+    E.offsets = torch.empty_like(A.offsets)
+    E.columns = torch.empty(nnz, dtype=torch.int32, device="cuda")
+    E.values = torch.empty(nnz, dtype=torch.float32, device="cuda")
+    E.nnz = nnz
+    coefE = torch.empty(coef_h.numel(), dtype=torch.float32, device="cuda")
+
+    def e2e_setup_step():
+        E.offsets.copy_(off_h, non_blocking=True)
+        E.columns.copy_(col_h, non_blocking=True)
+        E.values.copy_(val_h, non_blocking=True)
+        coefE.copy_(coef_h, non_blocking=True)
+        bE.copy_(b_h, non_blocking=True)
+        pm = multigrid.MultigridPreconditioner(E, system.geo, coefE)
+        pm.smoother = learned.LearnedSmoother(net, pm, coefE, backend="tc")
+        sol = linear.RefinedSolver(E, M=pm, method="fcg", inner_tol=args.inner_tol)
+        xs, inf = sol.solve(bE, tol=1e-8)
+        x_h.copy_(xs, non_blocking=True)
+        torch.cuda.synchronize()
+        return inf
+
+    e2e_setup_step()
+    t0 = time.perf_counter()
+    for _ in range(max(1, min(args.steps, 3))):
+        e2e_setup_step()
+    e2e_setup_ms = (time.perf_counter() - t0) * 1e3 / max(1, min(args.steps, 3))
+    h2d_setup = off_h.numel() * 4 + col_h.numel() * 4 + val_h.numel() * 4 + coef_h.numel() * 4 + n * 4
+
+    inner_iters = [i["inner_iterations"] for i in linfos]
+    outer = [i["outer"] for i in linfos]
+    # counted by the solver: residuals, argument stores, FCG inits, solution updates, and per FCG
+    # iteration its 4 kernels + the V-cycle's (learned smoother included)
+    gpu_launches = int(llaunch)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline_sample(system, int(statistics.median(inner_iters)))
+        cpu = cpu_baseline_sample(system, int(statistics.median([i["inner_iterations"] for i in jinfos])))
 
     line = {
         "metric": METRIC,
@@ -407,29 +458,34 @@ def main():
         "higher_is_better": False,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32+f64",
+        "dtype": "f32+f64 (bf16 conv net)",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "solver": "jacobi_cg_refined", "n_dofs": n, "nnz": nnz,
+        "config": {"workload": WORKLOAD, "solver": "learned_fcg_refined", "n_dofs": n, "nnz": nnz,
                    "parallelism": f"replicas{ws}", "l2": "inputs > L2 (matrix 204 MB vs 129 MB L2), no flush",
-                   "inner_tol": args.inner_tol},
+                   "inner_tol": args.inner_tol, "weights": os.path.relpath(args.weights, ROOT),
+                   "mg_levels": lmg.describe()},
         "roofline": {"bound": "hbm", "kernel": "k_bsr_mv<1,1,float>", "achieved": mv_gbs, "peak": hbm_peak,
                      "unit": "GB/s", "frac": mv_gbs / hbm_peak, "peak_kind": peak_kind,
                      "algorithmic_bytes": mv_bytes, "traffic": traffic, "launch_us": mv_s * 1e6},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e_with_setup": {"value": e2e_setup_ms, "unit": "ms", "h2d_bytes_per_step": h2d_setup,
+                           "d2h_bytes_per_step": d2h, "timing": "host wall clock, synchronised"},
         "gpu_launches": gpu_launches,
         "clocks": clocks,
-        "jacobi_cg_ms": ms,
-        "mg_fcg_ms": fcg_ms,
-        "mg_fcg_iterations": statistics.median([f["inner_iterations"] for f in finfos]),
-        "mg_fcg_rel_residual": max(f["rel_residual"] for f in finfos),
-        "mg_fcg_fallbacks": fsolver.fallbacks,
-        "mg_setup_ms": mg_setup_ms,
-        "mg_levels": mg.describe(),
+        "learned_fcg": {"ms": ms, "inner_iterations": statistics.median(inner_iters),
+                        "outer_iterations": statistics.median(outer),
+                        "rel_residual": max(i["rel_residual"] for i in linfos), "fallbacks": lsolver.fallbacks,
+                        "setup_ms": setup_ms, "speedup_vs_jacobi_cg": jms / ms},
+        "jacobi_cg": {"ms": jms, "inner_iterations": statistics.median([i["inner_iterations"] for i in jinfos]),
+                      "outer_iterations": statistics.median([i["outer"] for i in jinfos]),
+                      "rel_residual": max(i["rel_residual"] for i in jinfos), "clocks": jclocks},
+        "mg_fcg_no_net": {"ms": fcg_ms, "inner_iterations": statistics.median([f["inner_iterations"] for f in finfos]),
+                          "rel_residual": max(f["rel_residual"] for f in finfos), "fallbacks": fsolver.fallbacks,
+                          "setup_ms": mg_setup_ms},
+        "conv_net": {"smoother_us": smoother_us, "launches": sm.kernels_per_apply, "useful_tflops": net_tflops,
+                     "backend": "tcgen05 kind::f16 bf16 x bf16 -> fp32"},
         "bsr_mv_gbs": mv_gbs,
-        "inner_iterations": statistics.median(inner_iters),
-        "outer_iterations": statistics.median(outer),
-        "rel_residual": max(i["rel_residual"] for i in infos),
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -224,6 +224,26 @@ int gb_net_features_planar(int nx, int ny, int nz, const float* r, const float* 
 int gb_conv3_fwd_tc(int nx, int ny, int nz, int last, const void* in, const void* Wt, void* out, float* w,
                     const float* r, const float* dinv, const float* mask, float omega, int* status, gb_stream_t stream);
 
+/* ---- Batched solves --------------------------------------------------------------------------
+ * gb_batched_pcg replaces the batched CG of warp/_src/optim/linear.py:893-1032 (LinearOperator with
+ * batch_offsets, :33-133; per-subproblem tolerances :2063-2083; frozen converged subproblems
+ * :2333-2373) for a block-diagonal compact CSR (1x1 BSR) fp32 matrix with Jacobi (dinv) or no
+ * preconditioner: one persistent launch in which each CTA -- or, for subproblems of at most small_rows
+ * rows, each warp -- runs one subproblem's CG to its own convergence, taking subproblems from a queue
+ * in the order `order` (largest first).  Rows >= batch_offsets[nbatch] are not touched.
+ * threads: 128/256/512/1024; lanes_per_row: 1/2/4/8; grid <= 0: automatic.
+ * gb_q1_batched_assemble_2d: block-diagonal Q1 diffusion systems on unit squares (no reference
+ * counterpart: the reference assembles each subproblem with fem.integrate). */
+size_t gb_batched_pcg_workspace_bytes(int64_t n);
+int gb_batched_pcg(int nbatch, const int* batch_offsets, const int* order, int64_t n, const int* offsets,
+                   const int* columns, const float* values, const float* dinv, const float* b, float* x, double rtol,
+                   double atol, int maxiter, int x_is_zero, int threads, int lanes_per_row, int small_rows, int grid,
+                   int* iters, float* rr, float* atol_sq, void* workspace, size_t workspace_bytes, int* status,
+                   gb_stream_t stream);
+int gb_q1_batched_assemble_2d(int nbatch, const int* ncell, const int* row_off, const int* nnz_off,
+                              const int* cell_off, const float* coef, const float* f, int total_rows, int* offsets,
+                              int* columns, float* values, float* rhs, gb_stream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

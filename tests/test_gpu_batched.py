@@ -1,0 +1,206 @@
+"""GPU tests of batched uneven solves: the batched Q1 assembly against the single-problem drop-in
+path, and the persistent batched Jacobi-CG against per-subproblem solves and the reference's batched
+test cases (warp/tests/test_linear_solvers.py:418-575, restated)."""
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _block(Am, b, r0, r1):
+    nnz = Am.nnz_sync()
+    off = Am.offsets.cpu().numpy()
+    col = Am.columns[:nnz].cpu().numpy()
+    val = Am.values[:nnz].cpu().numpy()
+    k0, k1 = off[r0], off[r1]
+    return off[r0:r1 + 1] - k0, col[k0:k1] - r0, val[k0:k1], b[r0:r1].cpu().numpy()
+
+
+def test_batched_q1_assembly_matches_single_problem_path(cuda):
+    """Each block equals fem.integrate + project_linear_system of the same subproblem: structure
+    bit-exact, values and right-hand side within 1e-6 of the row maximum."""
+    from warp_gb300 import batched, problems
+
+    ncells = [4, 7, 16, 5]
+    Am, b, offs, fld = batched.q1_batch_2d(ncells, seed=3, return_fields=True)
+    row_off, cell_off = fld["row_off"], fld["cell_off"]
+    for i, n in enumerate(ncells):
+        coef = fld["coef"][cell_off[i]:cell_off[i + 1]]
+        f = fld["f"][row_off[i]:row_off[i + 1]]
+        s = problems.diffusion((n, n), coef=coef, f=f)
+        o1, c1, v1, b1 = _block(Am, b, int(row_off[i]), int(row_off[i + 1]))
+        nnz = s.A.nnz_sync()
+        o2 = s.A.offsets.cpu().numpy()
+        c2 = s.A.columns[:nnz].cpu().numpy()
+        v2 = s.A.values[:nnz].cpu().numpy()
+        np.testing.assert_array_equal(o1, o2)
+        np.testing.assert_array_equal(c1, c2)
+        rowmax = np.repeat(np.maximum.reduceat(np.abs(v2), o2[:-1]), np.diff(o2))
+        assert np.all(np.abs(v1 - v2) <= 1e-6 * rowmax + 1e-12)
+        b2 = s.b.cpu().numpy()
+        assert np.abs(b1 - b2).max() <= 1e-6 * np.abs(b2).max()
+
+
+def _batched_residuals(Am, b, x, offs, tol, iters, scale=32.0):
+    """True residual of every subproblem <= scale * tol * ||b_i|| (the reference's per-batch check)
+    plus the fp32 drift of the recursive residual, (16 + 2 k_i) eps ||(|A| |x|)_i|| after k_i
+    iterations (Q1 systems with ||b|| ~ h^2 reach that floor before the relative tolerance)."""
+    nnz = Am.nnz_sync()
+    off = Am.offsets.cpu().numpy()
+    col = Am.columns[:nnz].cpu().numpy()
+    val = Am.values[:nnz].cpu().numpy()
+    bh, xh = b.cpu().numpy().astype(np.float64), x.cpu().numpy().astype(np.float64)
+    ax = oracle.bsr_mv_f64(off, col, val, xh)
+    absax = oracle.bsr_mv_f64(off, col, np.abs(val), np.abs(xh))
+    for i in range(len(offs) - 1):
+        sl = slice(offs[i], offs[i + 1])
+        res = np.linalg.norm(ax[sl] - bh[sl])
+        drift = (16 + 2 * int(iters[i])) * 2.0 ** -24 * np.linalg.norm(absax[sl])
+        bound = scale * tol * np.linalg.norm(bh[sl]) + drift
+        assert res <= bound, f"subproblem {i}: {res:.3e} > {bound:.3e}"
+
+
+@pytest.mark.parametrize("config", [None, {"threads": 256, "lanes_per_row": 1, "small_rows": 0},
+                                    {"threads": 1024, "lanes_per_row": 4, "small_rows": 4096}])
+def test_batched_cg_each_subproblem_converges(cuda, config):
+    """Uneven Q1 subproblems in one launch: every subproblem meets its own tolerance (the reference's
+    per-batch check, scale 32 for fp32) and takes the iterations of the same Jacobi-CG run alone
+    (oracle) within 2."""
+    from warp_gb300 import batched
+    from warp_gb300.optim import linear
+
+    ncells = [16, 3, 40, 8, 25, 12, 2, 33, 20, 6]
+    Am, b, offs = batched.q1_batch_2d(ncells, seed=5)
+    offs_h = offs.cpu().numpy()
+    M = linear.preconditioner(Am, "diag")
+    x = torch.zeros_like(b)
+    op = linear.aslinearoperator(Am, batch_offsets=offs, max_batch_length=int(np.diff(offs_h).max()))
+    # relative tolerance only (with tol alone the reference rule also sets atol = tol)
+    state = linear.cg(op, b, x, tol=1e-6, atol=0.0, maxiter=2000, M=M, check_every=0, run=False)
+    if config is not None:
+        state(op, b, x)  # builds the batched solver
+        state._batched.config = dict(config)
+        state._batched._graph = None
+        x.zero_()
+    it, rr, atol_sq = state(op, b, x)
+    assert rr.shape == (len(ncells),) and atol_sq.shape == (len(ncells),)
+    assert bool((rr <= atol_sq).all())
+    iters = state._batched.iters.cpu().numpy()
+    _batched_residuals(Am, b, x, offs_h, 1e-6, iters)
+    xh = x.cpu().numpy().astype(np.float64)
+    nnz = Am.nnz_sync()
+    off = Am.offsets.cpu().numpy()
+    col = Am.columns[:nnz].cpu().numpy()
+    val = Am.values[:nnz].cpu().numpy()
+    bh = b.cpu().numpy()
+    for i in range(len(ncells)):
+        r0, r1 = int(offs_h[i]), int(offs_h[i + 1])
+        k0, k1 = off[r0], off[r1]
+        o = off[r0:r1 + 1] - k0
+        c = col[k0:k1] - r0
+        v = val[k0:k1]
+        dinv = oracle.inverse_diagonal_f32(o, c, v)
+        x_ref, it_ref, _, _ = oracle.pcg_f32(o, c, v, bh[r0:r1], inv_diag=dinv, tol=1e-6, atol=0.0, maxiter=2000)
+        assert abs(int(iters[i]) - it_ref) <= 2, (i, iters[i], it_ref)
+        # true residual no worse than the oracle's own fp32 solve (plus the relative tolerance)
+        res = np.linalg.norm(oracle.bsr_mv_f64(o, c, v, xh[r0:r1]) - bh[r0:r1])
+        res_ref = np.linalg.norm(oracle.bsr_mv_f64(o, c, v, x_ref) - bh[r0:r1])
+        assert res <= 2.0 * res_ref + 32 * 1e-6 * np.linalg.norm(bh[r0:r1]), (i, res, res_ref)
+    assert int(it.item()) == int(iters.max())
+
+
+def test_batched_subproblem_result_is_independent_of_the_batch(cuda):
+    """With a fixed configuration a subproblem's iterate does not depend on the rest of the batch
+    (each is solved by one CTA or warp): bitwise equal alone and inside the batch."""
+    from warp_gb300 import batched
+
+    ncells = [12, 30, 5, 22]
+    Am, b, offs = batched.q1_batch_2d(ncells, seed=7)
+    cfg = {"threads": 512, "lanes_per_row": 2, "small_rows": 1024}
+    from warp_gb300.optim import linear
+
+    M = linear.preconditioner(Am, "diag")
+    full = batched.BatchedCG(Am, offs, M._inv_diag, 1e-6, 0.0, 1000, config=cfg)
+    x = torch.zeros_like(b)
+    full.solve(b, x)
+    offs_h = offs.cpu().numpy()
+    for k in (1, 2):
+        sub_offs = torch.tensor([offs_h[k], offs_h[k + 1]], dtype=torch.int32)
+        one = batched.BatchedCG(Am, sub_offs, M._inv_diag, 1e-6, 0.0, 1000, config=cfg)
+        x1 = torch.zeros_like(b)
+        one.solve(b, x1)
+        sl = slice(int(offs_h[k]), int(offs_h[k + 1]))
+        assert torch.equal(x1[sl], x[sl])
+        assert int(one.iters[0]) == int(full.iters[k])
+
+
+def test_batched_dense_spd_systems(cuda):
+    """Restates test_batched_cg / test_batched_nonuniform: dense SPD blocks, per-batch residuals."""
+    from warp_gb300.optim import linear
+
+    rng = np.random.default_rng(0)
+    for sizes in ([20] * 4, [8, 15, 10, 12]):
+        n = sum(sizes)
+        Ad = np.zeros((n, n), np.float32)
+        bd = np.zeros(n, np.float32)
+        o = 0
+        for s in sizes:
+            Q = rng.standard_normal((s, s))
+            Ad[o:o + s, o:o + s] = (Q @ Q.T + s * np.eye(s)).astype(np.float32)
+            bd[o:o + s] = rng.standard_normal(s)
+            o += s
+        offs = torch.tensor(np.concatenate([[0], np.cumsum(sizes)]), dtype=torch.int32, device="cuda")
+        op = linear.aslinearoperator(torch.from_numpy(Ad).cuda(), batch_offsets=offs, max_batch_length=max(sizes))
+        assert op.batch_count == len(sizes)
+        b = torch.from_numpy(bd).cuda()
+        x = torch.zeros_like(b)
+        linear.cg(op, b, x, tol=1e-5, maxiter=1000)
+        xh = x.cpu().numpy().astype(np.float64)
+        o = 0
+        for s in sizes:
+            sl = slice(o, o + s)
+            res = np.linalg.norm(Ad[sl, sl].astype(np.float64) @ xh[sl] - bd[sl])
+            assert res <= 32 * 1e-5 * np.linalg.norm(bd[sl])
+            o += s
+
+
+def test_batched_inactive_tail_untouched(cuda):
+    """Restates test_batched_inactive_tail (fp32): rows past batch_offsets[-1] keep their values."""
+    from warp_gb300.optim import linear
+
+    diag = torch.tensor([2.0, 3.0, 4.0, 5.0, 6.0], device="cuda")
+    b = torch.tensor([2.0, 6.0, 12.0, 100.0, 200.0], device="cuda")
+    x = torch.tensor([0.0, 0.0, 0.0, 7.0, 8.0], device="cuda")
+    offs = torch.tensor([0, 3], dtype=torch.int32, device="cuda")
+    op = linear.aslinearoperator(diag, batch_offsets=offs, max_batch_length=3)
+    niter, err, atol = linear.cg(op, b, x, tol=1e-6, maxiter=20, check_every=1)
+    assert niter > 1 and err <= atol
+    np.testing.assert_allclose(x.cpu().numpy(), [1.0, 2.0, 3.0, 7.0, 8.0], rtol=1e-6, atol=1e-6)
+
+
+def test_autotuner_picks_a_candidate_and_caches_it(cuda):
+    from warp_gb300 import batched
+    from warp_gb300.optim import linear
+
+    rng = np.random.default_rng(1)
+    ncells = rng.integers(2, 24, size=64)
+    Am, b, offs = batched.q1_batch_2d(ncells, seed=9)
+    M = linear.preconditioner(Am, "diag")
+    solver = batched.BatchedCG(Am, offs, M._inv_diag, 1e-6, 0.0, 2000, config="auto")
+    x = torch.zeros_like(b)
+    cands = {"threads": (256, 1024), "lanes_per_row": (1, 4), "small_rows": (0, 1024)}
+    cfg = batched.autotune(solver, b, x, candidates=cands)
+    assert cfg["threads"] in (256, 1024) and cfg["lanes_per_row"] in (1, 4) and cfg["small_rows"] in (0, 1024)
+    assert batched._TUNED[solver.key] is cfg
+    solver.config, solver._autotune_pending = cfg, False
+    solver.solve(b, x)
+    _batched_residuals(Am, b, x, offs.cpu().numpy(), 1e-6, solver.iters.cpu().numpy())
+    # the CUDA-graph replay gives the same iterate as a direct launch
+    x2 = torch.zeros_like(b)
+    eager = batched.BatchedCG(Am, offs, M._inv_diag, 1e-6, 0.0, 2000, config=cfg, use_cuda_graph=False)
+    eager.solve(b, x2)
+    assert torch.equal(x, x2)

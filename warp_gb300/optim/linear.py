@@ -68,6 +68,7 @@ class LinearOperator:
         self._max_batch_length = max_batch_length
         self._bsr = None  # set for BSR operators (fused path)
         self._inv_diag = None  # set for Jacobi preconditioners (fused path)
+        self._source = None  # the dense matrix / diagonal of array operators (batched path)
 
     @property
     def shape(self):
@@ -128,7 +129,9 @@ def aslinearoperator(Am, batch_offsets=None, max_batch_length=None) -> LinearOpe
             N.check(N.lib().gb_dense_mv(A.gb_dtype(tc.dtype), m, n, A.ptr(tc), A.ptr(_flat(x)), A.ptr(_flat(y)),
                                         A.ptr(_flat(z)), float(alpha), float(beta), stream_of()), "dense_mv")
 
-        return LinearOperator(tuple(t.shape), t.dtype, t.device, dense_mv, batch_offsets, max_batch_length)
+        op = LinearOperator(tuple(t.shape), t.dtype, t.device, dense_mv, batch_offsets, max_batch_length)
+        op._source = tc
+        return op
     if t.dim() in (1, 2) or t.dim() >= 1:
         td = t.reshape(-1).contiguous()
 
@@ -138,6 +141,7 @@ def aslinearoperator(Am, batch_offsets=None, max_batch_length=None) -> LinearOpe
                     "diag_mv")
 
         op = LinearOperator((td.numel(), td.numel()), t.dtype, t.device, diag_mv, batch_offsets, max_batch_length)
+        op._source = td
         op._inv_diag = td
         return op
     raise ValueError(f"Unable to create LinearOperator from {Am}")
@@ -361,9 +365,16 @@ class LinearSolverState:
             raise ValueError(f"Incompatible b.shape: expected {tuple(self._b.shape)}, got {tuple(b_t.shape)}")
         if x_t.shape != self._x.shape:
             raise ValueError(f"Incompatible x.shape: expected {tuple(self._x.shape)}, got {tuple(x_t.shape)}")
+        if self._A.batch_offsets is not None:
+            if Aop is not self._A and Aop.batch_offsets is not self._A.batch_offsets:
+                raise ValueError("A.batch_offsets must be the same array as at construction")
+            return self._run_batched(Aop, b_t.reshape(-1), x_t.reshape(-1), Mop)
         if self._fused and self._fused_eligible(Aop, Mop, b_t, x_t):
             return self._run_fused(Aop, b_t, x_t, Mop)
         return self._run_generic(Aop, b_t.reshape(-1), x_t.reshape(-1), Mop)
+
+    def _run_batched(self, Aop, b, x, Mop):
+        raise NotImplementedError(f"{type(self).__name__}: batched operators (batch_offsets) are solved by cg only")
 
     # -- generic path (any LinearOperator) ------------------------------------------------
     def _dots(self, pairs):
@@ -399,6 +410,40 @@ class CG(LinearSolverState):
         super().__init__(A_, b, x, tol, atol, maxiter, M, callback, check_every, use_cuda_graph)
         if restart is not None:
             self._fused = False
+
+    def _run_batched(self, Aop, b, x, Mop):
+        """Batched operator: the whole batch is one persistent launch (``warp_gb300.batched``);
+        each subproblem converges to its own tolerance (reference: ``linear.py:893-1032``).  The
+        callback, if any, sees the final state."""
+        from .. import batched
+
+        if self._restart is not None:
+            raise NotImplementedError("batched CG with restart")
+        if b.dtype != torch.float32 or x.dtype != torch.float32:
+            raise NotImplementedError("batched CG: float32 systems")
+        inv = None
+        if Mop is not None:
+            inv = getattr(Mop, "_inv_diag", None)
+            if inv is None:
+                raise NotImplementedError("batched CG: Jacobi ('diag') or no preconditioner")
+        if getattr(self, "_batched", None) is None or self._batched_op is not Aop:
+            csr = batched.as_block_csr(Aop)
+            rtol, atol = _get_tolerances(torch.float32, self._tol, self._atol)
+            cfg = "auto" if Aop.batch_count >= 256 else None
+            self._batched = batched.BatchedCG(csr, Aop.batch_offsets, inv, rtol, atol, self._maxiter, config=cfg,
+                                              use_cuda_graph=self._use_cuda_graph)
+            self._batched_op = Aop
+        self._batched.inv_diag = inv
+        self._batched.solve(b, x)
+        it, rr, atol_sq = self._batched.results()
+        if self._check_every == 0:
+            return it, rr, atol_sq
+        it_h = int(it.item())
+        err = math.sqrt(float(rr.max())) if rr.numel() else 0.0
+        atol_v = math.sqrt(float(atol_sq.max())) if atol_sq.numel() else 0.0
+        if self._callback is not None:
+            self._callback(it_h, err, atol_v)
+        return it_h, err, atol_v
 
     def _run_generic(self, Aop, b, x, Mop):
         dt = b.dtype
@@ -613,7 +658,7 @@ class RefinedSolver:
 
     def __init__(self, Am: sparse.BsrMatrix, M: LinearOperator | None = None, method: str = "cg",
                  inner_tol: float = 1e-5, inner_maxiter: int = 0, inner_values: torch.Tensor | None = None,
-                 residual: str = "df32"):
+                 residual: str = "df32", use_cuda_graph: bool = True):
         self.A = Am
         self.M = M
         self.n = Am.nrow * Am.block_shape[0]
@@ -631,17 +676,21 @@ class RefinedSolver:
         self.method = method
         self.fallbacks = 0
         self._jacobi = None
+        # graph mode: each correction solve is one conditional-loop graph launch; otherwise eager
+        # launches with a host check after every iteration (for per-kernel profiling)
+        loop = dict(check_every=0, use_cuda_graph=True) if use_cuda_graph else dict(check_every=1,
+                                                                                   use_cuda_graph=False)
         if method == "fcg":
             self.inner = FCG(self._inner_A, self._r32, self._d, tol=self.inner_tol, atol=0.0,
-                             maxiter=self.inner_maxiter, M=M, check_every=0, use_cuda_graph=True)
+                             maxiter=self.inner_maxiter, M=M, **loop)
             # Jacobi-CG: the fallback when the flexible solve stagnates
             self._jacobi_M = preconditioner(self._inner_A, "diag")
             self._jacobi = CG(self._inner_A, self._r32, self._d, tol=self.inner_tol, atol=0.0,
-                              maxiter=self.inner_maxiter, M=self._jacobi_M, check_every=0, use_cuda_graph=True)
+                              maxiter=self.inner_maxiter, M=self._jacobi_M, **loop)
         else:
             cls = CG if method == "cg" else BiCGSTAB
             self.inner = cls(self._inner_A, self._r32, self._d, tol=self.inner_tol, atol=0.0,
-                             maxiter=self.inner_maxiter, M=M, check_every=0, use_cuda_graph=True)
+                             maxiter=self.inner_maxiter, M=M, **loop)
         if not self.inner._fused:
             raise ValueError("solve_refined needs a BSR operator with 1x1/3x3 float32 blocks and a Jacobi or no "
                              "preconditioner")
@@ -731,7 +780,8 @@ class RefinedSolver:
 
 def solve_refined(A_: sparse.BsrMatrix, b, x64=None, tol: float = 1e-8, M=None, method: str = "cg",
                   inner_tol: float = 1e-5, max_outer: int = 50, residual: str = "df32"):
-    """method: "cg" / "bicgstab" (M = Jacobi or None) or "fcg" (M = a preconditioner object)."""
-    """FP64-accurate solve of ``A x = b`` with an FP32 Krylov inner loop; returns ``(x64, info)``."""
+    """FP64-accurate solve of ``A x = b`` with an FP32 Krylov inner loop; returns ``(x64, info)``.
+
+    method: "cg" / "bicgstab" (M = Jacobi or None) or "fcg" (M = a preconditioner object)."""
     solver = RefinedSolver(A_, M=M, method=method, inner_tol=inner_tol, residual=residual)
     return solver.solve(b, x64=x64, tol=tol, max_outer=max_outer)

@@ -26,12 +26,12 @@ class System:
 
 
 def diffusion(res, sigma: float = 1.5, corr_length: float = 0.1, seed: int = 0, lognormal: bool = True,
-              constant: float | None = None, field_cell_size: float | None = None, coef=None) -> System:
+              constant: float | None = None, field_cell_size: float | None = None, coef=None, f=None) -> System:
     """-div(a grad u) = f, Q1 on a unit Grid2D/Grid3D, a = exp(g) with g a squared-exponential GRF
     (correlation ``corr_length``, std ``sigma``) per cell, f ~ U[-1, 1] per node, u = 0 on the whole
     boundary imposed by projection.  ``field_cell_size`` samples the field as if the cells had that
     size (a sub-block of a finer grid: same correlation length in cells); ``coef`` gives the per-cell
-    coefficient directly."""
+    coefficient directly and ``f`` the nodal source."""
     res = tuple(int(r) for r in res)
     geo = fem.Grid2D(res=res) if len(res) == 2 else fem.Grid3D(res=res)
     rng = np.random.default_rng(seed)
@@ -45,7 +45,7 @@ def diffusion(res, sigma: float = 1.5, corr_length: float = 0.1, seed: int = 0, 
         coef = np.exp(g).reshape(-1)
     else:
         coef = np.ones(geo.cell_count())
-    f = rng.uniform(-1.0, 1.0, geo.node_count()).astype(np.float32)
+    f = rng.uniform(-1.0, 1.0, geo.node_count()).astype(np.float32) if f is None else np.asarray(f, np.float32)
     space = fem.make_polynomial_space(geo, degree=1)
     Am = fem.integrate(fem.diffusion_form, fields={"u": fem.make_trial(space), "v": fem.make_test(space)},
                        values={"nu": coef.astype(np.float32)})
