@@ -153,6 +153,117 @@ def cpu_baseline_sample(system, gpu_iters: int, budget_s: float = 20.0):
                       f"threads (rel. residual {rel:.2e}); scaled to {full_iters} iterations"}
 
 
+def _event_ms(fn, reps: int, warmup: int = 1) -> float:
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def bench_batched(args, hbm_peak):
+    """4096 uneven 2-D Q1 diffusion systems (n ~ U{16..128} cells per side, GRF l=0.1, sigma=1), one
+    persistent batched Jacobi-CG launch (autotuned, CUDA graph) to 1e-6 relative residual each."""
+    import numpy as np
+    import torch
+
+    from warp_gb300 import batched
+    from warp_gb300.optim import linear
+
+    rng = np.random.default_rng(args.seed)
+    ncells = rng.integers(16, 129, size=args.batch_count)
+    t0 = time.perf_counter()
+    Am, b, offs = batched.q1_batch_2d(ncells, sigma=1.0, corr_length=0.1, seed=args.seed)
+    build_s = time.perf_counter() - t0
+    M = linear.preconditioner(Am, "diag")
+    solver = batched.BatchedCG(Am, offs, M._inv_diag, 1e-6, 0.0, 0, config="auto")
+    x = torch.zeros_like(b)
+    t0 = time.perf_counter()
+    solver.solve(b, x)  # autotunes on the first call
+    torch.cuda.synchronize()
+    tune_s = time.perf_counter() - t0
+
+    def step():
+        x.zero_()
+        solver.solve(b, x)
+
+    ms = _event_ms(step, args.steps, warmup=2)
+    it = solver.iters.cpu().numpy()
+    rows = np.diff(offs.cpu().numpy())
+    nnz_rows = (3 * ncells + 1) ** 2
+    # algorithmic bytes: per subproblem iteration the matrix (8 B / nonzero + 4 B / row offsets) and
+    # 48 B / row of vector traffic (Ap write; p, x, r, Ap, dinv read, x, r write; r, dinv, p read, p write)
+    algo = float((it * (nnz_rows * 8 + rows * 52)).sum())
+    gbs = algo / (ms * 1e-3) / 1e9
+    conv = float((solver.rr <= solver.atol_sq).float().mean())
+    return {"workload": f"{args.batch_count} Q1 2-D diffusion systems, n ~ U{{16..128}} cells/side, "
+                        f"{int(rows.sum())} rows, {int(nnz_rows.sum())} nnz, Jacobi-CG to 1e-6 each",
+            "ms": ms, "systems_per_s": args.batch_count / (ms * 1e-3), "launches_per_solve": 2,
+            "config": {k: v for k, v in solver.config.items() if k != "tuned_ms"},
+            "iterations": {"min": int(it.min()), "median": float(np.median(it)), "max": int(it.max())},
+            "converged_fraction": conv, "status": int(solver.status.item()),
+            "algorithmic_bytes": algo, "achieved_gbs": gbs, "frac_of_hbm": gbs / hbm_peak,
+            "build_s": build_s, "autotune_s": tune_s}
+
+
+def bench_assembly(args, system, hbm_peak):
+    """96^3 bilinear assembly through fem.integrate (Q1 triplets + bsr_set_from_triplets)."""
+    import numpy as np
+
+    from warp_gb300 import fem
+
+    geo = system.geo
+    space = fem.make_polynomial_space(geo, degree=1)
+    coef = np.asarray(system.coef, np.float32)
+    fields = {"u": fem.make_trial(space), "v": fem.make_test(space)}
+    ms = _event_ms(lambda: fem.integrate(fem.diffusion_form, fields=fields, values={"nu": coef}), 3)
+    A = system.A
+    T = geo.cell_count() * 64
+    nnz = A.nnz_sync()
+    algo = T * (8 + 4) + nnz * (4 + 4) + (A.nrow + 1) * 4
+    return {"ms": ms, "triplets": T, "nnz": nnz, "algorithmic_bytes": algo,
+            "achieved_gbs": algo / (ms * 1e-3) / 1e9, "frac_of_hbm": algo / (ms * 1e-3) / 1e9 / hbm_peak,
+            "note": "host-to-device copy of the coefficient field included"}
+
+
+def bench_elasticity(args, hbm_peak):
+    """64^3 Q1 vec3 elasticity (E lognormal sigma=1 i.i.d., nu=0.3, gravity, x=0 clamped): 3x3 bsr_mv
+    bandwidth and the refined Jacobi-CG solve to 1e-8."""
+    import torch
+
+    from warp_gb300 import problems, sparse
+    from warp_gb300.optim import linear
+
+    s = problems.elasticity((args.elasticity_res,) * 3, sigma=1.0, seed=args.seed)
+    A = s.A
+    nnz = A.nnz_sync()
+    n = A.nrow * 3
+    xv = torch.randn(n, device="cuda")
+    yv = torch.empty_like(xv)
+    mv_ms = _event_ms(lambda: sparse.bsr_mv(A, xv, yv), 20, warmup=3)
+    mv_bytes = nnz * (36 + 4) + (A.nrow + 1) * 4 + 2 * n * 4
+    solver = linear.RefinedSolver(A, M=linear.preconditioner(A, "diag"), inner_tol=args.inner_tol)
+    solver.solve(s.b, tol=1e-8)
+    infos = []
+
+    def step():
+        infos.append(solver.solve(s.b, tol=1e-8)[1])
+
+    ms = _event_ms(step, 2, warmup=0)
+    return {"workload": f"{args.elasticity_res}^3 Q1 vec3 elasticity, {A.nrow} block rows, {nnz} blocks",
+            "bsr_mv_us": mv_ms * 1e3, "bsr_mv_gbs": mv_bytes / (mv_ms * 1e-3) / 1e9,
+            "bsr_mv_frac_of_hbm": mv_bytes / (mv_ms * 1e-3) / 1e9 / hbm_peak,
+            "jacobi_cg_refined_ms": ms, "inner_iterations": infos[-1]["inner_iterations"],
+            "rel_residual": infos[-1]["rel_residual"]}
+
+
 def run_reference(args):
     ws, rank = _dist()
     if rank != 0:
@@ -252,6 +363,10 @@ def main():
     p.add_argument("--ref-iters", type=int, default=50)
     p.add_argument("--ref-full-iters", type=int, default=2000)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the batched, assembly and elasticity measurements")
+    p.add_argument("--batch-count", type=int, default=4096)
+    p.add_argument("--elasticity-res", type=int, default=64)
     p.add_argument("--weights", default=os.path.join(ROOT, "warp_gb300", "data", "smoother_q1_diffusion.npz"))
     p.add_argument("--profile", choices=["spmv", "cg", "jacobi_solve", "solve"], default=None,
                    help="run a fixed kernel sequence for an ncu capture and exit (prints no bench line): "
@@ -443,6 +558,12 @@ def main():
     # iteration its 4 kernels + the V-cycle's (learned smoother included)
     gpu_launches = int(llaunch)
 
+    extras = {}
+    if not args.no_extras:
+        extras["assembly_96cube"] = bench_assembly(args, system, hbm_peak)
+        extras["batched_uneven"] = bench_batched(args, hbm_peak)
+        extras["elasticity"] = bench_elasticity(args, hbm_peak)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline_sample(system, int(statistics.median([i["inner_iterations"] for i in jinfos])))
@@ -486,6 +607,7 @@ def main():
         "conv_net": {"smoother_us": smoother_us, "launches": sm.kernels_per_apply, "useful_tflops": net_tflops,
                      "backend": "tcgen05 kind::f16 bf16 x bf16 -> fp32"},
         "bsr_mv_gbs": mv_gbs,
+        **extras,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
