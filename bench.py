@@ -313,12 +313,45 @@ def run_reference(args):
 
 def run_profile(args):
     """Kernel sequences for ncu (launch lists and single-kernel captures) on the bench workload."""
+    import numpy as np
     import torch
 
     from warp_gb300 import problems, sparse
     from warp_gb300.optim import linear
 
     torch.cuda.set_device(0)
+    if args.profile == "conv":  # 3 launches of one hidden tcgen05 layer on the 97^3 node grid
+        import warp_gb300._native as N
+        from warp_gb300 import learned
+
+        dims = tuple(r + 1 for r in args.res)
+        src = learned.to_planar(torch.randn(int(np.prod(dims)), 16, device="cuda"), dims)
+        dst = torch.zeros_like(src)
+        Wt = (torch.randn(27, 16, 16, device="cuda") * 0.1).to(torch.bfloat16).contiguous()
+        st = torch.zeros(1, dtype=torch.int32, device="cuda")
+        for _ in range(3):
+            N.check(N.lib().gb_conv3_fwd_tc(*dims, 0, src.data_ptr(), Wt.data_ptr(), dst.data_ptr(), None, None, None,
+                                            None, 0.0, st.data_ptr(), torch.cuda.current_stream().cuda_stream))
+        torch.cuda.synchronize()
+        assert int(st.item()) == 0
+        print("profile run done", flush=True)
+        return 0
+    if args.profile == "batched":  # 512 uneven systems, two eager batched launches (fixed shape)
+        from warp_gb300 import batched
+
+        rng = np.random.default_rng(args.seed)
+        Am, b, offs = batched.q1_batch_2d(rng.integers(16, 129, size=512), seed=args.seed)
+        Mb = linear.preconditioner(Am, "diag")
+        bs = batched.BatchedCG(Am, offs, Mb._inv_diag, 1e-6, 0.0, 0, use_cuda_graph=False,
+                               config={"threads": 256, "lanes_per_row": 2, "small_rows": 0})
+        x = torch.zeros_like(b)
+        for _ in range(2):
+            x.zero_()
+            bs.solve(b, x)
+        torch.cuda.synchronize()
+        assert int(bs.status.item()) == 0
+        print("profile run done", flush=True)
+        return 0
     system = problems.diffusion(args.res, sigma=1.5, corr_length=0.1, seed=args.seed)
     A = system.A
     torch.cuda.synchronize()
@@ -368,10 +401,12 @@ def main():
     p.add_argument("--batch-count", type=int, default=4096)
     p.add_argument("--elasticity-res", type=int, default=64)
     p.add_argument("--weights", default=os.path.join(ROOT, "warp_gb300", "data", "smoother_q1_diffusion.npz"))
-    p.add_argument("--profile", choices=["spmv", "cg", "jacobi_solve", "solve"], default=None,
+    p.add_argument("--profile", choices=["spmv", "cg", "jacobi_solve", "solve", "conv", "batched"], default=None,
                    help="run a fixed kernel sequence for an ncu capture and exit (prints no bench line): "
                         "spmv = 8 bsr_mv launches, cg = 30 eager (non-graph) Jacobi-CG iterations, "
-                        "jacobi_solve = one refined Jacobi-CG solve, solve = two learned-FCG solves (eager launches)")
+                        "jacobi_solve = one refined Jacobi-CG solve, solve = two learned-FCG solves (eager launches), "
+                        "conv = 3 launches of one tcgen05 conv layer on the node grid, batched = two launches of "
+                        "the batched CG on 512 uneven systems")
     args = p.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 

@@ -65,7 +65,7 @@ def _batched_residuals(Am, b, x, offs, tol, iters, scale=32.0):
 
 
 @pytest.mark.parametrize("config", [None, {"threads": 256, "lanes_per_row": 1, "small_rows": 0},
-                                    {"threads": 1024, "lanes_per_row": 4, "small_rows": 4096}])
+                                    {"threads": 512, "lanes_per_row": 4, "small_rows": 4096}])
 def test_batched_cg_each_subproblem_converges(cuda, config):
     """Uneven Q1 subproblems in one launch: every subproblem meets its own tolerance (the reference's
     per-batch check, scale 32 for fp32) and takes the iterations of the same Jacobi-CG run alone
@@ -192,9 +192,9 @@ def test_autotuner_picks_a_candidate_and_caches_it(cuda):
     M = linear.preconditioner(Am, "diag")
     solver = batched.BatchedCG(Am, offs, M._inv_diag, 1e-6, 0.0, 2000, config="auto")
     x = torch.zeros_like(b)
-    cands = {"threads": (256, 1024), "lanes_per_row": (1, 4), "small_rows": (0, 1024)}
+    cands = {"threads": (128, 512), "lanes_per_row": (1, 4), "small_rows": (0, 1024)}
     cfg = batched.autotune(solver, b, x, candidates=cands)
-    assert cfg["threads"] in (256, 1024) and cfg["lanes_per_row"] in (1, 4) and cfg["small_rows"] in (0, 1024)
+    assert cfg["threads"] in (128, 512) and cfg["lanes_per_row"] in (1, 4) and cfg["small_rows"] in (0, 1024)
     assert batched._TUNED[solver.key] is cfg
     solver.config, solver._autotune_pending = cfg, False
     solver.solve(b, x)

@@ -26,7 +26,7 @@ from . import _native as N
 from . import sparse
 
 DEFAULT_CONFIG = {"threads": 512, "lanes_per_row": 2, "small_rows": 2048}
-CANDIDATES = {"threads": (256, 512, 1024), "lanes_per_row": (1, 2, 4), "small_rows": (0, 1024, 4096)}
+CANDIDATES = {"threads": (128, 256, 512), "lanes_per_row": (1, 2, 4), "small_rows": (0, 1024, 4096)}
 _TUNED: dict = {}
 
 

@@ -88,21 +88,54 @@ __device__ void solve_one(const BatchArgs& a, int pid, int tid, int nthr, double
             __syncthreads();
     };
     // A v on this group's rows; returns (per thread) the partial sum of w[row] * (A v)[row] and
-    // stores (A v) into out (sub-lane 0 only).  beta != 0: out = b - A v (initial residual).
+    // stores (A v) into out (sub-lane 0 only); residual: out = b - A v.  Two rows per group per
+    // pass, and each row's nonzeros of this lane are loaded as one predicated batch of U, so a lane
+    // keeps 2 U column / value loads and then 2 U gathers in flight instead of walking a chain.
+    constexpr int U = LPR == 1 ? 9 : (LPR == 2 ? 5 : (LPR == 4 ? 3 : 2));
     auto matvec = [&](const float* v, float* out, const float* w, bool residual) -> float {
         float part = 0.f;
-        for (int base = r0; base < r1; base += rows_per_pass) {
-            const int row = base + gid;
-            float s = 0.f;
-            if (row < r1) {
-                const int k0 = a.offsets[row], k1 = a.offsets[row + 1];
-                for (int k = k0 + sub; k < k1; k += LPR) s += a.values[k] * v[a.columns[k]];
+        for (int base = r0; base < r1; base += 2 * rows_per_pass) {
+            int row[2], k1[2], kb[2];
+            float s[2] = {0.f, 0.f};
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                row[h] = base + gid + h * rows_per_pass;
+                const bool valid = row[h] < r1;
+                kb[h] = valid ? a.offsets[row[h]] + sub : 0;
+                k1[h] = valid ? a.offsets[row[h] + 1] : 0;
             }
-            s = group_sum<LPR>(s);
-            if (row < r1 && sub == 0) {
-                const float o = residual ? a.b[row] - s : s;
-                out[row] = o;
-                if (w) part += w[row] * o;
+            while (kb[0] < k1[0] || kb[1] < k1[1]) {
+                int cc[2][U];
+                float vv[2][U];
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+#pragma unroll
+                    for (int u = 0; u < U; ++u) {
+                        const int k = kb[h] + u * LPR;
+                        const bool in = k < k1[h];
+                        cc[h][u] = in ? a.columns[k] : -1;
+                        vv[h][u] = in ? a.values[k] : 0.f;
+                    }
+                float xv[2][U];
+#pragma unroll
+                for (int h = 0; h < 2; ++h)
+#pragma unroll
+                    for (int u = 0; u < U; ++u) xv[h][u] = cc[h][u] >= 0 ? v[cc[h][u]] : 0.f;
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+#pragma unroll
+                    for (int u = 0; u < U; ++u) s[h] += vv[h][u] * xv[h][u];
+                    kb[h] += U * LPR;
+                }
+            }
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const float sh = group_sum<LPR>(s[h]);
+                if (row[h] < r1 && sub == 0) {
+                    const float o = residual ? a.b[row[h]] - sh : sh;
+                    out[row[h]] = o;
+                    if (w) part += w[row[h]] * o;
+                }
             }
         }
         return part;
@@ -154,6 +187,7 @@ __device__ void solve_one(const BatchArgs& a, int pid, int tid, int nthr, double
         if (WARP) __syncwarp();
         // ---- x += alpha p, r -= alpha Ap, z = D^-1 r, r.r, r.z --------------------------------
         float part2[2] = {0.f, 0.f};
+#pragma unroll 4
         for (int i = r0 + tid; i < r1; i += nthr) {
             const float pi = a.p[i];
             a.x[i] += alpha * pi;
@@ -174,6 +208,7 @@ __device__ void solve_one(const BatchArgs& a, int pid, int tid, int nthr, double
             break;
         }
         // ---- p = z + beta p --------------------------------------------------------------------
+#pragma unroll 4
         for (int i = r0 + tid; i < r1; i += nthr) {
             const float ri = a.r[i];
             const float zi = a.dinv ? a.dinv[i] * ri : ri;
@@ -194,7 +229,7 @@ __device__ void solve_one(const BatchArgs& a, int pid, int tid, int nthr, double
 }
 
 template <int LPR>
-__global__ void __launch_bounds__(1024, 1) k_batched_pcg(const BatchArgs a)
+__global__ void __launch_bounds__(512) k_batched_pcg(const BatchArgs a)
 {
     __shared__ double red[32 * 3];
     __shared__ int s_item;
@@ -299,8 +334,9 @@ GB_API size_t gb_batched_pcg_workspace_bytes(int64_t n) { return 3 * sizeof(floa
 
 // Persistent batched Jacobi-CG (see the file comment).  n: total rows (inactive tail included);
 // dinv may be null (no preconditioner); x is read as the initial guess unless x_is_zero;
-// threads in {128, 256, 512, 1024}; lanes_per_row in {1, 2, 4, 8}; small_rows: subproblems of at most
+// threads in {128, 256, 512}; lanes_per_row in {1, 2, 4, 8}; small_rows: subproblems of at most
 // this many rows are solved by one warp.  iters / rr / atol_sq: per-subproblem results (device).
+
 GB_API int gb_batched_pcg(int nbatch, const int* batch_offsets, const int* order, int64_t n, const int* offsets,
                           const int* columns, const float* values, const float* dinv, const float* b, float* x,
                           double rtol, double atol, int maxiter, int x_is_zero, int threads, int lanes_per_row,
@@ -308,8 +344,7 @@ GB_API int gb_batched_pcg(int nbatch, const int* batch_offsets, const int* order
                           size_t workspace_bytes, int* status, cudaStream_t stream)
 {
     GB_REQUIRE(nbatch >= 0 && n >= 0, "batched_pcg: negative sizes");
-    GB_REQUIRE(threads == 128 || threads == 256 || threads == 512 || threads == 1024,
-               "batched_pcg: threads must be 128, 256, 512 or 1024");
+    GB_REQUIRE(threads == 128 || threads == 256 || threads == 512, "batched_pcg: threads must be 128, 256 or 512");
     GB_REQUIRE(workspace_bytes >= gb_batched_pcg_workspace_bytes(n), "batched_pcg: workspace too small");
     GB_REQUIRE(status != nullptr && iters != nullptr && rr != nullptr && atol_sq != nullptr,
                "batched_pcg: status and per-subproblem result arrays are required");

@@ -171,11 +171,11 @@ class BsrMatrix:
         vals = A.to_numpy(self.values[:nnz].float() if self.values.dtype == torch.bfloat16 else self.values[:nnz])
         br, bc = self._block_shape
         D = np.zeros((self.nrow * br, self.ncol * bc), np.float64)
-        vals = vals.reshape(-1, br, bc)
-        for r in range(self.nrow):
-            for k in range(off[r], off[r + 1]):
-                c = cols[k]
-                D[r * br:(r + 1) * br, c * bc:(c + 1) * bc] += vals[k]
+        vals = vals.reshape(-1, br, bc).astype(np.float64)
+        rows = np.repeat(np.arange(self.nrow), np.diff(off[: self.nrow + 1]))
+        for i in range(br):
+            for j in range(bc):
+                np.add.at(D, (rows * br + i, cols.astype(np.int64) * bc + j), vals[:, i, j])
         return D
 
 
