@@ -224,13 +224,18 @@ def bench_assembly(args, system, hbm_peak):
     coef = np.asarray(system.coef, np.float32)
     fields = {"u": fem.make_trial(space), "v": fem.make_test(space)}
     ms = _event_ms(lambda: fem.integrate(fem.diffusion_form, fields=fields, values={"nu": coef}), 3)
+    rc_ms = _event_ms(lambda: fem.integrate(fem.diffusion_form, fields=fields, values={"nu": coef},
+                                            bsr_options={"construction": "row_compress"}), 3)
     A = system.A
     T = geo.cell_count() * 64
     nnz = A.nnz_sync()
     algo = T * (8 + 4) + nnz * (4 + 4) + (A.nrow + 1) * 4
     return {"ms": ms, "triplets": T, "nnz": nnz, "algorithmic_bytes": algo,
             "achieved_gbs": algo / (ms * 1e-3) / 1e9, "frac_of_hbm": algo / (ms * 1e-3) / 1e9 / hbm_peak,
-            "note": "host-to-device copy of the coefficient field included"}
+            "row_compress_ms": rc_ms, "row_compress_gbs": algo / (rc_ms * 1e-3) / 1e9,
+            "row_compress_frac_of_hbm": algo / (rc_ms * 1e-3) / 1e9 / hbm_peak,
+            "note": "fem.integrate with the triplet construction (LSD radix sort) and with the row_compress "
+                    "construction (no global sort); host-to-device copy of the coefficient field included"}
 
 
 def bench_elasticity(args, hbm_peak):

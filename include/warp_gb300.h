@@ -224,6 +224,21 @@ int gb_net_features_planar(int nx, int ny, int nz, const float* r, const float* 
 int gb_conv3_fwd_tc(int nx, int ny, int nz, int last, const void* in, const void* Wt, void* out, float* w,
                     const float* r, const float* dinv, const float* mask, float omega, int* status, gb_stream_t stream);
 
+/* ---- Row-local compression (the "row_compress" construction) ------------------------------------
+ * gb_bsr_compress_rows replaces bsr_compress(inplace=True) (warp/_src/sparse.py:1571-1640 ->
+ * warp/native/sparse.cu:1494-1656, per-row routine warp/native/sparse_util.h:82-139): prune zero
+ * blocks, stable sort by column and coalesce each active row in place, out_counts[r] = blocks kept.
+ * gb_bsr_compact: compact CSR (exclusive scan of counts[nrow + 1], counts[nrow] = 0, then a gather).
+ * gb_bsr_rows_to_offsets: padded row starts of candidates grouped by row (fem.integrate assembles
+ * them that way, warp/_src/fem/integrate.py:1664-1712); unsorted or out-of-range rows set status. */
+int gb_bsr_rows_to_offsets(int64_t T, const int* rows, int nrow, int* offsets, int* status, gb_stream_t stream);
+int gb_bsr_compress_rows(int block_size, int dtype, int nrow, const int* offsets, const int* row_counts, int* columns,
+                         void* values, int prune, uint64_t zero_mask, int* out_counts, gb_stream_t stream);
+size_t gb_bsr_compact_workspace_bytes(int nrow);
+int gb_bsr_compact(int block_size, int dtype, int nrow, const int* old_offsets, int* counts, const int* columns_in,
+                   const void* values_in, int* offsets_out, int* columns_out, void* values_out, void* workspace,
+                   size_t workspace_bytes, gb_stream_t stream);
+
 /* ---- Batched solves --------------------------------------------------------------------------
  * gb_batched_pcg replaces the batched CG of warp/_src/optim/linear.py:893-1032 (LinearOperator with
  * batch_offsets, :33-133; per-subproblem tolerances :2063-2083; frozen converged subproblems

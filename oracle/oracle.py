@@ -155,6 +155,62 @@ def ref_bsr_from_triplets(nrow, ncol, rows, cols, values=None, block_size=1, pru
                 tpl_block_indices=tbi[:n].copy(), nnz=nb)
 
 
+def ref_bsr_compress(offsets, row_counts, columns, values, block_size=1, prune_numerical_zeros=True,
+                     make_compact=True):
+    """Run the reference's own compiled in-place compression (sparse.cpp:521-610,
+    wp_bsr_compress_inplace_host, float32 values).  Returns dict(offsets, row_counts, columns, values,
+    nnz) or None when the reference library was not built here."""
+    R = ref_lib()
+    if R is None:
+        return None
+    nrow = len(offsets) - 1
+    off = np.array(offsets, np.int32)
+    rc = None if row_counts is None else np.array(row_counts, np.int32)
+    cols = np.array(columns, np.int32)
+    vals = np.array(values, np.float32).reshape(len(cols), block_size)
+    nnz = np.zeros(1, np.int32)
+    R.wp_bsr_compress_inplace_host.restype = None
+    R.wp_bsr_compress_inplace_host.argtypes = [
+        ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_bool, ctypes.c_uint64,
+        ctypes.c_bool, _i32p, _i32p, _i32p, ctypes.c_void_p, ctypes.c_bool, _i32p, ctypes.c_void_p]
+    R.wp_bsr_compress_inplace_host(nrow, block_size, 4, 0, len(cols), bool(prune_numerical_zeros), 0,
+                                   bool(make_compact), _ptr(off, _i32p), None if rc is None else _ptr(rc, _i32p),
+                                   _ptr(cols, _i32p), vals.ctypes.data, True, _ptr(nnz, _i32p), None)
+    n = int(nnz[0]) if make_compact else len(cols)
+    return dict(offsets=off, row_counts=rc, columns=cols[:n].copy(), values=vals[:n].copy(), nnz=n)
+
+
+def bsr_compress_rows(offsets, row_counts, columns, values, block_size=1, prune_numerical_zeros=True):
+    """Restatement (pure Python, small inputs) of the reference's per-row in-place compression
+    (warp/native/sparse_util.h:82-139) followed by compaction: per active row, zero blocks dropped
+    when pruning (all scalars == 0), stable insertion sort by column, runs of equal columns summed
+    in order (float32 arithmetic).  Returns compact (offsets, columns, values)."""
+    nrow = len(offsets) - 1
+    cols = [int(c) for c in columns]
+    vals = np.array(values, np.float32).reshape(len(cols), block_size).copy()
+    out_off, out_cols, out_vals = [0], [], []
+    for r in range(nrow):
+        beg = int(offsets[r])
+        end = beg + int(row_counts[r]) if row_counts is not None else int(offsets[r + 1])
+        blk = [(cols[b], vals[b].copy()) for b in range(beg, end)]
+        if prune_numerical_zeros:
+            blk = [(c if (c < 0 or np.any(v != 0)) else -1, v) for c, v in blk]
+        order = sorted(range(len(blk)), key=lambda i: blk[i][0])  # stable
+        blk = [blk[i] for i in order if blk[i][0] >= 0]
+        i = 0
+        while i < len(blk):
+            c, acc = blk[i][0], blk[i][1].copy()
+            i += 1
+            while i < len(blk) and blk[i][0] == c:
+                acc = (acc + blk[i][1]).astype(np.float32)
+                i += 1
+            out_cols.append(c)
+            out_vals.append(acc)
+        out_off.append(len(out_cols))
+    return (np.array(out_off, np.int32), np.array(out_cols, np.int32),
+            np.array(out_vals, np.float32).reshape(-1, block_size))
+
+
 def bsr_mv_f32(offsets, columns, values, x, y=None, alpha=1.0, beta=0.0, block_shape=(1, 1)):
     br, bc = block_shape
     nrow = len(offsets) - 1

@@ -161,3 +161,38 @@ def test_fem_oracle_triplet_order():
     # node 4 (centre of a 2x2 grid) touches all four cells: its first trial block is cell 0
     first = np.where(r == 4)[0][0]
     np.testing.assert_array_equal(c[first:first + 4], [0, 1, 3, 4])
+
+
+COMPRESS_GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "compress_ref.npz")
+
+
+@pytest.mark.parametrize("prune", [0, 1])
+def test_compress_restatement_matches_reference_golden(prune):
+    """The row-compress restatement equals the reference's compiled in-place compression bit for bit
+    (frozen by tests/golden/make_golden_compress.py)."""
+    g = np.load(COMPRESS_GOLDEN)
+    names = sorted({k.split("_")[0] for k in g.files})
+    for n in names:
+        bs = int(g[n + "_bs"][0])
+        off, col, val = oracle.bsr_compress_rows(g[n + "_offsets"], g[n + "_counts"], g[n + "_cols"], g[n + "_vals"],
+                                                 bs, bool(prune))
+        np.testing.assert_array_equal(off, g[f"{n}_p{prune}_offsets"])
+        np.testing.assert_array_equal(col, g[f"{n}_p{prune}_columns"])
+        np.testing.assert_array_equal(val.reshape(-1).view(np.uint32),
+                                      g[f"{n}_p{prune}_values"].reshape(-1).view(np.uint32))
+
+
+def test_compress_restatement_matches_live_reference():
+    if oracle.ref_lib() is None:
+        pytest.skip("reference library not built here")
+    rng = np.random.default_rng(5)
+    counts = rng.integers(0, 40, 25).astype(np.int32)
+    offsets = np.concatenate([[0], np.cumsum(counts + 1)]).astype(np.int32)
+    cols = rng.integers(-1, 15, int(offsets[-1])).astype(np.int32)
+    vals = rng.standard_normal(int(offsets[-1])).astype(np.float32)
+    vals[rng.random(vals.size) < 0.2] = 0.0
+    r = oracle.ref_bsr_compress(offsets, counts, cols, vals)
+    off, col, val = oracle.bsr_compress_rows(offsets, counts, cols, vals)
+    np.testing.assert_array_equal(off, r["offsets"])
+    np.testing.assert_array_equal(col, r["columns"])
+    np.testing.assert_array_equal(val.reshape(-1), r["values"].reshape(-1))

@@ -273,7 +273,24 @@ def integrate(integrand: Integrand, domain=None, quadrature=None, fields=None, v
     nnode = geo.node_count()
     block_type = torch.float32 if ncomp == 1 else ((3, 3), torch.float32)
     mat = output if (output is not None and not add) else sparse.bsr_zeros(nnode, nnode, block_type)
-    sparse.bsr_set_from_triplets(mat, rows, cols, vals)
+    opts = dict(bsr_options or {})
+    construction = opts.pop("construction", "triplets")
+    if construction not in ("triplets", "row_compress", "auto"):
+        raise ValueError(f"Unsupported BSR construction policy: {construction}")
+    prune = bool(opts.pop("prune_numerical_zeros", True))
+    if construction in ("row_compress", "auto"):
+        # the candidates come out row by row (test node, ascending element, trial node): they already
+        # are the padded row layout of integrate.py:1664-1712, so only a row-local compression remains
+        status = A.zeros(1, torch.int32)
+        offsets = A.empty(nnode + 1, torch.int32)
+        N.check(L.gb_bsr_rows_to_offsets(T, A.ptr(rows), nnode, A.ptr(offsets), A.ptr(status), stream), "row offsets")
+        mat.offsets, mat.columns, mat.values, mat.row_counts = offsets, cols, vals, None
+        mat.nnz, mat._nnz_event, mat._nnz_exact = T, None, True
+        sparse.bsr_compress(mat, prune_numerical_zeros=prune)
+        if int(status.item()) != 0:
+            raise RuntimeError("fem.integrate(row_compress): candidate rows are not grouped by test node")
+    else:
+        sparse.bsr_set_from_triplets(mat, rows, cols, vals, prune_numerical_zeros=prune)
     mat._keep_assembly = (K0, K1, c0, c1)
     if add and output is not None:
         raise NotImplementedError("add=True is not supported")

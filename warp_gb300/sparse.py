@@ -29,6 +29,7 @@ __all__ = [
     "bsr_get_diag",
     "bsr_copy",
     "bsr_scale",
+    "bsr_compress",
 ]
 
 # Zero masks for numerical-zero pruning, by scalar type (reference: sparse.py:991-1007).
@@ -300,6 +301,60 @@ def bsr_set_from_triplets(
             "bsr_accumulate_triplet_values")
     # keep temporaries alive until the stream has consumed them
     dest._last_temporaries = (ws, tbo, tbi, rows, columns, values)
+
+
+def bsr_compress(src: BsrMatrix, prune_numerical_zeros: bool = True, inplace: bool = False,
+                 topology: str | None = None) -> BsrMatrix:
+    """Sort and coalesce the active blocks of every row (reference: ``sparse.py:1571-1640``).
+
+    Active blocks are ``[offsets[r], offsets[r] + row_counts[r])`` (or ``offsets[r + 1]`` when
+    ``row_counts`` is None); negative columns are inactive.  Zero blocks are dropped before
+    coalescing when ``prune_numerical_zeros``; runs of equal columns are summed in their original
+    order (the order the triplet path accumulates in).  ``topology="compact"`` (default) packs the
+    rows into a compact CSR (new arrays; ``row_counts`` becomes None); ``"padded"`` keeps the row
+    capacity and sets ``row_counts``.  Both ``inplace`` values run the same native in-place row pass.
+    """
+    if not isinstance(src, BsrMatrix):
+        raise ValueError("bsr_compress() requires a BsrMatrix")
+    if topology is None:
+        topology = "compact"
+    elif topology not in ("compact", "padded"):
+        raise ValueError(f"Unsupported topology policy: {topology}")
+    if src.nrow == 0:
+        return src
+    dt = A.gb_dtype(src.scalar_type)
+    if dt not in (N.GB_F32, N.GB_F64):
+        raise NotImplementedError("bsr_compress: float32 or float64 values")
+    L = N.lib()
+    stream = A.stream()
+    counts = A.zeros(src.nrow + 1, torch.int32)
+    mask = _ZERO_MASK[src.scalar_type] if prune_numerical_zeros else 0
+    N.check(L.gb_bsr_compress_rows(src.block_size, dt, src.nrow, A.ptr(src.offsets), A.ptr(src.row_counts),
+                                   A.ptr(src.columns), A.ptr(src.values), int(prune_numerical_zeros), mask,
+                                   A.ptr(counts), stream), "bsr_compress_rows")
+    if topology == "padded":
+        src.row_counts = counts[: src.nrow]
+        src._topology_version += 1
+        return src
+    cap = src.capacity
+    new_off = A.empty(src.nrow + 1, torch.int32)
+    new_cols = A.empty(cap, torch.int32)
+    new_vals = A.empty(src._values_shape(cap), src.scalar_type)
+    ws = A.workspace(L.gb_bsr_compact_workspace_bytes(src.nrow))
+    N.check(L.gb_bsr_compact(src.block_size, dt, src.nrow, A.ptr(src.offsets), A.ptr(counts), A.ptr(src.columns),
+                             A.ptr(src.values), A.ptr(new_off), A.ptr(new_cols), A.ptr(new_vals), A.ptr(ws),
+                             ws.numel(), stream), "bsr_compact")
+    src._last_temporaries = (src.offsets, src.columns, src.values, counts, ws)
+    src.offsets, src.columns, src.values, src.row_counts = new_off, new_cols, new_vals, None
+    src._nnz_host = torch.zeros(1, dtype=torch.int32, pin_memory=True)
+    src._nnz_host.copy_(new_off[src.nrow:], non_blocking=True)
+    event = torch.cuda.Event()
+    event.record()
+    src._nnz_event = event
+    src._nnz_exact = False
+    src.nnz = cap
+    src._topology_version += 1
+    return src
 
 
 def _set_from_triplets_masked(dest, rows, columns, values, count, prune_numerical_zeros):
