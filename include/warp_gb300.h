@@ -224,6 +224,15 @@ int gb_net_features_planar(int nx, int ny, int nz, const float* r, const float* 
 int gb_conv3_fwd_tc(int nx, int ny, int nz, int last, const void* in, const void* Wt, void* out, float* w,
                     const float* r, const float* dinv, const float* mask, float omega, int* status, gb_stream_t stream);
 
+/* Multi-column dot / axpy for GMRES's Gram-Schmidt steps (warp/_src/optim/linear.py:1653-1916 computes
+ * them with TiledDot over the basis and _gmres_arnoldi_axpy_kernel): out[c] = V[c] . w (rows of V ldv
+ * apart, fp64 accumulation, deterministic); w = beta w + alpha sum_c coef[c] V[c] (coef: device doubles). */
+size_t gb_multi_dot_workspace_bytes(int ncols);
+int gb_multi_dot(int dtype, int64_t n, int ncols, const void* V, int64_t ldv, const void* w, double* out,
+                 void* workspace, size_t workspace_bytes, gb_stream_t stream);
+int gb_multi_axpy(int dtype, int64_t n, int ncols, const void* V, int64_t ldv, const double* coef, double alpha,
+                  double beta, void* w, gb_stream_t stream);
+
 /* ---- Row-local compression (the "row_compress" construction) ------------------------------------
  * gb_bsr_compress_rows replaces bsr_compress(inplace=True) (warp/_src/sparse.py:1571-1640 ->
  * warp/native/sparse.cu:1494-1656, per-row routine warp/native/sparse_util.h:82-139): prune zero

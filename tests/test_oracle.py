@@ -196,3 +196,24 @@ def test_compress_restatement_matches_live_reference():
     np.testing.assert_array_equal(off, r["offsets"])
     np.testing.assert_array_equal(col, r["columns"])
     np.testing.assert_array_equal(val.reshape(-1), r["values"].reshape(-1))
+
+
+def test_krylov_restatements_converge_to_direct_solutions():
+    """The CR / GMRES restatements (oracle.krylov) reach their tolerance and the direct solution."""
+    from oracle import krylov
+
+    rng = np.random.default_rng(4)
+    Q = rng.standard_normal((40, 40))
+    S = Q @ Q.T + 40 * np.eye(40)
+    b = rng.standard_normal(40)
+    xs = np.linalg.solve(S, b)
+    for dinv in (None, 1.0 / np.diag(S)):
+        x, it, res = krylov.cr(S, b, dinv=dinv, tol=1e-10, atol=0.0)
+        assert res <= 1e-10 * np.linalg.norm(b) and np.allclose(x, xs, rtol=1e-7, atol=1e-9) and 0 < it < 40
+    N_ = 4 * np.eye(50) + 0.3 * rng.standard_normal((50, 50))
+    b = rng.standard_normal(50)
+    xs = np.linalg.solve(N_, b)
+    for dinv, left in ((None, False), (1.0 / np.diag(N_), False), (1.0 / np.diag(N_), True)):
+        x, it, res = krylov.gmres(N_, b, dinv=dinv, tol=1e-10, atol=0.0, restart=8, left=left)
+        assert np.linalg.norm(N_ @ x - b) <= 1e-10 * np.linalg.norm(b) and it % 8 == 0
+        assert np.allclose(x, xs, rtol=1e-7, atol=1e-9)

@@ -257,3 +257,88 @@ GB_API int gb_axpby(int dtype, int64_t n, double alpha, const void* x, double be
     GB_CHECK_CUDA(cudaGetLastError());
     return GB_OK;
 }
+
+// ---- multi-column dot / axpy (Gram-Schmidt steps of GMRES) -------------------------------------
+namespace gb {
+constexpr int MD_PARTS = 152;
+
+template <typename T>
+__global__ void k_multi_dot_part(int64_t n, const T* __restrict__ V, int64_t ldv, const T* __restrict__ w,
+                                 double* __restrict__ partials)
+{
+    __shared__ double scratch[32];
+    const int c = blockIdx.y;
+    const T* v = V + (int64_t)c * ldv;
+    const int64_t chunk = (n + gridDim.x - 1) / gridDim.x;
+    const int64_t i0 = (int64_t)blockIdx.x * chunk, i1 = min(n, i0 + chunk);
+    double s = 0.0;
+    for (int64_t i = i0 + threadIdx.x; i < i1; i += blockDim.x) s += (double)v[i] * (double)w[i];
+    double in[1] = {s}, out[1];
+    block_sum<1, double>(in, scratch, out);
+    if (threadIdx.x == 0) partials[(int64_t)c * gridDim.x + blockIdx.x] = out[0];
+}
+
+__global__ void k_multi_dot_finish(int parts, const double* __restrict__ partials, double* __restrict__ out)
+{
+    const int c = blockIdx.x;
+    double s = 0.0;
+    for (int p = threadIdx.x; p < parts; p += 32) s += partials[(int64_t)c * parts + p];
+    s = warp_sum(s);
+    if (threadIdx.x == 0) out[c] = s;
+}
+
+// w = beta * w + alpha * sum_c coef[c] * V[c]
+template <typename T>
+__global__ void k_multi_axpy(int64_t n, int ncols, const T* __restrict__ V, int64_t ldv, const double* __restrict__ coef,
+                             double alpha, double beta, T* __restrict__ w)
+{
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int c = 0; c < ncols; ++c) s += coef[c] * (double)V[(int64_t)c * ldv + i];
+        w[i] = (T)(beta * (double)w[i] + alpha * s);
+    }
+}
+}  // namespace gb
+
+GB_API size_t gb_multi_dot_workspace_bytes(int ncols) { return sizeof(double) * (size_t)std::max(ncols, 1) * gb::MD_PARTS; }
+
+// out[c] = V[c] . w for c < ncols (rows of V are ldv apart), fp64 accumulation, deterministic.
+GB_API int gb_multi_dot(int dtype, int64_t n, int ncols, const void* V, int64_t ldv, const void* w, double* out,
+                        void* workspace, size_t workspace_bytes, cudaStream_t stream)
+{
+    GB_REQUIRE(ncols >= 1 && ncols <= 65535 && n >= 0, "multi_dot: bad sizes");
+    GB_REQUIRE(workspace_bytes >= gb_multi_dot_workspace_bytes(ncols), "multi_dot: workspace too small");
+    double* partials = static_cast<double*>(workspace);
+    dim3 grid(gb::MD_PARTS, ncols);
+    if (dtype == GB_F32)
+        gb::k_multi_dot_part<float><<<grid, 256, 0, stream>>>(n, (const float*)V, ldv, (const float*)w, partials);
+    else if (dtype == GB_F64)
+        gb::k_multi_dot_part<double><<<grid, 256, 0, stream>>>(n, (const double*)V, ldv, (const double*)w, partials);
+    else {
+        gb::set_error("multi_dot: dtype must be f32 or f64");
+        return GB_ERR_UNSUPPORTED;
+    }
+    gb::k_multi_dot_finish<<<ncols, 32, 0, stream>>>(gb::MD_PARTS, partials, out);
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+// w = beta * w + alpha * sum_c coef[c] * V[c]  (coef: device doubles)
+GB_API int gb_multi_axpy(int dtype, int64_t n, int ncols, const void* V, int64_t ldv, const double* coef, double alpha,
+                         double beta, void* w, cudaStream_t stream)
+{
+    GB_REQUIRE(ncols >= 0 && n >= 0, "multi_axpy: bad sizes");
+    if (n == 0) return GB_OK;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(n, 256), kSmCount * 8));
+    if (dtype == GB_F32)
+        gb::k_multi_axpy<float><<<grid, 256, 0, stream>>>(n, ncols, (const float*)V, ldv, coef, alpha, beta, (float*)w);
+    else if (dtype == GB_F64)
+        gb::k_multi_axpy<double><<<grid, 256, 0, stream>>>(n, ncols, (const double*)V, ldv, coef, alpha, beta,
+                                                           (double*)w);
+    else {
+        gb::set_error("multi_axpy: dtype must be f32 or f64");
+        return GB_ERR_UNSUPPORTED;
+    }
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}

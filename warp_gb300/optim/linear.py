@@ -44,6 +44,10 @@ __all__ = [
     "bicgstab",
     "CG",
     "BiCGSTAB",
+    "CR",
+    "cr",
+    "GMRES",
+    "gmres",
     "solve_refined",
 ]
 
@@ -492,6 +496,193 @@ class CG(LinearSolverState):
         return it, math.sqrt(rr), atol_v
 
 
+def _generic_return(self, it, rr, atol_sq, device):
+    if self._check_every == 0:
+        return (torch.tensor([it], dtype=torch.int32, device=device),
+                torch.tensor([rr], dtype=torch.float64, device=device),
+                torch.tensor([atol_sq], dtype=torch.float64, device=device))
+    return it, math.sqrt(rr), math.sqrt(atol_sq)
+
+
+class CR(LinearSolverState):
+    """Conjugate Residual (reference: ``linear.py:1124-1286``, kernels ``:2377-2423``): minimises the
+    A-norm of the (preconditioned) residual for symmetric A; same tolerance rule and returns as
+    ``CG``.  Runs on the generic path (library matvec / dot / axpby kernels, host-read scalars)."""
+
+    def __init__(self, A_, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_every=10,
+                 use_cuda_graph=True, restart=None):
+        if restart is not None and (isinstance(restart, bool) or not isinstance(restart, int) or restart < 1):
+            raise ValueError("restart must be a positive integer")
+        self._restart = restart
+        super().__init__(A_, b, x, tol, atol, maxiter, M, callback, check_every, use_cuda_graph)
+
+    def _fused_eligible(self, Aop, Mop, b, x) -> bool:
+        return False
+
+    def _run_generic(self, Aop, b, x, Mop):
+        rtol, atol = _get_tolerances(b.dtype, self._tol, self._atol)
+        r = torch.empty_like(b)
+        z = torch.zeros_like(b) if Mop is not None else r
+        Az = torch.zeros_like(b)
+        y = torch.zeros_like(b) if Mop is not None else None
+        (bb,) = self._dots([(b, b)])
+        atol_v = max(rtol * math.sqrt(bb), atol)
+        atol_sq = atol_v * atol_v
+
+        def refresh():
+            Aop.matvec(x, b, r, -1.0, 1.0)
+            if Mop is not None:
+                Mop.matvec(r, z, z, 1.0, 0.0)
+            Aop.matvec(z, Az, Az, 1.0, 0.0)
+            return self._dots([(r, r), (z, Az)])
+
+        rr, zAz = refresh()
+        p, Ap = z.clone(), Az.clone()
+        it = 0
+        if self._callback is not None and self._check_every > 0:
+            self._callback(0, math.sqrt(rr), atol_v)
+        while not (rr <= atol_sq) and it < self._maxiter:
+            zAz_old = zAz
+            yv = Ap
+            if Mop is not None:
+                Mop.matvec(Ap, y, y, 1.0, 0.0)
+                yv = y
+            (yAp,) = self._dots([(Ap, yv)])
+            alpha = zAz_old / yAp if (rr > atol_sq and yAp > 0.0) else 0.0
+            self._axpby(alpha, p, 1.0, x, x)
+            self._axpby(-alpha, Ap, 1.0, r, r)
+            if Mop is not None:
+                self._axpby(-alpha, y, 1.0, z, z)
+            it += 1
+            if self._restart is not None and it % self._restart == 0:
+                rr, zAz = refresh()
+                p.copy_(z)
+                Ap.copy_(Az)
+            else:
+                Aop.matvec(z, Az, Az, 1.0, 0.0)
+                rr, zAz = self._dots([(r, r), (z, Az)])
+                beta = zAz / zAz_old if (rr > atol_sq and zAz_old > 0.0) else 0.0
+                self._axpby(1.0, z, beta, p, p)
+                self._axpby(1.0, Az, beta, Ap, Ap)
+            if self._callback is not None and self._check_every > 0 and it % self._check_every == 0:
+                self._callback(it, math.sqrt(rr), atol_v)
+        return _generic_return(self, it, rr, atol_sq, b.device)
+
+
+class GMRES(LinearSolverState):
+    """Restarted GMRES(k) (reference: ``linear.py:1653-1916``, least squares ``:2497-2560``): each
+    cycle runs k Arnoldi steps (one-pass classical Gram-Schmidt against the basis, library multi-dot
+    / multi-axpy kernels), solves the small least-squares problem by Givens QR with the pivot
+    tolerance eps^2 (on the host, float64), updates x, and tests the true residual
+    ||b - A x|| <= max(rtol ||b||, atol).  Left or right preconditioning; the iteration count
+    advances by k per cycle, as in the reference."""
+
+    def __init__(self, A_, b, x, tol=None, atol=None, restart=31, maxiter=0, M=None, callback=None, check_every=31,
+                 use_cuda_graph=True, is_left_preconditioner=False):
+        self._restart = int(restart)
+        self._is_left_preconditioner = bool(is_left_preconditioner)
+        super().__init__(A_, b, x, tol, atol, maxiter, M, callback, check_every, use_cuda_graph)
+        self._restart = max(1, min(self._restart, self._maxiter))
+        if self._check_every > 0:
+            self._check_every = max(self._restart, self._check_every)
+
+    def _fused_eligible(self, Aop, Mop, b, x) -> bool:
+        return False
+
+    def _run_generic(self, Aop, b, x, Mop):
+        L = N.lib()
+        dt = b.dtype
+        gdt = A.gb_dtype(dt)
+        rtol, atol = _get_tolerances(dt, self._tol, self._atol)
+        pivot = _dtype_epsilon(dt) ** 2
+        k = self._restart
+        n = b.numel()
+        left = self._is_left_preconditioner and Mop is not None
+        V = torch.zeros((k + 1, n), dtype=dt, device=b.device)
+        r = torch.empty_like(b)
+        w = torch.zeros_like(b)
+        tmp = torch.zeros_like(b)
+        h_dev = A.zeros(k + 1, torch.float64)
+        ws = A.workspace(int(L.gb_multi_dot_workspace_bytes(k + 1)))
+        stream = A.stream()
+        (bb,) = self._dots([(b, b)])
+        atol_v = max(rtol * math.sqrt(bb), atol)
+        atol_sq = atol_v * atol_v
+        Aop.matvec(x, b, r, -1.0, 1.0)
+        (rr,) = self._dots([(r, r)])
+        it = 0
+        if self._callback is not None and self._check_every > 0:
+            self._callback(0, math.sqrt(rr), atol_v)
+        while not (rr <= atol_sq) and it < self._maxiter:
+            rh = r
+            if left:
+                Mop.matvec(r, w, w, 1.0, 0.0)
+                rh = w
+            (beta2,) = self._dots([(rh, rh)])
+            beta = math.sqrt(beta2)
+            self._axpby(1.0 / beta if beta2 != 0.0 else 1.0, rh, 0.0, rh, V[0])
+            H = np.zeros((k + 1, k))
+            for j in range(k):
+                if Mop is not None:
+                    if left:
+                        Aop.matvec(V[j], tmp, tmp, 1.0, 0.0)
+                        Mop.matvec(tmp, w, w, 1.0, 0.0)
+                    else:
+                        Mop.matvec(V[j], tmp, tmp, 1.0, 0.0)
+                        Aop.matvec(tmp, w, w, 1.0, 0.0)
+                else:
+                    Aop.matvec(V[j], w, w, 1.0, 0.0)
+                N.check(L.gb_multi_dot(gdt, n, j + 1, A.ptr(V), n, A.ptr(w), A.ptr(h_dev), A.ptr(ws), ws.numel(),
+                                       stream), "multi_dot")
+                N.check(L.gb_multi_axpy(gdt, n, j + 1, A.ptr(V), n, A.ptr(h_dev), -1.0, 1.0, A.ptr(w), stream),
+                        "multi_axpy")
+                H[: j + 1, j] = h_dev[: j + 1].cpu().numpy()
+                (hh,) = self._dots([(w, w)])
+                H[j + 1, j] = math.sqrt(hh)
+                self._axpby(1.0 / math.sqrt(hh) if hh != 0.0 else 1.0, w, 0.0, w, V[j + 1])
+            y = _gmres_least_squares(H, beta, pivot)
+            coef = A.from_numpy(np.concatenate([y, np.zeros(k + 1 - len(y))]).astype(np.float64))
+            if Mop is None or left:
+                N.check(L.gb_multi_axpy(gdt, n, k, A.ptr(V), n, A.ptr(coef), 1.0, 1.0, A.ptr(x), stream), "update x")
+            else:
+                N.check(L.gb_multi_axpy(gdt, n, k, A.ptr(V), n, A.ptr(coef), 1.0, 0.0, A.ptr(w), stream), "update w")
+                Mop.matvec(w, tmp, tmp, 1.0, 0.0)
+                self._axpby(1.0, tmp, 1.0, x, x)
+            Aop.matvec(x, b, r, -1.0, 1.0)
+            (rr,) = self._dots([(r, r)])
+            it += k
+            if self._callback is not None and self._check_every > 0 and it % self._check_every < k:
+                self._callback(it, math.sqrt(rr), atol_v)
+        return _generic_return(self, it, rr, atol_sq, b.device)
+
+
+def _gmres_least_squares(H: np.ndarray, beta: float, pivot: float) -> np.ndarray:
+    """min ||beta e1 - H y|| for the (k+1) x k Hessenberg H by Givens rotations; stops at the first
+    rotation whose pivot norm^2 is below ``pivot`` (the Arnoldi process ended early)."""
+    H = H.copy()
+    k = H.shape[1]
+    g = np.zeros(k + 1)
+    rhs = beta
+    kk = k
+    for i in range(k):
+        a, b_ = H[i, i], H[i + 1, i]
+        n2 = a * a + b_ * b_
+        if n2 < pivot:
+            kk = i
+            break
+        nrm = math.sqrt(n2)
+        c, s = a / nrm, b_ / nrm
+        Hi, Hj = H[i, i:].copy(), H[i + 1, i:].copy()
+        H[i, i:] = c * Hi + s * Hj
+        H[i + 1, i:] = c * Hj - s * Hi
+        g[i] = c * rhs
+        rhs = -s * rhs
+    y = np.zeros(kk)
+    for i in range(kk - 1, -1, -1):
+        y[i] = (g[i] - H[i, i + 1:kk] @ y[i + 1:kk]) / H[i, i]
+    return y
+
+
 class BiCGSTAB(LinearSolverState):
     """Pre-allocated BiCGSTAB solver (reference: ``linear.py:1377-1574``)."""
 
@@ -624,6 +815,26 @@ def cg(A_, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_ev
     """Preconditioned Conjugate Gradient (reference: ``linear.py:1035-1121``)."""
     state = CG(A_, b, x, tol=tol, atol=atol, maxiter=maxiter, M=M, callback=callback, check_every=check_every,
                use_cuda_graph=use_cuda_graph, restart=restart)
+    if run:
+        return state()
+    return state
+
+
+def cr(A_, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_every=10, use_cuda_graph=True,
+       run=True, *, restart=None):
+    """Conjugate Residual (reference: ``linear.py:1288-1374``)."""
+    state = CR(A_, b, x, tol=tol, atol=atol, maxiter=maxiter, M=M, callback=callback, check_every=check_every,
+               use_cuda_graph=use_cuda_graph, restart=restart)
+    if run:
+        return state()
+    return state
+
+
+def gmres(A_, b, x, tol=None, atol=None, restart=31, maxiter=0, M=None, callback=None, check_every=31,
+          use_cuda_graph=True, is_left_preconditioner=False, run=True):
+    """Restarted GMRES(k) (reference: ``linear.py:1918-2008``)."""
+    state = GMRES(A_, b, x, tol=tol, atol=atol, restart=restart, maxiter=maxiter, M=M, callback=callback,
+                  check_every=check_every, use_cuda_graph=use_cuda_graph, is_left_preconditioner=is_left_preconditioner)
     if run:
         return state()
     return state
