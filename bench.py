@@ -262,7 +262,15 @@ def bench_elasticity(args, hbm_peak):
         infos.append(solver.solve(s.b, tol=1e-8)[1])
 
     ms = _event_ms(step, 2, warmup=0)
+    # bf16 storage of the matrix values for the FP32 inner loop (the FP64 residual keeps fp32 values)
+    bsolver = linear.RefinedSolver(A, M=linear.preconditioner(A, "diag"), inner_tol=args.inner_tol,
+                                   inner_values=A.values[:nnz].to(torch.bfloat16).contiguous())
+    binfos = []
+    bsolver.solve(s.b, tol=1e-8)
+    bms = _event_ms(lambda: binfos.append(bsolver.solve(s.b, tol=1e-8)[1]), 2, warmup=0)
     return {"workload": f"{args.elasticity_res}^3 Q1 vec3 elasticity, {A.nrow} block rows, {nnz} blocks",
+            "jacobi_cg_refined_bf16_values_ms": bms, "bf16_inner_iterations": binfos[-1]["inner_iterations"],
+            "bf16_outer_iterations": binfos[-1]["outer"], "bf16_rel_residual": binfos[-1]["rel_residual"],
             "bsr_mv_us": mv_ms * 1e3, "bsr_mv_gbs": mv_bytes / (mv_ms * 1e-3) / 1e9,
             "bsr_mv_frac_of_hbm": mv_bytes / (mv_ms * 1e-3) / 1e9 / hbm_peak,
             "jacobi_cg_refined_ms": ms, "inner_iterations": infos[-1]["inner_iterations"],

@@ -87,7 +87,7 @@ class MultigridPreconditioner:
             cgeo = fem.Grid3D(res=cres, bounds_lo=cur_geo.bounds_lo, bounds_hi=cur_geo.bounds_hi)
             space = fem.make_polynomial_space(cgeo, degree=1)
             cA = fem.integrate(fem.diffusion_form, fields={"u": fem.make_trial(space), "v": fem.make_test(space)},
-                               values={"nu": ccoef})
+                               values={"nu": ccoef}, bsr_options={"construction": "row_compress"})
             rhs = A.zeros(cgeo.node_count(), torch.float32)
             bd = fem.BoundarySides(cgeo, self.faces)
             P = fem.integrate(fem.boundary_projector_form,
