@@ -178,7 +178,11 @@ def bench_batched(args, hbm_peak):
     from warp_gb300.optim import linear
 
     rng = np.random.default_rng(args.seed)
-    ncells = rng.integers(16, 129, size=args.batch_count)
+    ncells_all = rng.integers(16, 129, size=args.batch_count)
+    ws, rank = _dist()
+    # N GPUs: the systems are split by batched.shard (weak in work per GPU, no collective)
+    mine = batched.shard((ncells_all + 1) ** 2, rank, ws)
+    ncells = ncells_all[mine]
     t0 = time.perf_counter()
     Am, b, offs = batched.q1_batch_2d(ncells, sigma=1.0, corr_length=0.1, seed=args.seed)
     build_s = time.perf_counter() - t0
@@ -194,7 +198,7 @@ def bench_batched(args, hbm_peak):
         x.zero_()
         solver.solve(b, x)
 
-    ms = _event_ms(step, args.steps, warmup=2)
+    ms = _barrier_max(_event_ms(step, args.steps, warmup=2), ws)
     it = solver.iters.cpu().numpy()
     rows = np.diff(offs.cpu().numpy())
     nnz_rows = (3 * ncells + 1) ** 2
@@ -204,8 +208,9 @@ def bench_batched(args, hbm_peak):
     gbs = algo / (ms * 1e-3) / 1e9
     conv = float((solver.rr <= solver.atol_sq).float().mean())
     return {"workload": f"{args.batch_count} Q1 2-D diffusion systems, n ~ U{{16..128}} cells/side, "
-                        f"{int(rows.sum())} rows, {int(nnz_rows.sum())} nnz, Jacobi-CG to 1e-6 each",
+                        f"{int(rows.sum())} rows, {int(nnz_rows.sum())} nnz on this rank, Jacobi-CG to 1e-6 each",
             "ms": ms, "systems_per_s": args.batch_count / (ms * 1e-3), "launches_per_solve": 2,
+            "sharding": f"{len(mine)} of {args.batch_count} systems on rank {rank} of {ws} (batched.shard)",
             "config": {k: v for k, v in solver.config.items() if k != "tuned_ms"},
             "iterations": {"min": int(it.min()), "median": float(np.median(it)), "max": int(it.max())},
             "converged_fraction": conv, "status": int(solver.status.item()),

@@ -225,3 +225,23 @@ def q1_batch_2d(ncells, sigma: float = 1.0, corr_length: float = 0.1, seed: int 
     if return_fields:
         return Am, b, A.from_numpy(row_off), dict(coef=coef, f=f, cell_off=cell_off, row_off=row_off)
     return Am, b, A.from_numpy(row_off)
+
+
+def shard(sizes, rank: int, world: int) -> np.ndarray:
+    """Subproblems of ``rank`` when a batch is split over ``world`` GPUs (no collective on the data
+    path: every rank computes the same deterministic split from the sizes alone).  Greedy
+    largest-first assignment to the least-loaded rank by the estimated work rows^1.5 (Jacobi-CG
+    iterations grow like the grid width); returns the rank's subproblem ids in increasing order."""
+    sizes = np.asarray(sizes, np.float64)
+    if world <= 1:
+        return np.arange(len(sizes))
+    if not 0 <= rank < world:
+        raise ValueError("rank out of range")
+    order = np.argsort(-sizes, kind="stable")
+    load = np.zeros(world)
+    owner = np.empty(len(sizes), np.int64)
+    for i in order:
+        r = int(np.argmin(load))
+        owner[i] = r
+        load[r] += sizes[i] ** 1.5
+    return np.nonzero(owner == rank)[0]
