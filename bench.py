@@ -25,6 +25,7 @@ host cores for the same workload, and prints the same line with impl=reference.
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import math
 import os
@@ -52,26 +53,36 @@ def _peaks():
 
 
 class ClockSampler:
-    """nvidia-smi clock/throttle sampling during the timed region."""
+    """nvidia-smi clock/throttle sampling around the timed region.
+
+    The sampler is started before the warm-up (so that spawning nvidia-smi does not stall the host
+    inside the timed region) and polls every 50 ms; each sample carries nvidia-smi's timestamp, and
+    summary() keeps the samples whose timestamps fall inside the window set by mark()."""
+
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu_index: int = 0):
         self.proc = None
         self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
         self.gpu = gpu_index
+        self.window = None
 
     def __enter__(self):
         try:
             os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
-                ["nvidia-smi", "-i", str(self.gpu),
-                 "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
-                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
-                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
-                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
         return self
+
+    def mark(self, t0, t1):
+        """The timed region, as host datetimes."""
+        self.window = (t0, t1)
 
     def __exit__(self, *exc):
         if self.proc is not None:
@@ -85,24 +96,32 @@ class ClockSampler:
     def summary(self):
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        rows = []
         try:
             for line in open(self.path):
                 parts = [p.strip() for p in line.split(",")]
-                if len(parts) < 9:
+                if len(parts) < 10:
                     continue
                 try:
-                    sm.append(float(parts[1]))
-                    smax.append(float(parts[2]))
+                    ts = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f")
+                    rows.append((ts, float(parts[2]), float(parts[3]),
+                                 {nm for nm, v in zip(names, parts[6:10]) if v.lower().startswith("active")}))
                 except ValueError:
                     continue
-                for nm, v in zip(names, parts[5:9]):
-                    if v.lower().startswith("active"):
-                        reasons.add(nm)
         except OSError:
             pass
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+        inside = rows
+        if self.window is not None and rows:
+            t0, t1 = self.window
+            pad = datetime.timedelta(milliseconds=60)
+            inside = [r for r in rows if t0 - pad <= r[0] <= t1 + pad]
+            if not inside:  # region shorter than the sampling interval: the nearest sample
+                mid = t0 + (t1 - t0) / 2
+                inside = [min(rows, key=lambda r: abs((r[0] - mid).total_seconds()))]
+        sm = [r[1] for r in inside]
+        reasons = set().union(*[r[3] for r in inside]) if inside else set()
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(r[2] for r in inside) if inside else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
@@ -404,7 +423,7 @@ def run_profile(args):
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--steps", type=int, default=20)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--res", type=int, nargs="+", default=[96, 96, 96])
@@ -455,24 +474,27 @@ def main():
     from warp_gb300 import learned, multigrid
 
     def timed(solver, b, steps, sample_clocks=False):
+        sampler = ClockSampler(local) if sample_clocks else None
+        if sampler:
+            sampler.__enter__()
         for _ in range(args.warmup):
             solver.solve(b, tol=1e-8)
         torch.cuda.synchronize()
         infos = []
-        sampler = ClockSampler(local) if sample_clocks else None
-        if sampler:
-            sampler.__enter__()
         if ws > 1:
             torch.distributed.barrier()
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         launches0 = solver.kernel_launches
+        w0 = datetime.datetime.now()
         e0.record(stream)
         for _ in range(steps):
             _, info = solver.solve(b, tol=1e-8)
             infos.append(info)
         e1.record(stream)
         torch.cuda.synchronize()
+        if sampler:
+            sampler.mark(w0, datetime.datetime.now())
         launches = solver.kernel_launches - launches0
         if ws > 1:
             torch.distributed.barrier()
@@ -539,6 +561,13 @@ def main():
     mv_s = m0.elapsed_time(m1) / args.mv_launches * 1e-3
     mv_bytes = nnz * (4 + 4) + (n + 1) * 4 + n * 4 + n * 4
     mv_gbs = mv_bytes / mv_s / 1e9
+    # the same number of bytes moved by a plain device copy (read + write = mv_bytes): the bandwidth a
+    # single launch of this size reaches (ramp-up and tail included), for context beside the peak
+    cbuf = torch.empty(mv_bytes // 8, dtype=torch.float32, device="cuda")
+    cdst = torch.empty_like(cbuf)
+    copy_s = _event_ms(lambda: cdst.copy_(cbuf), args.mv_launches, warmup=3) * 1e-3
+    copy_gbs = mv_bytes / copy_s / 1e9
+    del cbuf, cdst
     traffic = None
     try:
         with open(os.path.join(ROOT, "profiles", "bsr_mv_96cube.md")) as f:
@@ -640,7 +669,8 @@ def main():
                    "mg_levels": lmg.describe()},
         "roofline": {"bound": "hbm", "kernel": "k_bsr_mv<1,1,float>", "achieved": mv_gbs, "peak": hbm_peak,
                      "unit": "GB/s", "frac": mv_gbs / hbm_peak, "peak_kind": peak_kind,
-                     "algorithmic_bytes": mv_bytes, "traffic": traffic, "launch_us": mv_s * 1e6},
+                     "algorithmic_bytes": mv_bytes, "traffic": traffic, "launch_us": mv_s * 1e6,
+                     "same_size_copy_gbs": copy_gbs, "frac_of_same_size_copy": mv_gbs / copy_gbs},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_ms, "unit": "ms", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "e2e_with_setup": {"value": e2e_setup_ms, "unit": "ms", "h2d_bytes_per_step": h2d_setup,

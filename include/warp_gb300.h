@@ -35,6 +35,12 @@ enum { GB_KRYLOV_CG = 0, GB_KRYLOV_BICGSTAB = 1 };
 const char* gb_last_error(void);
 void gb_clear_error(void);
 int gb_version(void);
+
+/* Programmatic dependent launch of the eagerly launched solver-loop kernels (default on; launches
+ * into a capturing stream stay plain).  No reference counterpart:
+ * a launch option of this library; results are identical either way. */
+int gb_set_pdl(int enabled);
+int gb_get_pdl(void);
 int gb_device_arch(void);
 
 /* ---- prefix sums ---------------------------------------------------------------------------

@@ -102,7 +102,10 @@ def test_conv3_bf16_tensor_core_matches_oracle(cuda, dims, cout, relu):
     np.testing.assert_allclose(got, ref, rtol=8e-3, atol=1e-3 * np.abs(ref).max())
 
 
-@pytest.mark.parametrize("dims", [(1, 1, 1), (2, 4, 16), (7, 9, 11), (9, 7, 35), (33, 17, 20), (20, 12, 97)])
+# (64, 40, 40) and (300, 10, 10): more work items (columns x slabs) than CTAs, so CTAs walk several
+# x-slabs and cross column boundaries in their shared-memory ring of x-plane blocks
+@pytest.mark.parametrize("dims", [(1, 1, 1), (2, 4, 16), (7, 9, 11), (9, 7, 35), (33, 17, 20), (20, 12, 97),
+                                  (64, 40, 40), (300, 10, 10)])
 def test_conv3_tcgen05_layer_matches_oracle(cuda, dims):
     """tcgen05 implicit-GEMM layer on the planar padded layout: equal to the oracle on bf16-rounded
     operands up to output rounding; border rows stay zero; no device status raised."""
@@ -128,7 +131,7 @@ def test_conv3_tcgen05_layer_matches_oracle(cuda, dims):
     assert int(status.item()) == 0
 
 
-@pytest.mark.parametrize("dims", [(5, 6, 7), (24, 25, 25)])
+@pytest.mark.parametrize("dims", [(5, 6, 7), (24, 25, 25), (64, 40, 40)])
 def test_conv3_tcgen05_last_layer_fuses_jacobi_step(cuda, dims):
     import warp_gb300._native as N
     from warp_gb300 import learned

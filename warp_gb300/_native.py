@@ -32,6 +32,8 @@ _SIGNATURES = {
     "gb_last_error": (ctypes.c_char_p, []),
     "gb_clear_error": (None, []),
     "gb_version": (_c_int, []),
+    "gb_set_pdl": (_c_int, [_c_int]),
+    "gb_get_pdl": (_c_int, []),
     "gb_device_arch": (_c_int, []),
     "gb_scan_i32_workspace_bytes": (_c_sz, [_c_i64]),
     "gb_scan_i32": (_c_int, [_vp, _vp, _c_i64, _c_int, _vp, _c_sz, _vp]),

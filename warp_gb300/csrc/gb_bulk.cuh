@@ -1,9 +1,11 @@
 // gb_bulk.cuh -- 1-D bulk-copy (TMA, cp.async.bulk) and mbarrier helpers for sm_103a.
 //
-// Every wait is bounded in time: a non-blocking mbarrier.test_wait is polled with a short sleep
-// against the %globaltimer clock; after kWaitLimitNs the caller gets `false`, ORs
-// GB_DEV_WAIT_TIMEOUT into its status word and drains (again bounded) before returning, so a
-// kernel can never hang the GPU on a barrier.
+// Every wait is bounded in time: mbarrier.try_wait (which suspends the thread until the phase
+// completes or a short hardware time limit passes) is repeated against the %globaltimer clock; after
+// kWaitLimitNs the caller gets `false`, ORs GB_DEV_WAIT_TIMEOUT into its status word and drains
+// (again bounded) before returning, so a kernel can never hang the GPU on a barrier.  (A
+// test_wait poll with __nanosleep between polls was measured to add ~1.4 us whenever the first poll
+// missed.)
 #pragma once
 #include "gb_common.cuh"
 
@@ -73,12 +75,11 @@ __device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity)
 // Wait on phase `parity`, bounded by kWaitLimitNs of wall time; false if the limit was reached.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity)
 {
-    if (mbar_test_wait(bar, parity)) return true;
+    if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = globaltimer_ns();
     for (;;) {
-        if (mbar_test_wait(bar, parity)) return true;
+        if (mbar_try_wait(bar, parity)) return true;
         if (globaltimer_ns() - t0 > kWaitLimitNs) return false;
-        __nanosleep(64);
     }
 }
 

@@ -22,6 +22,10 @@ int cuda_fail(cudaError_t err, const char* what)
     return GB_ERR_CUDA;
 }
 
+static int g_pdl = 1;  // 0 off, 1 eager launches only, 2 eager launches and stream captures
+
+bool pdl_enabled(bool capturing) { return capturing ? g_pdl >= 2 : g_pdl >= 1; }
+
 }  // namespace gb
 
 GB_API const char* gb_last_error(void) { return gb::g_last_error; }
@@ -29,6 +33,19 @@ GB_API const char* gb_last_error(void) { return gb::g_last_error; }
 GB_API void gb_clear_error(void) { gb::g_last_error[0] = 0; }
 
 GB_API int gb_version(void) { return 100; }  // 1.0.0
+
+// Programmatic dependent launch of the solver-loop kernels (multigrid transfers and smoothing,
+// SpMV, Krylov updates, conv-net layers): on by default.  Off launches the same kernels with plain
+// stream ordering.  Takes effect for eager launches made after the call; launches into a capturing
+// stream are plain either way.
+GB_API int gb_set_pdl(int mode)
+{
+    GB_REQUIRE(mode >= 0 && mode <= 2, "set_pdl: mode must be 0, 1 or 2");
+    gb::g_pdl = mode;
+    return GB_OK;
+}
+
+GB_API int gb_get_pdl(void) { return gb::g_pdl; }
 
 // Returns the compute capability (major*10+minor) of the current device, or a negative status.
 GB_API int gb_device_arch(void)

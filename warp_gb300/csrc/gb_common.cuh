@@ -50,6 +50,44 @@ int cuda_fail(cudaError_t err, const char* what);
 
 constexpr int kSmCount = 152;  // GB300: 2 dies x 76 SMs
 
+// Programmatic dependent launch.  A kernel launched with launch_pdl() may be scheduled while the
+// previous kernel of the stream drains; every such kernel calls pdl_enter() before its first global
+// memory access: it lets its own successor be scheduled (launch_dependents) and then waits until its
+// predecessor grid has completed and its writes are visible (wait).  Without the launch attribute both
+// instructions are no-ops, so the same kernels may also be launched normally.  Launches into a
+// capturing stream stay plain: inside a CUDA graph the early scheduling measured slower (1-2% on the
+// graph-captured solves), while eager launch sequences gain (multigrid V-cycle 241 -> 203 us at 97^3).
+__device__ __forceinline__ void pdl_enter()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
+// Process-wide switch (gb_set_pdl): whether a launch into a capturing / non-capturing stream gets
+// the programmatic-serialization attribute.
+bool pdl_enabled(bool capturing);
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                              Args&&... args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    const cudaError_t qerr = cudaStreamIsCapturing(stream, &cap);
+    if (qerr != cudaSuccess) (void)cudaGetLastError();  // the query's own error; the launch reports its own
+    const bool capturing = qerr != cudaSuccess || cap != cudaStreamCaptureStatusNone;
+    cfg.numAttrs = pdl_enabled(capturing) ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
+
 template <typename T> __host__ __device__ inline T ceil_div(T a, T b) { return (a + b - 1) / b; }
 
 __device__ __forceinline__ float to_f32(float v) { return v; }

@@ -35,25 +35,53 @@ namespace gb {
 
 constexpr int TC_M = 128;                  // rows of one window (UMMA M)
 constexpr int TC_OUT = TC_M - 2;           // output rows per window
-constexpr int TC_SUB = 4;                  // windows per stage
+constexpr int TC_SUB = 4;                  // windows per work item (504 output rows of one x-slab)
 constexpr int TC_N = 48;                   // 3 dz taps x 16 output channels (UMMA N)
+constexpr int TC_ISSUERS = TC_SUB;         // one MMA-issuing warp per window
 constexpr int TC_EPI_GROUPS = 2;           // epilogue groups of 4 warps (one per TMEM lane quarter)
-constexpr int TC_THREADS = 64 + TC_EPI_GROUPS * 128;  // warp 0 copies, warp 1 MMA, warps 2.. epilogue
+constexpr int TC_EPI_WARP0 = 1 + TC_ISSUERS;  // warp 0 copies, warps 1..4 issue MMAs, then the epilogue
+constexpr int TC_THREADS = 32 * TC_EPI_WARP0 + TC_EPI_GROUPS * 128;
 constexpr uint32_t TC_TMEM_COLS = 512;     // 2 slots x 4 windows x 48 columns = 384, rounded up
 constexpr int TC_W_BYTES = 9 * 1536;       // per (dx, dy): [k-half][dz 3 x co 16][8 ci] bf16
-constexpr int TC_XCHG_BYTES = TC_EPI_GROUPS * 2 * 4 * 2 * 16 * 4;
-constexpr int TC_MAX_STAGES = 3;
+constexpr int TC_WPG = TC_SUB / TC_EPI_GROUPS;  // windows per epilogue group per item (drained together)
+constexpr int TC_XCHG_BYTES = TC_EPI_GROUPS * 2 * TC_WPG * 4 * 2 * 16 * 4;  // [group][parity][window][quarter][lo/hi][16]
+constexpr int TC_MAX_SLOTS = 8;            // x-plane blocks in the shared-memory ring
+constexpr int TC_MIN_SLOTS = 4;            // three in use (x-1, x, x+1) plus one in flight
+constexpr size_t TC_SMEM_LIMIT = 220 * 1024;
+constexpr int TC_BAR_PROLOGUE = 2 + TC_EPI_GROUPS;  // named barriers: 0 CTA, 1..groups epilogue groups,
+                                                    // 1 + groups all epilogue warps, then the prologue
+
+// Division by a loop-invariant divisor with a multiply and shifts (Granlund and Montgomery, "Division
+// by invariant integers using multiplication", PLDI 1994, figure 4.1): exact for every 32-bit n.
+struct FastDivU32 {
+    uint32_t m, s1, s2;
+};
+
+static inline FastDivU32 make_fastdiv(uint32_t d)
+{
+    uint32_t l = 0;
+    while (l < 32 && (uint64_t(1) << l) < d) ++l;  // l = ceil(log2 d)
+    const uint64_t m = ((((uint64_t)1 << l) - d) << 32) / d + 1;
+    return FastDivU32{(uint32_t)m, l ? 1u : 0u, l ? l - 1 : 0u};
+}
+
+__device__ __forceinline__ uint32_t fastdiv(uint32_t n, FastDivU32 f)
+{
+    const uint32_t t = __umulhi(f.m, n);
+    return (t + ((n - t) >> f.s1)) >> f.s2;
+}
 
 struct TcConv {
     int nx, ny, nz;
+    FastDivU32 div_sx, div_sy;  // row -> (x, y, z) of the padded grid
     int sy;              // nz + 2
-    int stages;
+    int slots;           // x-plane blocks in the ring
+    int ncols;           // work items per x-slab (columns of TC_SUB * TC_OUT rows)
     int64_t sx;          // (ny + 2) * (nz + 2)
-    int64_t p_begin;     // first interior row
-    int64_t ntiles;      // stage tiles of TC_SUB * TC_OUT output rows
+    int64_t nitems;      // ncols * nx; item k = (column k / nx, x = 1 + k % nx)
     int64_t plane_rows;  // rows per plane (plane stride)
     uint32_t rows_bytes; // R * 16, R = 2 sy + TC_OUT (TC_SUB - 1) + TC_M
-    uint32_t stage_bytes;  // 6 * rows_bytes
+    uint32_t block_bytes;  // 2 * rows_bytes: one x-plane block, both channel planes
     const unsigned char* in;
     const __nv_bfloat16* Wt;  // [27][16 co][16 ci] bf16
     unsigned char* out;       // hidden layers: planar padded bf16
@@ -124,13 +152,12 @@ __device__ __forceinline__ float tc_ld1(uint32_t taddr)
 // bounded wait that also gives up when another role has aborted
 __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity, volatile int* abort_flag)
 {
-    if (mbar_test_wait(bar, parity)) return true;
+    if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = globaltimer_ns();
     for (;;) {
-        if (mbar_test_wait(bar, parity)) return true;
+        if (mbar_try_wait(bar, parity)) return true;
         if (*abort_flag) return false;
         if (globaltimer_ns() - t0 > kWaitLimitNs) return false;
-        __nanosleep(32);
     }
 }
 
@@ -149,121 +176,164 @@ template <bool LAST>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
-    unsigned char* stages = smem;
-    unsigned char* wsm = smem + (size_t)c.stages * c.stage_bytes;
-    float* xchg = reinterpret_cast<float*>(wsm + TC_W_BYTES);  // [parity][quarter][lo/hi][16]
+    pdl_enter();
+    unsigned char* ring = smem;
+    unsigned char* wsm = smem + (size_t)c.slots * c.block_bytes;
+    float* xchg = reinterpret_cast<float*>(wsm + TC_W_BYTES);  // [group][parity][window][quarter][lo/hi][16]
     uint64_t* full = reinterpret_cast<uint64_t*>(wsm + TC_W_BYTES + TC_XCHG_BYTES);
-    uint64_t* empty = full + TC_MAX_STAGES;
-    uint64_t* accfull = empty + TC_MAX_STAGES;
+    uint64_t* empty = full + TC_MAX_SLOTS;
+    uint64_t* accfull = empty + TC_MAX_SLOTS;
     uint64_t* accempty = accfull + 2;
-    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(accempty + 2);
+    uint64_t* done = accempty + 2;  // every issuer's last commit: all MMAs of the CTA completed
+    uint32_t* s_tmem = reinterpret_cast<uint32_t*>(done + 1);
     volatile int* s_abort = reinterpret_cast<volatile int*>(s_tmem + 1);
-    volatile int* s_counts = s_abort + 1;  // [0] copies issued, [1] tiles taken by MMA, [2] tiles committed
-    volatile int* s_epi_abort = s_counts + 3;  // written by epilogue warps only, read after their barrier
-    const int S = c.stages;
-
+    volatile int* s_issued = s_abort + 1;      // x-plane blocks whose copies were issued
+    volatile int* s_epi_abort = s_issued + 1;  // written by epilogue warps only, read after their barrier
+    const int NS = c.slots;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // contiguous range of work items; consecutive items of one column differ by one x-slab, so the
+    // blocks x and x+1 of an item are the blocks x-1 and x of the next one
+    const int64_t k_begin = (int64_t)blockIdx.x * c.nitems / gridDim.x;
+    const int64_t k_end = (int64_t)(blockIdx.x + 1) * c.nitems / gridDim.x;
+
     if (threadIdx.x == 0) {
-        for (int s = 0; s < S; ++s) {
+        for (int s = 0; s < NS; ++s) {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], 1);
+            mbar_init(&empty[s], TC_ISSUERS);
         }
         for (int a = 0; a < 2; ++a) {
-            mbar_init(&accfull[a], 1);
+            mbar_init(&accfull[a], TC_ISSUERS);
             mbar_init(&accempty[a], 4 * TC_EPI_GROUPS);
         }
+        mbar_init(done, TC_ISSUERS);
         *s_abort = 0;
+        *s_issued = 0;
         *s_epi_abort = 0;
-        s_counts[0] = s_counts[1] = s_counts[2] = 0;
         fence_mbar_init();
     }
-    // weights -> B operands: (dx, dy) pair g, k-half kc, row n = 16 dz_idx + co at g*1536 + kc*768 + n*16
-    for (int i = threadIdx.x; i < 27 * 16 * 2; i += blockDim.x) {
-        const int t = i >> 5, co = (i >> 1) & 15, kc = i & 1;
-        const int g = t / 3, dzi = t % 3;
-        const uint4 v = reinterpret_cast<const uint4*>(c.Wt)[(t * 16 + co) * 2 + kc];
-        *reinterpret_cast<uint4*>(wsm + g * 1536 + kc * 768 + (dzi * 16 + co) * 16) = v;
+    uint32_t tmem = 0;
+    if (warp == 0) {
+        // the copy warp needs only the barriers: it starts filling the ring while the other warps
+        // stage the weights and allocate TMEM
+        __syncwarp();
+        __threadfence_block();  // the barrier words and flags written by thread 0 before the arrival
+        asm volatile("bar.arrive %0, %1;" ::"r"(TC_BAR_PROLOGUE), "r"(TC_THREADS) : "memory");
+    } else {
+        // weights -> B operands: (dx, dy) pair g, k-half kc, row n = 16 dz_idx + co at g*1536 + kc*768 + n*16
+        for (int i = threadIdx.x - 32; i < 27 * 16 * 2; i += blockDim.x - 32) {
+            const int t = i >> 5, co = (i >> 1) & 15, kc = i & 1;
+            const int g = t / 3, dzi = t % 3;
+            const uint4 v = reinterpret_cast<const uint4*>(c.Wt)[(t * 16 + co) * 2 + kc];
+            *reinterpret_cast<uint4*>(wsm + g * 1536 + kc * 768 + (dzi * 16 + co) * 16) = v;
+        }
+        fence_proxy_async_shared();  // make the generic-proxy stores visible to the tensor cores
+        if (warp == 1) {
+            asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(s_tmem)),
+                         "r"(TC_TMEM_COLS)
+                         : "memory");
+            asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+        }
+        tc_fence_before();
+        asm volatile("bar.sync %0, %1;" ::"r"(TC_BAR_PROLOGUE), "r"(TC_THREADS) : "memory");
+        tc_fence_after();
+        tmem = *s_tmem;
     }
-    fence_proxy_async_shared();  // make the generic-proxy stores visible to the tensor cores
-    if (warp == 1) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(s_tmem)),
-                     "r"(TC_TMEM_COLS)
-                     : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    }
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const uint32_t tmem = *s_tmem;
 
     if (warp == 0) {
+        // ------------------------- copy warp: x-plane blocks into the ring ----------------------------
         if (lane == 0) {
-            int it = 0;
-            for (int64_t tile = blockIdx.x; tile < c.ntiles; tile += gridDim.x, ++it) {
-                const int s = it % S;
-                if (it >= S && !tc_wait(&empty[s], ((it / S) & 1) ^ 1, s_abort)) {
-                    *s_abort = 1;
-                    break;
-                }
-                if (*s_abort) break;
-                const int64_t q0 = c.p_begin + tile * (TC_SUB * TC_OUT) - 1;
-                unsigned char* dst = stages + (size_t)s * c.stage_bytes;
-                mbar_arrive_expect_tx(&full[s], c.stage_bytes);
-#pragma unroll
-                for (int b = 0; b < 3; ++b) {
-                    const int64_t row = q0 + (int64_t)(b - 1) * c.sx - c.sy;
+            int q = 0;  // sequence number of the next block; its slot is q % NS
+            bool ok = true;
+            for (int64_t k = k_begin; k < k_end && ok;) {
+                const int o = (int)(k / c.nx);
+                const int x0 = (int)(k % c.nx) + 1;
+                const int64_t run_end = min(k_end, (int64_t)(o + 1) * c.nx);
+                const int x1 = (int)((run_end - 1) % c.nx) + 1;
+                for (int xb = x0 - 1; xb <= x1 + 1; ++xb, ++q) {
+                    const int s = q % NS;
+                    if (q >= NS && !tc_wait(&empty[s], ((q / NS) - 1) & 1, s_abort)) {
+                        *s_abort = 1;
+                        ok = false;
+                        break;
+                    }
+                    if (*s_abort) {
+                        ok = false;
+                        break;
+                    }
+                    const int64_t row = (int64_t)xb * c.sx + (int64_t)o * (TC_SUB * TC_OUT);
+                    unsigned char* dst = ring + (size_t)s * c.block_bytes;
+                    mbar_arrive_expect_tx(&full[s], c.block_bytes);
 #pragma unroll
                     for (int h = 0; h < 2; ++h)
-                        bulk_g2s(dst + (b * 2 + h) * c.rows_bytes, c.in + ((int64_t)h * c.plane_rows + row) * 16,
-                                 c.rows_bytes, &full[s]);
+                        bulk_g2s(dst + h * c.rows_bytes, c.in + ((int64_t)h * c.plane_rows + row) * 16, c.rows_bytes,
+                                 &full[s]);
+                    *s_issued = q + 1;
                 }
-                s_counts[0] = it + 1;
+                k = run_end;
             }
         }
-    } else if (warp == 1) {
+    } else if (warp <= TC_ISSUERS) {
+        // ------------- MMA warps: warp 1 + j issues the 9 (dx, dy) MMAs of window j --------------------
         if (lane == 0) {
+            const int j = warp - 1;
             const uint32_t wbase = smem_u32(wsm);
-            int it = 0;
-            for (int64_t tile = blockIdx.x; tile < c.ntiles; tile += gridDim.x, ++it) {
-                const int s = it % S;
-                const int a = it & 1;
-                if (!tc_wait(&full[s], (it / S) & 1, s_abort)) {
-                    *s_abort = 1;
-                    break;
-                }
-                s_counts[1] = it + 1;
-                if (it >= 2 && !tc_wait(&accempty[a], ((it >> 1) & 1) ^ 1, s_abort)) {
-                    *s_abort = 1;
-                    break;
-                }
-                tc_fence_after();
-                const uint32_t base = smem_u32(stages + (size_t)s * c.stage_bytes);
-#pragma unroll 1
-                for (int g = 0; g < 9; ++g) {
-                    const int b = g / 3, dyi = g % 3;
-                    const uint64_t bdesc = umma_desc(wbase + g * 1536, 768, 128);
-                    const uint32_t arow = base + (uint32_t)(b * 2) * c.rows_bytes + (uint32_t)(dyi * c.sy) * 16u;
+            const uint32_t rbase = smem_u32(ring);
+            int it = 0;  // items of this CTA so far (TMEM slot it & 1)
+            int q0 = 0;  // sequence number of the current run's first block (x0 - 1)
+            bool ok = true;
+            for (int64_t k = k_begin; k < k_end && ok;) {
+                const int o = (int)(k / c.nx);
+                const int64_t run_end = min(k_end, (int64_t)(o + 1) * c.nx);
+                const int run = (int)(run_end - k);
+                for (int t = 0; t < run; ++t, ++it) {
+                    const int a = it & 1;
+                    // blocks q0+t (x-1), q0+t+1 (x), q0+t+2 (x+1); the earlier item of the run waited for the first two
+                    for (int d = (t == 0 ? 0 : 2); d < 3 && ok; ++d) {
+                        const int q = q0 + t + d;
+                        ok = tc_wait(&full[q % NS], (q / NS) & 1, s_abort);
+                    }
+                    if (ok && it >= 2) ok = tc_wait(&accempty[a], ((it >> 1) & 1) ^ 1, s_abort);
+                    if (!ok) {
+                        *s_abort = 1;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t dcol = tmem + (uint32_t)((a * TC_SUB + j) * TC_N);
 #pragma unroll
-                    for (int j = 0; j < TC_SUB; ++j)
-                        tc_mma(tmem + (uint32_t)((a * TC_SUB + j) * TC_N),
-                               umma_desc(arow + (uint32_t)(j * TC_OUT) * 16u, c.rows_bytes, 128), bdesc, kTcIdesc,
-                               g > 0 ? 1u : 0u);
+                    for (int g = 0; g < 9; ++g) {
+                        const int b = g / 3, dyi = g % 3;
+                        const uint32_t arow = rbase + (uint32_t)((q0 + t + b) % NS) * c.block_bytes +
+                                              (uint32_t)(dyi * c.sy + j * TC_OUT) * 16u;
+                        tc_mma(dcol, umma_desc(arow, c.rows_bytes, 128), umma_desc(wbase + g * 1536, 768, 128),
+                               kTcIdesc, g > 0 ? 1u : 0u);
+                    }
+                    // x-1 is not read again in this run; after the run's last item neither are x and x+1
+                    tc_commit(&empty[(q0 + t) % NS]);
+                    if (t == run - 1) {
+                        tc_commit(&empty[(q0 + t + 1) % NS]);
+                        tc_commit(&empty[(q0 + t + 2) % NS]);
+                    }
+                    tc_commit(&accfull[a]);
                 }
-                tc_commit(&empty[s]);
-                tc_commit(&accfull[a]);
-                s_counts[2] = it + 1;
+                q0 += run + 2;
+                k = run_end;
             }
+            tc_commit(done);  // arrives once every MMA this thread issued has completed
         }
     } else {
-        const int quarter = warp & 3;        // TMEM lanes 32*quarter .. +31 belong to this warp
-        const int group = (warp - 2) >> 2;   // windows group, group + TC_EPI_GROUPS, ...
-        const int i = quarter * 32 + lane;   // row of the 128-row window
+        // --------------------------------- epilogue warps --------------------------------------------
+        const int quarter = warp & 3;                   // TMEM lanes 32*quarter .. +31 belong to this warp
+        const int group = (warp - TC_EPI_WARP0) >> 2;   // windows group, group + TC_EPI_GROUPS, ...
+        const int i = quarter * 32 + lane;              // row of the 128-row window
         const uint32_t usx = (uint32_t)c.sx, usy = (uint32_t)c.sy;
-        float* xg = xchg + group * (2 * 4 * 2 * 16);
+        float* xg = xchg + group * (2 * TC_WPG * 4 * 2 * 16);
         int it = 0;
         int xp = 0;  // exchange buffer parity
-        for (int64_t tile = blockIdx.x; tile < c.ntiles; tile += gridDim.x, ++it) {
+        for (int64_t k = k_begin; k < k_end; ++k, ++it) {
             const int a = it & 1;
+            const uint32_t xk = (uint32_t)(k % c.nx) + 1u;
+            // row of lane 0 of window 0: one row before the item's first output row
+            const uint32_t q0 = xk * usx + usy + (uint32_t)(k / c.nx) * (uint32_t)(TC_SUB * TC_OUT);
             int ok = 1;
             if (lane == 0) ok = tc_wait(&accfull[a], (it >> 1) & 1, s_abort) ? 1 : 0;
             ok = __shfl_sync(0xffffffffu, ok, 0);
@@ -275,91 +345,138 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
                 break;
             }
             tc_fence_after();
-#pragma unroll 1
-            for (int j = group; j < TC_SUB; j += TC_EPI_GROUPS) {
-                __syncwarp();
-                const uint32_t taddr = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)((a * TC_SUB + j) * TC_N);
-                float* xb = xg + xp * (4 * 2 * 16);
-                const int64_t p = c.p_begin + (tile * TC_SUB + j) * TC_OUT - 1 + i;
-                // voxel of row p (rows < 2^31: checked on the host)
-                const uint32_t up = (uint32_t)p;
-                const uint32_t xq = up / usx;
+            __syncwarp();
+            // this group's windows j = group + w * TC_EPI_GROUPS are drained together: all TMEM loads,
+            // one exchange of the quarter-boundary rows, one barrier, then the outputs
+            float* xb = xg + xp * (TC_WPG * 4 * 2 * 16);
+            uint32_t taddr[TC_WPG];
+            bool valid[TC_WPG];
+            uint32_t prow[TC_WPG];
+            int64_t vox[TC_WPG];
+#pragma unroll
+            for (int w = 0; w < TC_WPG; ++w) {
+                const int j = group + w * TC_EPI_GROUPS;
+                taddr[w] = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)((a * TC_SUB + j) * TC_N);
+                // voxel of row p (rows < 2^31: checked on the host); rows of the next x-slab belong to
+                // the next item of the column
+                const uint32_t up = q0 + (uint32_t)(j * TC_OUT + i);
+                const uint32_t xq = fastdiv(up, c.div_sx);
                 const uint32_t rem = up - xq * usx;
-                const uint32_t yq = rem / usy;
+                const uint32_t yq = fastdiv(rem, c.div_sy);
                 const uint32_t zq = rem - yq * usy;
-                const bool valid = i >= 1 && i <= TC_OUT && xq >= 1 && xq <= (uint32_t)c.nx && yq >= 1 &&
-                                   yq <= (uint32_t)c.ny && zq >= 1 && zq <= (uint32_t)c.nz;
-                if (LAST) {
-                    const float zm = tc_ld1(taddr), z0 = tc_ld1(taddr + 16), zp = tc_ld1(taddr + 32);
-                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                    if (lane == 31) xb[(quarter * 2 + 0) * 16] = zm;
-                    if (lane == 0) xb[(quarter * 2 + 1) * 16] = zp;
-                    epi_group_barrier(group);
-                    float lo = __shfl_up_sync(0xffffffffu, zm, 1);
-                    float hi = __shfl_down_sync(0xffffffffu, zp, 1);
-                    if (lane == 0 && quarter > 0) lo = xb[((quarter - 1) * 2 + 0) * 16];
-                    if (lane == 31 && quarter < 3) hi = xb[((quarter + 1) * 2 + 1) * 16];
-                    xp ^= 1;
-                    if (valid) {
-                        const int64_t vox = ((int64_t)(xq - 1) * c.ny + (yq - 1)) * (int64_t)c.nz + (zq - 1);
-                        float o = lo + z0 + hi;
-                        if (c.mask && c.mask[vox] != 0.f) o = 0.f;
-                        if (c.dinv) o += c.omega * c.dinv[vox] * c.r[vox];
-                        c.w[vox] = o;
+                prow[w] = up;
+                valid[w] = i >= 1 && i <= TC_OUT && xq == xk && yq - 1u < (uint32_t)c.ny && zq - 1u < (uint32_t)c.nz;
+                vox[w] = ((int64_t)(xq - 1) * c.ny + (yq - 1)) * (int64_t)c.nz + (zq - 1);
+            }
+            if (LAST) {
+                float zm[TC_WPG], z0[TC_WPG], zp[TC_WPG];
+#pragma unroll
+                for (int w = 0; w < TC_WPG; ++w) {
+                    zm[w] = tc_ld1(taddr[w]);
+                    z0[w] = tc_ld1(taddr[w] + 16);
+                    zp[w] = tc_ld1(taddr[w] + 32);
+                }
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int w = 0; w < TC_WPG; ++w) {
+                    if (lane == 31) xb[((w * 4 + quarter) * 2 + 0) * 16] = zm[w];
+                    if (lane == 0) xb[((w * 4 + quarter) * 2 + 1) * 16] = zp[w];
+                }
+                epi_group_barrier(group);
+#pragma unroll
+                for (int w = 0; w < TC_WPG; ++w) {
+                    float lo = __shfl_up_sync(0xffffffffu, zm[w], 1);
+                    float hi = __shfl_down_sync(0xffffffffu, zp[w], 1);
+                    if (lane == 0 && quarter > 0) lo = xb[((w * 4 + quarter - 1) * 2 + 0) * 16];
+                    if (lane == 31 && quarter < 3) hi = xb[((w * 4 + quarter + 1) * 2 + 1) * 16];
+                    if (valid[w]) {
+                        const int64_t v = vox[w];
+                        float o = lo + z0[w] + hi;
+                        if (c.mask && c.mask[v] != 0.f) o = 0.f;
+                        if (c.dinv) o += c.omega * c.dinv[v] * c.r[v];
+                        c.w[v] = o;
                     }
-                } else {
-                    float zm[16], z0[16], zp[16];
-                    tc_ld16(taddr, zm);
-                    tc_ld16(taddr + 16, z0);
-                    tc_ld16(taddr + 32, zp);
-                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                }
+            } else {
+                float zm[TC_WPG][16], z0[TC_WPG][16], zp[TC_WPG][16];
+#pragma unroll
+                for (int w = 0; w < TC_WPG; ++w) {
+                    tc_ld16(taddr[w], zm[w]);
+                    tc_ld16(taddr[w] + 16, z0[w]);
+                    tc_ld16(taddr[w] + 32, zp[w]);
+                }
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                for (int w = 0; w < TC_WPG; ++w) {
+                    float4* lo_dst = reinterpret_cast<float4*>(xb + ((w * 4 + quarter) * 2 + 0) * 16);
+                    float4* hi_dst = reinterpret_cast<float4*>(xb + ((w * 4 + quarter) * 2 + 1) * 16);
                     if (lane == 31) {
 #pragma unroll
-                        for (int k = 0; k < 16; ++k) xb[(quarter * 2 + 0) * 16 + k] = zm[k];
+                        for (int q = 0; q < 4; ++q)
+                            lo_dst[q] = make_float4(zm[w][4 * q], zm[w][4 * q + 1], zm[w][4 * q + 2], zm[w][4 * q + 3]);
                     }
                     if (lane == 0) {
 #pragma unroll
-                        for (int k = 0; k < 16; ++k) xb[(quarter * 2 + 1) * 16 + k] = zp[k];
+                        for (int q = 0; q < 4; ++q)
+                            hi_dst[q] = make_float4(zp[w][4 * q], zp[w][4 * q + 1], zp[w][4 * q + 2], zp[w][4 * q + 3]);
                     }
-                    epi_group_barrier(group);
-                    float o[16];
+                }
+                epi_group_barrier(group);
 #pragma unroll
-                    for (int k = 0; k < 16; ++k) {
-                        float lo = __shfl_up_sync(0xffffffffu, zm[k], 1);
-                        float hi = __shfl_down_sync(0xffffffffu, zp[k], 1);
-                        if (lane == 0 && quarter > 0) lo = xb[((quarter - 1) * 2 + 0) * 16 + k];
-                        if (lane == 31 && quarter < 3) hi = xb[((quarter + 1) * 2 + 1) * 16 + k];
-                        o[k] = fmaxf(lo + z0[k] + hi, 0.f);
+                for (int w = 0; w < TC_WPG; ++w) {
+                    float lo[16], hi[16];
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) {
+                        lo[q] = __shfl_up_sync(0xffffffffu, zm[w][q], 1);
+                        hi[q] = __shfl_down_sync(0xffffffffu, zp[w][q], 1);
                     }
-                    xp ^= 1;
-                    if (valid) {
+                    if (lane == 0 && quarter > 0) {
+                        const float4* src = reinterpret_cast<const float4*>(xb + ((w * 4 + quarter - 1) * 2 + 0) * 16);
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            const float4 v = src[q];
+                            lo[4 * q] = v.x; lo[4 * q + 1] = v.y; lo[4 * q + 2] = v.z; lo[4 * q + 3] = v.w;
+                        }
+                    }
+                    if (lane == 31 && quarter < 3) {
+                        const float4* src = reinterpret_cast<const float4*>(xb + ((w * 4 + quarter + 1) * 2 + 1) * 16);
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            const float4 v = src[q];
+                            hi[4 * q] = v.x; hi[4 * q + 1] = v.y; hi[4 * q + 2] = v.z; hi[4 * q + 3] = v.w;
+                        }
+                    }
+                    if (valid[w]) {
                         uint32_t pk[8];
 #pragma unroll
-                        for (int k = 0; k < 8; ++k) {
-                            const __nv_bfloat162 h2 = __floats2bfloat162_rn(o[2 * k], o[2 * k + 1]);
-                            pk[k] = *reinterpret_cast<const uint32_t*>(&h2);
+                        for (int q = 0; q < 8; ++q) {
+                            const __nv_bfloat162 h2 =
+                                __floats2bfloat162_rn(fmaxf(lo[2 * q] + z0[w][2 * q] + hi[2 * q], 0.f),
+                                                      fmaxf(lo[2 * q + 1] + z0[w][2 * q + 1] + hi[2 * q + 1], 0.f));
+                            pk[q] = *reinterpret_cast<const uint32_t*>(&h2);
                         }
+                        const int64_t p = prow[w];
                         *reinterpret_cast<uint4*>(c.out + p * 16) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
                         *reinterpret_cast<uint4*>(c.out + (c.plane_rows + p) * 16) =
                             make_uint4(pk[4], pk[5], pk[6], pk[7]);
                     }
                 }
             }
+            xp ^= 1;
             tc_fence_before();
             __syncwarp();
             if (lane == 0) mbar_arrive1(&accempty[a]);
         }
     }
 
-    // teardown: every copy landed and every MMA finished before shared memory and TMEM go away
+    // teardown: every MMA finished and every copy landed before shared memory and TMEM go away
     __syncthreads();
     if (threadIdx.x == 32) {
-        const int issued = s_counts[0], taken = s_counts[1], committed = s_counts[2];
-        bool ok = true;
-        for (int j = taken; j < issued; ++j)  // copies nobody consumed (abort path only)
-            ok = mbar_wait_bounded(&full[j % S], (j / S) & 1) && ok;
-        for (int j = committed > S ? committed - S : 0; j < committed; ++j)
-            ok = mbar_wait_bounded(&empty[j % S], (j / S) & 1) && ok;
+        bool ok = mbar_wait_bounded(done, 0);
+        const int issued = *s_issued;
+        // the last NS blocks occupy distinct slots; earlier fills of a slot were consumed before reuse
+        for (int q = issued > NS ? issued - NS : 0; q < issued; ++q)
+            ok = mbar_wait_bounded(&full[q % NS], (q / NS) & 1) && ok;
         if (!ok || *s_abort) atomicOr(c.status, GB_DEV_WAIT_TIMEOUT);
     }
     tc_fence_before();
@@ -374,6 +491,7 @@ __global__ void k_features_planar(int nx, int ny, int nz, int64_t plane_rows, co
                                   const float* __restrict__ dinv, const float* __restrict__ chat,
                                   const float* __restrict__ mask, unsigned char* __restrict__ out)
 {
+    pdl_enter();
     const int64_t n = (int64_t)nx * ny * nz;
     const int64_t sy = nz + 2, sx = (int64_t)(ny + 2) * sy;
     for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
@@ -418,9 +536,8 @@ GB_API int gb_net_features_planar(int nx, int ny, int nz, const float* r, const 
     if (n <= 0) return GB_OK;
     GB_REQUIRE((uintptr_t)out % 16 == 0, "net_features_planar: output must be 16-byte aligned");
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(n, 256), kSmCount * 16));
-    k_features_planar<<<grid, 256, 0, stream>>>(nx, ny, nz, planar_rows(nx, ny, nz), r, dinv, chat, mask,
-                                                 static_cast<unsigned char*>(out));
-    GB_CHECK_CUDA(cudaGetLastError());
+    GB_CHECK_CUDA(launch_pdl(k_features_planar, grid, 256, 0, stream, nx, ny, nz, planar_rows(nx, ny, nz), r, dinv,
+                             chat, mask, static_cast<unsigned char*>(out)));
     return GB_OK;
 }
 
@@ -442,22 +559,28 @@ GB_API int gb_conv3_fwd_tc(int nx, int ny, int nz, int last, const void* in, con
     c.nz = nz;
     c.sy = nz + 2;
     c.sx = (int64_t)(ny + 2) * (nz + 2);
-    c.p_begin = c.sx + c.sy + 1;
-    const int64_t p_last = (int64_t)nx * c.sx + (int64_t)ny * c.sy + nz;
-    c.ntiles = ceil_div<int64_t>(p_last - c.p_begin + 1, TC_SUB * TC_OUT);
+    c.div_sx = make_fastdiv((uint32_t)c.sx);
+    c.div_sy = make_fastdiv((uint32_t)c.sy);
+    // work items: columns of TC_SUB * TC_OUT rows covering an x-slab's interior rows (y = 1, z = 1 up
+    // to y = ny, z = nz), times the nx slabs
+    const int64_t span = (int64_t)(ny - 1) * c.sy + nz;
+    c.ncols = (int)ceil_div<int64_t>(span, TC_SUB * TC_OUT);
+    c.nitems = (int64_t)c.ncols * nx;
     c.plane_rows = planar_rows(nx, ny, nz);
     GB_REQUIRE(c.plane_rows < (int64_t(1) << 31), "conv3_fwd_tc: grid too large (padded rows must fit in 31 bits)");
     const int64_t rows = 2 * (int64_t)c.sy + TC_OUT * (TC_SUB - 1) + TC_M;
+    // the last block read (x = nx + 1, last column) must end inside the padded planes
+    GB_REQUIRE((int64_t)(nx + 1) * c.sx + (int64_t)(c.ncols - 1) * (TC_SUB * TC_OUT) + rows <= c.plane_rows,
+               "conv3_fwd_tc: planar padding too small");
     c.rows_bytes = (uint32_t)(rows * 16);
-    c.stage_bytes = 6 * c.rows_bytes;
+    c.block_bytes = 2 * c.rows_bytes;
     const size_t fixed = TC_W_BYTES + TC_XCHG_BYTES + 256;
-    c.stages = TC_MAX_STAGES;
-    while (c.stages > 2 && (size_t)c.stages * c.stage_bytes + fixed > 220 * 1024) --c.stages;
-    const size_t smem = (size_t)c.stages * c.stage_bytes + fixed;
-    if (smem > 220 * 1024) {
-        gb::set_error("conv3_fwd_tc: grid too long in z (nz = %d) for the staged tile", nz);
+    c.slots = (int)std::min<size_t>(TC_MAX_SLOTS, (TC_SMEM_LIMIT - fixed) / c.block_bytes);
+    if (c.slots < TC_MIN_SLOTS) {
+        gb::set_error("conv3_fwd_tc: grid too long in z (nz = %d) for the staged x-plane blocks", nz);
         return GB_ERR_UNSUPPORTED;
     }
+    const size_t smem = (size_t)c.slots * c.block_bytes + fixed;
     c.in = static_cast<const unsigned char*>(in);
     c.Wt = static_cast<const __nv_bfloat16*>(Wt);
     c.out = static_cast<unsigned char*>(out);
@@ -478,11 +601,10 @@ GB_API int gb_conv3_fwd_tc(int nx, int ny, int nz, int last, const void* in, con
         GB_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3_tc<false>, TC_THREADS, smem));
     }
     per_sm = 1;  // one CTA per SM: it holds all 512 TMEM columns
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(c.ntiles, (int64_t)sms * per_sm));
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(c.nitems, (int64_t)sms * per_sm));
     if (last)
-        k_conv3_tc<true><<<grid, TC_THREADS, smem, stream>>>(c);
+        GB_CHECK_CUDA(launch_pdl(k_conv3_tc<true>, grid, TC_THREADS, smem, stream, c));
     else
-        k_conv3_tc<false><<<grid, TC_THREADS, smem, stream>>>(c);
-    GB_CHECK_CUDA(cudaGetLastError());
+        GB_CHECK_CUDA(launch_pdl(k_conv3_tc<false>, grid, TC_THREADS, smem, stream, c));
     return GB_OK;
 }

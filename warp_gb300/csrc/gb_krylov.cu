@@ -119,6 +119,7 @@ template <int BR, typename VT>
 __global__ __launch_bounds__(SPMV_THREADS) void k_cg_init(const SolveArgs* __restrict__ args, int nrow, SpmvShape sh,
                                                           cudaGraphConditionalHandle h, int has_cond)
 {
+    pdl_enter();
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ double s_red[32 * 3];
     const SolveArgs a = *args;
@@ -152,6 +153,7 @@ template <int BR, typename AT> struct EpiCgAp {
 template <int BR, typename VT>
 __global__ __launch_bounds__(SPMV_THREADS) void k_cg_spmv(const SolveArgs* __restrict__ args, int nrow, SpmvShape sh)
 {
+    pdl_enter();
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ double s_red[32];
     const SolveArgs a = *args;
@@ -179,6 +181,7 @@ __global__ __launch_bounds__(SPMV_THREADS) void k_cg_spmv(const SolveArgs* __res
 __global__ __launch_bounds__(VEC_THREADS) void k_cg_update(const SolveArgs* __restrict__ args,
                                                            cudaGraphConditionalHandle h, int has_cond)
 {
+    pdl_enter();
     __shared__ double s_red[32 * 2];
     const SolveArgs a = *args;
     KrylovScalars* S = a.S;
@@ -258,6 +261,7 @@ __global__ __launch_bounds__(VEC_THREADS) void k_cg_update(const SolveArgs* __re
 // p = D^-1 r + beta p
 __global__ __launch_bounds__(VEC_THREADS) void k_cg_pupdate(const SolveArgs* __restrict__ args)
 {
+    pdl_enter();
     const SolveArgs a = *args;
     KrylovScalars* S = a.S;
     if (!S->cond) return;
@@ -318,6 +322,7 @@ template <int BR, typename VT>
 __global__ __launch_bounds__(SPMV_THREADS) void k_bi_init(const SolveArgs* __restrict__ args, int nrow, SpmvShape sh,
                                                           cudaGraphConditionalHandle h, int has_cond)
 {
+    pdl_enter();
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ double s_red[32 * 2];
     const SolveArgs a = *args;
@@ -367,6 +372,7 @@ template <int BR, typename VT>
 __global__ __launch_bounds__(SPMV_THREADS) void k_bi_spmv_v(const SolveArgs* __restrict__ args, int nrow,
                                                             SpmvShape sh)
 {
+    pdl_enter();
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ double s_red[32];
     const SolveArgs a = *args;
@@ -393,6 +399,7 @@ __global__ __launch_bounds__(SPMV_THREADS) void k_bi_spmv_v(const SolveArgs* __r
 // x += alpha y; r -= alpha v; z = M r; rr
 __global__ __launch_bounds__(VEC_THREADS) void k_bi_update1(const SolveArgs* __restrict__ args)
 {
+    pdl_enter();
     __shared__ double s_red[32];
     const SolveArgs a = *args;
     KrylovScalars* S = a.S;
@@ -439,6 +446,7 @@ template <int BR, typename VT>
 __global__ __launch_bounds__(SPMV_THREADS) void k_bi_spmv_t(const SolveArgs* __restrict__ args, int nrow,
                                                             SpmvShape sh)
 {
+    pdl_enter();
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ double s_red[32 * 2];
     const SolveArgs a = *args;
@@ -467,6 +475,7 @@ __global__ __launch_bounds__(SPMV_THREADS) void k_bi_spmv_t(const SolveArgs* __r
 __global__ __launch_bounds__(VEC_THREADS) void k_bi_update2(const SolveArgs* __restrict__ args,
                                                             cudaGraphConditionalHandle h, int has_cond)
 {
+    pdl_enter();
     __shared__ double s_red[32 * 2];
     const SolveArgs a = *args;
     KrylovScalars* S = a.S;
@@ -510,6 +519,7 @@ __global__ __launch_bounds__(VEC_THREADS) void k_bi_update2(const SolveArgs* __r
 // p = r + beta p - beta_omega v ; y = M p
 __global__ __launch_bounds__(VEC_THREADS) void k_bi_pupdate(const SolveArgs* __restrict__ args)
 {
+    pdl_enter();
     const SolveArgs a = *args;
     KrylovScalars* S = a.S;
     if (!S->cond) return;
@@ -530,6 +540,7 @@ __global__ __launch_bounds__(VEC_THREADS) void k_bi_pupdate(const SolveArgs* __r
 __global__ __launch_bounds__(VEC_THREADS) void k_fcg_dir(const SolveArgs* __restrict__ args,
                                                          cudaGraphConditionalHandle h, int has_cond)
 {
+    pdl_enter();
     __shared__ double s_red[32 * 2];
     const SolveArgs a = *args;
     KrylovScalars* S = a.S;
@@ -558,6 +569,7 @@ __global__ __launch_bounds__(VEC_THREADS) void k_fcg_dir(const SolveArgs* __rest
 
 __global__ __launch_bounds__(VEC_THREADS) void k_fcg_p(const SolveArgs* __restrict__ args)
 {
+    pdl_enter();
     const SolveArgs a = *args;
     KrylovScalars* S = a.S;
     if (!S->cond) return;
@@ -630,9 +642,9 @@ template <int BR, typename VT>
 static int launch_init_t(Solver* s, cudaStream_t st, cudaGraphConditionalHandle h, int has_cond)
 {
     if (s->kind == KRYLOV_CG || s->kind == KRYLOV_FCG)
-        k_cg_init<BR, VT><<<s->spmv_grid, SPMV_THREADS, s->spmv_smem, st>>>(s->d_args, s->nrow, s->sh, h, has_cond);
+        GB_CHECK_CUDA(launch_pdl(k_cg_init<BR, VT>, s->spmv_grid, SPMV_THREADS, s->spmv_smem, st, s->d_args, s->nrow, s->sh, h, has_cond));
     else
-        k_bi_init<BR, VT><<<s->spmv_grid, SPMV_THREADS, s->spmv_smem, st>>>(s->d_args, s->nrow, s->sh, h, has_cond);
+        GB_CHECK_CUDA(launch_pdl(k_bi_init<BR, VT>, s->spmv_grid, SPMV_THREADS, s->spmv_smem, st, s->d_args, s->nrow, s->sh, h, has_cond));
     GB_CHECK_CUDA(cudaGetLastError());
     return GB_OK;
 }
@@ -649,20 +661,20 @@ static int launch_iter_t(Solver* s, cudaStream_t st, cudaGraphConditionalHandle 
             gb::set_error("flexible solver: preconditioner callback failed");
             return GB_ERR_INVALID;
         }
-        k_fcg_dir<<<s->vec_grid, VEC_THREADS, 0, st>>>(s->d_args, h, has_cond);
-        k_fcg_p<<<s->vec_grid, VEC_THREADS, 0, st>>>(s->d_args);
-        k_cg_spmv<BR, VT><<<s->spmv_grid, SPMV_THREADS, s->spmv_smem, st>>>(s->d_args, s->nrow, s->sh);
-        k_cg_update<<<s->vec_grid, VEC_THREADS, 0, st>>>(s->d_args, h, has_cond);
+        GB_CHECK_CUDA(launch_pdl(k_fcg_dir, s->vec_grid, VEC_THREADS, 0, st, s->d_args, h, has_cond));
+        GB_CHECK_CUDA(launch_pdl(k_fcg_p, s->vec_grid, VEC_THREADS, 0, st, s->d_args));
+        GB_CHECK_CUDA(launch_pdl(k_cg_spmv<BR, VT>, s->spmv_grid, SPMV_THREADS, s->spmv_smem, st, s->d_args, s->nrow, s->sh));
+        GB_CHECK_CUDA(launch_pdl(k_cg_update, s->vec_grid, VEC_THREADS, 0, st, s->d_args, h, has_cond));
     } else if (s->kind == KRYLOV_CG) {
-        k_cg_spmv<BR, VT><<<s->spmv_grid, SPMV_THREADS, s->spmv_smem, st>>>(s->d_args, s->nrow, s->sh);
-        k_cg_update<<<s->vec_grid, VEC_THREADS, 0, st>>>(s->d_args, h, has_cond);
-        k_cg_pupdate<<<s->vec_grid, VEC_THREADS, 0, st>>>(s->d_args);
+        GB_CHECK_CUDA(launch_pdl(k_cg_spmv<BR, VT>, s->spmv_grid, SPMV_THREADS, s->spmv_smem, st, s->d_args, s->nrow, s->sh));
+        GB_CHECK_CUDA(launch_pdl(k_cg_update, s->vec_grid, VEC_THREADS, 0, st, s->d_args, h, has_cond));
+        GB_CHECK_CUDA(launch_pdl(k_cg_pupdate, s->vec_grid, VEC_THREADS, 0, st, s->d_args));
     } else {
-        k_bi_spmv_v<BR, VT><<<s->spmv_grid, SPMV_THREADS, s->spmv_smem, st>>>(s->d_args, s->nrow, s->sh);
-        k_bi_update1<<<s->vec_grid, VEC_THREADS, 0, st>>>(s->d_args);
-        k_bi_spmv_t<BR, VT><<<s->spmv_grid, SPMV_THREADS, s->spmv_smem, st>>>(s->d_args, s->nrow, s->sh);
-        k_bi_update2<<<s->vec_grid, VEC_THREADS, 0, st>>>(s->d_args, h, has_cond);
-        k_bi_pupdate<<<s->vec_grid, VEC_THREADS, 0, st>>>(s->d_args);
+        GB_CHECK_CUDA(launch_pdl(k_bi_spmv_v<BR, VT>, s->spmv_grid, SPMV_THREADS, s->spmv_smem, st, s->d_args, s->nrow, s->sh));
+        GB_CHECK_CUDA(launch_pdl(k_bi_update1, s->vec_grid, VEC_THREADS, 0, st, s->d_args));
+        GB_CHECK_CUDA(launch_pdl(k_bi_spmv_t<BR, VT>, s->spmv_grid, SPMV_THREADS, s->spmv_smem, st, s->d_args, s->nrow, s->sh));
+        GB_CHECK_CUDA(launch_pdl(k_bi_update2, s->vec_grid, VEC_THREADS, 0, st, s->d_args, h, has_cond));
+        GB_CHECK_CUDA(launch_pdl(k_bi_pupdate, s->vec_grid, VEC_THREADS, 0, st, s->d_args));
     }
     GB_CHECK_CUDA(cudaGetLastError());
     return GB_OK;

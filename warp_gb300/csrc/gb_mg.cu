@@ -26,6 +26,7 @@ __device__ __forceinline__ int64_t nidx(const NodeGrid& g, int x, int y, int z)
 __global__ void k_restrict_fw(NodeGrid fg, NodeGrid cg, const float* __restrict__ r, const float* __restrict__ fmask,
                               const float* __restrict__ cmask, float* __restrict__ rc)
 {
+    pdl_enter();
     const int64_t n = (int64_t)cg.nx * cg.ny * cg.nz;
     const int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (I >= n) return;
@@ -61,6 +62,7 @@ __global__ void k_restrict_fw(NodeGrid fg, NodeGrid cg, const float* __restrict_
 __global__ void k_prolong_add(NodeGrid fg, NodeGrid cg, const float* __restrict__ zc, const float* __restrict__ fmask,
                               float scale, float* __restrict__ z)
 {
+    pdl_enter();
     const int64_t n = (int64_t)fg.nx * fg.ny * fg.nz;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -83,6 +85,7 @@ __global__ void k_prolong_add(NodeGrid fg, NodeGrid cg, const float* __restrict_
 __global__ void k_jacobi0(int64_t n, float omega, const float* __restrict__ dinv, const float* __restrict__ r,
                           float* __restrict__ z)
 {
+    pdl_enter();
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         z[i] = omega * dinv[i] * r[i];
 }
@@ -118,8 +121,7 @@ GB_API int gb_mg_restrict(int fnx, int fny, int fnz, int cnx, int cny, int cnz, 
 {
     GB_REQUIRE(cnx == (fnx + 1) / 2 && cny == (fny + 1) / 2 && cnz == (fnz + 1) / 2, "mg_restrict: grid mismatch");
     NodeGrid fg{fnx, fny, fnz}, cg{cnx, cny, cnz};
-    k_restrict_fw<<<grid1((int64_t)cnx * cny * cnz), 256, 0, stream>>>(fg, cg, r, fmask, cmask, rc);
-    GB_CHECK_CUDA(cudaGetLastError());
+    GB_CHECK_CUDA(launch_pdl(k_restrict_fw, grid1((int64_t)cnx * cny * cnz), 256, 0, stream, fg, cg, r, fmask, cmask, rc));
     return GB_OK;
 }
 
@@ -128,16 +130,14 @@ GB_API int gb_mg_prolong_add(int fnx, int fny, int fnz, int cnx, int cny, int cn
 {
     GB_REQUIRE(cnx == (fnx + 1) / 2 && cny == (fny + 1) / 2 && cnz == (fnz + 1) / 2, "mg_prolong: grid mismatch");
     NodeGrid fg{fnx, fny, fnz}, cg{cnx, cny, cnz};
-    k_prolong_add<<<grid1((int64_t)fnx * fny * fnz), 256, 0, stream>>>(fg, cg, zc, fmask, scale, z);
-    GB_CHECK_CUDA(cudaGetLastError());
+    GB_CHECK_CUDA(launch_pdl(k_prolong_add, grid1((int64_t)fnx * fny * fnz), 256, 0, stream, fg, cg, zc, fmask, scale, z));
     return GB_OK;
 }
 
 GB_API int gb_mg_jacobi0(int64_t n, float omega, const float* dinv, const float* r, float* z, cudaStream_t stream)
 {
     if (n <= 0) return GB_OK;
-    k_jacobi0<<<(int)std::min<int64_t>(grid1(n), kSmCount * 8), 256, 0, stream>>>(n, omega, dinv, r, z);
-    GB_CHECK_CUDA(cudaGetLastError());
+    GB_CHECK_CUDA(launch_pdl(k_jacobi0, (int)std::min<int64_t>(grid1(n), kSmCount * 8), 256, 0, stream, n, omega, dinv, r, z));
     return GB_OK;
 }
 

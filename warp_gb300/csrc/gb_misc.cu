@@ -78,6 +78,7 @@ template <typename T>
 __global__ void k_dense_mv(int m, int n, const T* __restrict__ A, const T* __restrict__ x, const T* y, T* z, T alpha,
                            T beta)
 {
+    pdl_enter();
     const int row = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
     const int lane = threadIdx.x & 31;
     if (row >= m) return;
@@ -197,11 +198,11 @@ GB_API int gb_dense_mv(int dtype, int m, int n, const void* A, const void* x, co
     if (m <= 0) return GB_OK;
     const int grid = ceil_div(m, 8);
     if (dtype == GB_F32)
-        k_dense_mv<float><<<grid, 256, 0, stream>>>(m, n, (const float*)A, (const float*)x, (const float*)y,
-                                                   (float*)z, (float)alpha, (float)beta);
+        GB_CHECK_CUDA(launch_pdl(k_dense_mv<float>, grid, 256, 0, stream, m, n, (const float*)A, (const float*)x,
+                                 (const float*)y, (float*)z, (float)alpha, (float)beta));
     else if (dtype == GB_F64)
-        k_dense_mv<double><<<grid, 256, 0, stream>>>(m, n, (const double*)A, (const double*)x, (const double*)y,
-                                                    (double*)z, alpha, beta);
+        GB_CHECK_CUDA(launch_pdl(k_dense_mv<double>, grid, 256, 0, stream, m, n, (const double*)A, (const double*)x,
+                                 (const double*)y, (double*)z, alpha, beta));
     else {
         gb::set_error("dense_mv: unsupported dtype");
         return GB_ERR_UNSUPPORTED;

@@ -32,6 +32,7 @@ __global__ __launch_bounds__(SPMV_THREADS) void k_bsr_mv(int nrow, SpmvShape sh,
                                                          const XT* y_in, XT* y_out, AT alpha, AT beta, int* status)
 {
     extern __shared__ __align__(16) unsigned char smem[];
+    pdl_enter();
     EpiAxpby<BR, XT, AT> epi{y_out, y_in, alpha, beta};
     spmv_run<BR, BC, VT, XT, AT>(nrow, sh, offsets, row_counts, columns, values, x, smem, status, epi);
 }
@@ -58,6 +59,7 @@ __global__ __launch_bounds__(SPMV_THREADS) void k_bsr_smooth(int nrow, SpmvShape
                                                              float* z_out, int* status)
 {
     extern __shared__ __align__(16) unsigned char smem[];
+    pdl_enter();
     EpiSmooth<BR> epi{z, r, dinv, omega, z_out};
     spmv_run<BR, BR, VT, float, float>(nrow, sh, offsets, nullptr, columns, values, z, smem, status, epi);
 }
@@ -120,9 +122,8 @@ static int launch_mv(int nrow, SpmvShape sh, const int* offsets, const int* row_
     finalize_shape(sh, nrow, smem, offsets);
     auto kern = k_bsr_mv<BR, BC, VT, XT, AT>;
     if (smem > 48 * 1024) GB_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<sh.grid, SPMV_THREADS, smem, stream>>>(nrow, sh, offsets, row_counts, columns, (const VT*)values,
-                                               (const XT*)x, (const XT*)y_in, (XT*)y_out, (AT)alpha, (AT)beta, status);
-    GB_CHECK_CUDA(cudaGetLastError());
+    GB_CHECK_CUDA(launch_pdl(kern, sh.grid, SPMV_THREADS, smem, stream, nrow, sh, offsets, row_counts, columns,
+                             (const VT*)values, (const XT*)x, (const XT*)y_in, (XT*)y_out, (AT)alpha, (AT)beta, status));
     return GB_OK;
 }
 
@@ -333,13 +334,13 @@ GB_API int gb_bsr_jacobi_smooth(int bdim, int nrow, int64_t nnz, int64_t ncap, c
     if (bdim == 1) {
         if (smem > 48 * 1024)
             GB_CHECK_CUDA(cudaFuncSetAttribute(k_bsr_smooth<1, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_bsr_smooth<1, float><<<sh.grid, SPMV_THREADS, smem, stream>>>(nrow, sh, offsets, columns, values, z, r, dinv,
-                                                                      omega, z_out, status);
+        GB_CHECK_CUDA(launch_pdl(k_bsr_smooth<1, float>, sh.grid, SPMV_THREADS, smem, stream, nrow, sh, offsets,
+                                 columns, values, z, r, dinv, omega, z_out, status));
     } else {
         if (smem > 48 * 1024)
             GB_CHECK_CUDA(cudaFuncSetAttribute(k_bsr_smooth<3, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_bsr_smooth<3, float><<<sh.grid, SPMV_THREADS, smem, stream>>>(nrow, sh, offsets, columns, values, z, r, dinv,
-                                                                      omega, z_out, status);
+        GB_CHECK_CUDA(launch_pdl(k_bsr_smooth<3, float>, sh.grid, SPMV_THREADS, smem, stream, nrow, sh, offsets,
+                                 columns, values, z, r, dinv, omega, z_out, status));
     }
     GB_CHECK_CUDA(cudaGetLastError());
     return GB_OK;
