@@ -198,6 +198,16 @@ int gb_mg_prolong_add(int fnx, int fny, int fnz, int cnx, int cny, int cnz, cons
                       float scale, float* z, gb_stream_t stream);
 int gb_mg_jacobi0(int64_t n, float omega, const float* dinv, const float* r, float* z, gb_stream_t stream);
 int gb_mg_coarsen_cells(int fx, int fy, int fz, const float* a, float* ac, gb_stream_t stream);
+/* 27-point stencil form of a multigrid level's operator (no reference counterpart): node-major
+ * coefficients S[i][k], k = 9(dx+1) + 3(dy+1) + (dz+1), i = (x*ny + y)*nz + z (gb_st27_bytes, 16-byte
+ * aligned), built from a compact 1x1 fp32 CSR matrix (status bit 1: an entry outside the
+ * 27-neighbourhood).  gb_st27_apply mode 0: out = r - A w;  mode 1: w_out = omega D^-1 r,
+ * out = r - A w_out;  mode 2: out = w + omega D^-1 (r - A w); status: GB_DEV_WAIT_TIMEOUT. */
+size_t gb_st27_bytes(int nx, int ny, int nz);
+int gb_st27_build(int nx, int ny, int nz, const int* offsets, const int* columns, const float* values, float* S,
+                  int* status, gb_stream_t stream);
+int gb_st27_apply(int mode, int nx, int ny, int nz, const float* S, const float* w, const float* r, const float* dinv,
+                  float omega, float* w_out, float* out, int* status, gb_stream_t stream);
 /* 3x3x3 convolutions on a node grid, channels-last activations act[v][C], v = (x*ny + y)*nz + z,
  * weights W[t][ci][co] (t = 9(dx+1) + 3(dy+1) + (dz+1)), zero padding.  fp32 training kernels
  * (gb_conv3_bwd_weight_f32 accumulates into gW, deterministic), Adam, and the bf16 tensor-core

@@ -1,0 +1,150 @@
+"""GPU tests of the 27-point stencil form of the multigrid level operators (gb_st27_build /
+gb_st27_apply): every mode against a float64 product of the same CSR matrix, the out-of-stencil
+flag, and the V-cycle / flexible-CG solve against the CSR kernels."""
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _system(dims_cells, seed):
+    from warp_gb300 import problems
+
+    return problems.diffusion(dims_cells, sigma=1.5, corr_length=0.2, seed=seed)
+
+
+def _csr(Am):
+    n = Am.nrow
+    nnz = Am.nnz_sync()
+    off = Am.offsets.cpu().numpy().astype(np.int64)
+    col = Am.columns[:nnz].cpu().numpy().astype(np.int64)
+    val = Am.values[:nnz].cpu().numpy().astype(np.float64)
+    return n, off, col, val
+
+
+def _matvec(off, col, val, x):
+    y = np.zeros(len(off) - 1)
+    rows = np.repeat(np.arange(len(off) - 1), np.diff(off))
+    np.add.at(y, rows, val * x[col])
+    return y
+
+
+@pytest.mark.parametrize("cells", [(6, 5, 4), (9, 7, 12), (1, 3, 2)])
+def test_st27_modes_match_csr_product(cuda, cells):
+    from warp_gb300 import _native as N
+
+    s = _system(cells, seed=3)
+    dims = tuple(c + 1 for c in cells)
+    n, off, col, val = _csr(s.A)
+    assert n == int(np.prod(dims))
+    L = N.lib()
+    S = torch.empty(int(L.gb_st27_bytes(*dims)) // 4, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    N.check(L.gb_st27_build(*dims, s.A.offsets.data_ptr(), s.A.columns.data_ptr(), s.A.values.data_ptr(),
+                            S.data_ptr(), status.data_ptr(), 0))
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    rng = np.random.default_rng(1)
+    r = rng.standard_normal(n).astype(np.float32)
+    w = rng.standard_normal(n).astype(np.float32)
+    d = np.zeros(n)
+    rows = np.repeat(np.arange(n), np.diff(off))
+    d[rows[col == rows]] = val[col == rows]
+    dinv = (1.0 / d).astype(np.float32)
+    omega = 0.6
+    rt, wt, dt = (torch.from_numpy(a).cuda() for a in (r, w, dinv))
+    out = torch.empty_like(rt)
+    w_out = torch.empty_like(rt)
+    scale = np.abs(val).max() * np.abs(w).max() * 27
+    # mode 0: r - A w
+    st = status.data_ptr()
+    N.check(L.gb_st27_apply(0, *dims, S.data_ptr(), wt.data_ptr(), rt.data_ptr(), None, omega, None, out.data_ptr(), st,
+                            0))
+    ref = r - _matvec(off, col, val, w.astype(np.float64))
+    np.testing.assert_allclose(out.cpu().numpy(), ref, atol=1e-5 * scale, rtol=1e-5)
+    # mode 1: w = omega D^-1 r, r - A w
+    N.check(L.gb_st27_apply(1, *dims, S.data_ptr(), None, rt.data_ptr(), dt.data_ptr(), omega, w_out.data_ptr(),
+                            out.data_ptr(), st, 0))
+    w1 = omega * dinv.astype(np.float64) * r
+    np.testing.assert_allclose(w_out.cpu().numpy(), w1, rtol=1e-6, atol=1e-7)
+    ref = r - _matvec(off, col, val, w1)
+    np.testing.assert_allclose(out.cpu().numpy(), ref, atol=1e-5 * scale, rtol=1e-5)
+    # mode 2: w + omega D^-1 (r - A w)
+    N.check(L.gb_st27_apply(2, *dims, S.data_ptr(), wt.data_ptr(), rt.data_ptr(), dt.data_ptr(), omega, None,
+                            out.data_ptr(), st, 0))
+    ref = w + omega * dinv * (r - _matvec(off, col, val, w.astype(np.float64)))
+    np.testing.assert_allclose(out.cpu().numpy(), ref, atol=1e-5 * scale * np.abs(dinv).max(), rtol=1e-5)
+    assert int(status.item()) == 0
+
+
+def test_st27_build_flags_entries_outside_the_stencil(cuda):
+    from warp_gb300 import _native as N
+    from warp_gb300 import sparse
+
+    dims = (4, 4, 4)
+    n = 64
+    rows = np.concatenate([np.arange(n), [5]]).astype(np.int32)
+    cols = np.concatenate([np.arange(n), [5 + 2 * 16]]).astype(np.int32)  # two x-slabs away
+    vals = np.ones(n + 1, np.float32)
+    Am = sparse.bsr_zeros(n, n, torch.float32)
+    sparse.bsr_set_from_triplets(Am, torch.from_numpy(rows).cuda(), torch.from_numpy(cols).cuda(),
+                                 torch.from_numpy(vals).cuda())
+    L = N.lib()
+    S = torch.empty(int(L.gb_st27_bytes(*dims)) // 4, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    N.check(L.gb_st27_build(*dims, Am.offsets.data_ptr(), Am.columns.data_ptr(), Am.values.data_ptr(), S.data_ptr(),
+                            status.data_ptr(), 0))
+    torch.cuda.synchronize()
+    assert int(status.item()) == 1
+
+
+def test_st27_rejects_aliasing_and_bad_mode(cuda):
+    from warp_gb300 import _native as N
+
+    L = N.lib()
+    x = torch.zeros(27 * 8, device="cuda")
+    v = torch.zeros(8, device="cuda")
+    o = torch.zeros(8, device="cuda")
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    assert L.gb_st27_apply(0, 2, 2, 2, x.data_ptr(), v.data_ptr(), v.data_ptr(), None, 0.6, None, v.data_ptr(),
+                           st.data_ptr(), 0) != 0
+    assert L.gb_st27_apply(7, 2, 2, 2, x.data_ptr(), v.data_ptr(), v.data_ptr(), v.data_ptr(), 0.6, None, o.data_ptr(),
+                           st.data_ptr(), 0) != 0
+
+
+@pytest.mark.parametrize("learned_smoother", [False, True])
+def test_vcycle_and_fcg_stencil_match_csr(cuda, learned_smoother):
+    """The stencil V-cycle equals the CSR one up to fp32 summation order, and the flexible-CG solve
+    converges in the same number of iterations (within one)."""
+    import os
+
+    from warp_gb300 import learned, multigrid
+    from warp_gb300.optim import linear
+
+    s = _system((16, 16, 16), seed=7)
+    mgs = {}
+    for st in (False, True):
+        mg = multigrid.MultigridPreconditioner(s.A, s.geo, s.coef, stencil=st)
+        if learned_smoother:
+            w = os.path.join(os.path.dirname(__file__), "..", "warp_gb300", "data", "smoother_q1_diffusion.npz")
+            mg.smoother = learned.LearnedSmoother(learned.ConvNet.load(w), mg, s.coef)
+        mgs[st] = mg
+    assert all(lv.S is not None for lv in mgs[True].levels[:-1])
+    assert mgs[True].kernels_per_apply < mgs[False].kernels_per_apply
+    r = torch.randn(s.A.nrow, device="cuda", generator=torch.Generator("cuda").manual_seed(2))
+    r = r * (1 - mgs[True].levels[0].mask)
+    z_csr = mgs[False].apply(r)
+    z_st = mgs[True].apply(r)
+    torch.cuda.synchronize()
+    assert int(mgs[True].status.item()) == 0
+    err = float((z_st - z_csr).abs().max()) / float(z_csr.abs().max())
+    assert err < 1e-4, err
+    its = {}
+    for st, mg in mgs.items():
+        x = torch.zeros_like(s.b)
+        it, res, atol = linear.fcg(s.A, s.b, x, tol=1e-6, atol=0.0, maxiter=200, M=mg, check_every=1)
+        assert res <= atol
+        its[st] = it
+    assert abs(its[True] - its[False]) <= 1, its

@@ -75,6 +75,9 @@ _SIGNATURES = {
     "gb_mg_restrict": (_c_int, [_c_int] * 6 + [_vp, _vp, _vp, _vp, _vp]),
     "gb_mg_prolong_add": (_c_int, [_c_int] * 6 + [_vp, _vp, ctypes.c_float, _vp, _vp]),
     "gb_mg_jacobi0": (_c_int, [_c_i64, ctypes.c_float, _vp, _vp, _vp, _vp]),
+    "gb_st27_bytes": (_c_sz, [_c_int, _c_int, _c_int]),
+    "gb_st27_build": (_c_int, [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "gb_st27_apply": (_c_int, [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, ctypes.c_float, _vp, _vp, _vp, _vp]),
     "gb_mg_coarsen_cells": (_c_int, [_c_int, _c_int, _c_int, _vp, _vp, _vp]),
     "gb_bsr_get_diag": (_c_int, [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gb_bsr_inverse_diagonal": (_c_int, [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_int, _vp, _vp]),

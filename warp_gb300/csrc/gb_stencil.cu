@@ -1,0 +1,229 @@
+// gb_stencil.cu -- 27-point stencil form of the multigrid levels' operators.
+//
+// No reference counterpart: Warp's solvers apply CSR/BSR matrices only.  The multigrid levels of
+// the flexible-CG preconditioner are Q1 operators on structured node grids, so every row has at most
+// the 27 neighbours (dx, dy, dz) in {-1, 0, 1}^3 of its node.  Storing the coefficients node-major,
+//     S[i][k],  k = (dx+1)*9 + (dy+1)*3 + (dz+1),  node i = (x*ny + y)*nz + z
+// (n rounded up to a multiple of 4 nodes, so every tile is a multiple of 16 bytes) drops the column
+// indices and row offsets of the CSR form: a smoothing or residual pass reads 108 bytes of
+// coefficients per row plus the vectors, against 27*8 + 4 for CSR.  Coefficients that the CSR row
+// does not hold are stored as zero, so the product is the CSR product (summed in tap order).
+// Neighbours outside the grid are skipped.
+//
+// The apply kernel is persistent: per 256-node tile one thread issues a 1-D bulk copy of the tile's
+// 27.6 KB of coefficients into a 3-stage shared-memory ring (one contiguous stream per CTA, as the
+// CSR kernel's staging); each thread reads its node's 27 coefficients from shared memory (word
+// stride 27, odd: no bank conflicts) and its neighbours' vector entries through the read-only path.
+// (A planar S[k][i] layout read with 27 plain loads per thread ran 1.5-2x slower than the CSR kernel:
+// 27 concurrent streams per warp.)
+//
+// Kernels:
+//   gb_st27_build  CSR (1x1 fp32, compact) -> S; an entry outside the 27-neighbourhood sets
+//                  status bit 1 (the caller keeps the CSR form then)
+//   gb_st27_apply  mode 0: t = r - A w
+//                  mode 1: w = omega D^-1 r (written), t = r - A w   (first Jacobi step + residual)
+//                  mode 2: z = w + omega D^-1 (r - A w)               (Jacobi step fused with residual)
+#include "gb_bulk.cuh"
+#include "gb_common.cuh"
+
+namespace gb {
+
+struct St27Grid {
+    int nx, ny, nz;
+    int64_t n;
+};
+
+// node -> (x, y, z); node counts are below 2^31 (checked on the host), so 32-bit division suffices
+__device__ __forceinline__ void st27_coords(const St27Grid& g, int64_t i, int& x, int& y, int& z)
+{
+    const uint32_t ui = (uint32_t)i, yz = (uint32_t)g.ny * (uint32_t)g.nz;
+    const uint32_t ux = ui / yz, rem = ui - ux * yz;
+    const uint32_t uy = rem / (uint32_t)g.nz;
+    x = (int)ux;
+    y = (int)uy;
+    z = (int)(rem - uy * (uint32_t)g.nz);
+}
+
+__global__ void k_st27_build(St27Grid g, const int* __restrict__ offsets, const int* __restrict__ columns,
+                             const float* __restrict__ values, float* __restrict__ S, int* status)
+{
+    pdl_enter();
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < g.n; i += stride) {
+        int x, y, z;
+        st27_coords(g, i, x, y, z);
+        float s[27];
+#pragma unroll
+        for (int k = 0; k < 27; ++k) s[k] = 0.f;
+        bool bad = false;
+        for (int e = offsets[i]; e < offsets[i + 1]; ++e) {
+            int cx, cy, cz;
+            st27_coords(g, columns[e], cx, cy, cz);
+            const int dx = cx - x, dy = cy - y, dz = cz - z;
+            if (dx < -1 || dx > 1 || dy < -1 || dy > 1 || dz < -1 || dz > 1 || columns[e] < 0 ||
+                (int64_t)columns[e] >= g.n) {
+                bad = true;
+                continue;
+            }
+            const int k = (dx + 1) * 9 + (dy + 1) * 3 + (dz + 1);
+            // a compact row holds each column once; a repeated one would be summed by the CSR product
+#pragma unroll
+            for (int q = 0; q < 27; ++q)
+                if (q == k) s[q] += values[e];
+        }
+        if (bad) atomicOr(status, 1);
+#pragma unroll
+        for (int k = 0; k < 27; ++k) S[i * 27 + k] = s[k];
+    }
+}
+
+constexpr int ST_TILE = 256;    // nodes per tile = threads per CTA
+constexpr int ST_STAGES = 3;
+constexpr size_t ST_STAGE_BYTES = (size_t)ST_TILE * 27 * sizeof(float);
+constexpr size_t ST_SMEM = ST_STAGES * ST_STAGE_BYTES + 64;
+
+__host__ __device__ inline int64_t st27_padded_nodes(int64_t n) { return (n + 3) / 4 * 4; }
+
+template <int MODE>
+__global__ void __launch_bounds__(ST_TILE) k_st27_apply(St27Grid g, const float* __restrict__ S, const float* w,
+                                                         const float* __restrict__ r, const float* __restrict__ dinv,
+                                                         float omega, float* w_out, float* out, int* status)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    pdl_enter();
+    float* ring = reinterpret_cast<float*>(smem);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + ST_STAGES * ST_STAGE_BYTES);
+    const int64_t ntiles = (g.n + ST_TILE - 1) / ST_TILE;
+    const int64_t npad = st27_padded_nodes(g.n);
+    // copy of tile `tile` into stage s: its nodes rounded up to 4 (the padded tail of S)
+    auto issue = [&](int64_t tile, int s) {
+        const int64_t i0 = tile * ST_TILE;
+        const int64_t cnt = npad - i0 < ST_TILE ? npad - i0 : ST_TILE;
+        const uint32_t bytes = (uint32_t)(cnt * 27 * sizeof(float));
+        mbar_arrive_expect_tx(&full[s], bytes);
+        bulk_g2s(ring + (size_t)s * ST_TILE * 27, S + i0 * 27, bytes, &full[s]);
+    };
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < ST_STAGES; ++s) mbar_init(&full[s], 1);
+        fence_mbar_init();
+        for (int s = 0; s < ST_STAGES; ++s)
+            if (blockIdx.x + (int64_t)s * gridDim.x < ntiles) issue(blockIdx.x + (int64_t)s * gridDim.x, s);
+    }
+    __syncthreads();
+    const int64_t yz = (int64_t)g.ny * g.nz;
+    int it = 0;
+    int64_t tile = blockIdx.x;
+    for (; tile < ntiles; tile += gridDim.x, ++it) {
+        const int s = it % ST_STAGES;
+        // every thread waits (bounded); the CTA leaves together if any wait gave up
+        if (!__syncthreads_and(mbar_wait_bounded(&full[s], (uint32_t)(it / ST_STAGES) & 1u))) break;
+        const int64_t i = tile * ST_TILE + threadIdx.x;
+        if (i < g.n) {
+            const float* c = ring + (size_t)s * ST_TILE * 27 + threadIdx.x * 27;
+            int x, y, z;
+            st27_coords(g, i, x, y, z);
+            const bool okx[3] = {x > 0, true, x < g.nx - 1};
+            const bool oky[3] = {y > 0, true, y < g.ny - 1};
+            const bool okz[3] = {z > 0, true, z < g.nz - 1};
+            float acc = 0.f;
+#pragma unroll
+            for (int k = 0; k < 27; ++k) {
+                const int dx = k / 9 - 1, dy = (k / 3) % 3 - 1, dz = k % 3 - 1;
+                if (okx[dx + 1] && oky[dy + 1] && okz[dz + 1]) {
+                    const int64_t j = i + dx * yz + (int64_t)dy * g.nz + dz;
+                    // MODE 1: the first Jacobi iterate w = omega D^-1 r, formed on the fly
+                    const float wj = MODE == 1 ? omega * __ldg(dinv + j) * __ldg(r + j) : w[j];
+                    acc = fmaf(c[k], wj, acc);
+                }
+            }
+            const float ri = r[i];
+            if (MODE == 0) {
+                out[i] = ri - acc;
+            } else if (MODE == 1) {
+                w_out[i] = omega * dinv[i] * ri;
+                out[i] = ri - acc;
+            } else {
+                out[i] = w[i] + omega * dinv[i] * (ri - acc);
+            }
+        }
+        __syncthreads();  // stage s is read: refill it
+        if (threadIdx.x == 0 && tile + (int64_t)ST_STAGES * gridDim.x < ntiles)
+            issue(tile + (int64_t)ST_STAGES * gridDim.x, s);
+    }
+    if (tile < ntiles) {
+        // a wait gave up: drain the copies still in flight (bounded) before shared memory goes away
+        if (threadIdx.x == 0) {
+            for (int q = 0; q < ST_STAGES; ++q) {
+                const int64_t tq = tile + (int64_t)q * gridDim.x;
+                if (tq < ntiles) mbar_wait_bounded(&full[(it + q) % ST_STAGES], (uint32_t)((it + q) / ST_STAGES) & 1u);
+            }
+            atomicOr(status, GB_DEV_WAIT_TIMEOUT);
+        }
+        __syncthreads();
+    }
+}
+
+static int st27_grid(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(n, 256), kSmCount * 8)); }
+
+static int st27_apply_grid(int64_t n)
+{
+    int dev = 0, sms = kSmCount;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(n, ST_TILE), (int64_t)sms * 2));
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+GB_API size_t gb_st27_bytes(int nx, int ny, int nz)
+{
+    return (size_t)27 * st27_padded_nodes((int64_t)nx * ny * nz) * sizeof(float);
+}
+
+// CSR (1x1 fp32, compact rows) on an nx x ny x nz node grid -> node-major coefficients S
+// (gb_st27_bytes; 16-byte aligned; the padded tail is not read back into results).
+// status bit 1: an entry lies outside the 27-neighbourhood (S is then incomplete).
+GB_API int gb_st27_build(int nx, int ny, int nz, const int* offsets, const int* columns, const float* values,
+                         float* S, int* status, cudaStream_t stream)
+{
+    GB_REQUIRE(nx >= 1 && ny >= 1 && nz >= 1 && offsets && columns && values && S && status, "st27_build: bad arguments");
+    const St27Grid g{nx, ny, nz, (int64_t)nx * ny * nz};
+    GB_REQUIRE(g.n < (int64_t(1) << 31), "st27_build: grid too large");
+    GB_REQUIRE((uintptr_t)S % 16 == 0, "st27_build: S must be 16-byte aligned");
+    GB_CHECK_CUDA(launch_pdl(k_st27_build, st27_grid(g.n), 256, 0, stream, g, offsets, columns, values, S, status));
+    return GB_OK;
+}
+
+// mode 0: out = r - A w;  mode 1: w_out = omega D^-1 r, out = r - A w_out;  mode 2: out = w + omega D^-1 (r - A w).
+// out must not alias w, r or w_out.  status: GB_DEV_WAIT_TIMEOUT if a staging wait gave up.
+GB_API int gb_st27_apply(int mode, int nx, int ny, int nz, const float* S, const float* w, const float* r,
+                         const float* dinv, float omega, float* w_out, float* out, int* status, cudaStream_t stream)
+{
+    GB_REQUIRE(nx >= 1 && ny >= 1 && nz >= 1 && S && r && out && status, "st27_apply: bad arguments");
+    GB_REQUIRE((uintptr_t)S % 16 == 0, "st27_apply: S must be 16-byte aligned");
+    GB_REQUIRE(mode == 1 ? (dinv && w_out) : (w != nullptr && (mode == 0 || dinv != nullptr)),
+               "st27_apply: missing operand for mode");
+    GB_REQUIRE(out != w && out != r && out != w_out, "st27_apply: out must not alias an input");
+    const St27Grid g{nx, ny, nz, (int64_t)nx * ny * nz};
+    GB_REQUIRE(g.n < (int64_t(1) << 31), "st27_apply: grid too large");
+    const int grid = st27_apply_grid(g.n);
+    if (mode == 0) {
+        GB_CHECK_CUDA(cudaFuncSetAttribute(k_st27_apply<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ST_SMEM));
+        GB_CHECK_CUDA(launch_pdl(k_st27_apply<0>, grid, ST_TILE, ST_SMEM, stream, g, S, w, r, dinv, omega, w_out, out,
+                                 status));
+    } else if (mode == 1) {
+        GB_CHECK_CUDA(cudaFuncSetAttribute(k_st27_apply<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ST_SMEM));
+        GB_CHECK_CUDA(launch_pdl(k_st27_apply<1>, grid, ST_TILE, ST_SMEM, stream, g, S, w, r, dinv, omega, w_out, out,
+                                 status));
+    } else if (mode == 2) {
+        GB_CHECK_CUDA(cudaFuncSetAttribute(k_st27_apply<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ST_SMEM));
+        GB_CHECK_CUDA(launch_pdl(k_st27_apply<2>, grid, ST_TILE, ST_SMEM, stream, g, S, w, r, dinv, omega, w_out, out,
+                                 status));
+    } else {
+        gb::set_error("st27_apply: mode must be 0, 1 or 2");
+        return GB_ERR_INVALID;
+    }
+    return GB_OK;
+}

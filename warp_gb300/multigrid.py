@@ -12,6 +12,11 @@ learned preconditioner of this package needs a carrier with global reach, since 
 * smoothing: damped Jacobi, the post-smoothing step fused with its residual product
   (``gb_bsr_jacobi_smooth``); the coarsest level (<= ``coarsest_nodes`` nodes) is solved with a
   dense inverse computed once at set-up;
+* level operators in 27-point stencil form (``gb_st27_build``: 27 coefficient planes instead of CSR
+  columns and offsets, about half the bytes per pass, staged by bulk copies), the first Jacobi step fused
+  with the residual
+  and the post-smoothing step fused with its residual (``gb_st27_apply``); a level whose CSR has
+  entries outside the 27-neighbourhood keeps the CSR kernels;
 * an optional learned fine-level smoother (``warp_gb300.learned``) replaces the first Jacobi step.
 
 Every launch goes to the stream the caller passes, so the flexible solver can capture a whole
@@ -42,10 +47,11 @@ class MultigridPreconditioner:
         faces: Dirichlet faces (default: the whole boundary).
         omega: Jacobi damping.
         coarsest_nodes: stop coarsening at or below this many nodes.
+        stencil: apply the level operators in 27-point stencil form (else the CSR kernels).
     """
 
     def __init__(self, Am: sparse.BsrMatrix, geo, coef, faces=("x-", "x+", "y-", "y+", "z-", "z+"), omega: float = 0.6,
-                 coarsest_nodes: int = 400, max_levels: int = 12):
+                 coarsest_nodes: int = 400, max_levels: int = 12, stencil: bool = True):
         if Am.block_shape != (1, 1) or Am.scalar_type != torch.float32:
             raise ValueError("multigrid preconditioner: scalar fp32 BSR matrix required")
         self.omega = float(omega)
@@ -94,6 +100,17 @@ class MultigridPreconditioner:
                               fields={"u": fem.make_trial(space, bd), "v": fem.make_test(space, bd)}, assembly="nodal")
             fem.project_linear_system(cA, rhs, P)
             cur_geo, cur_A, cur_coef = cgeo, cA, ccoef
+        # stencil planes of every level above the coarsest
+        st_status = A.zeros(len(levels), torch.int32)
+        for li, lv in enumerate(levels):
+            lv.S = None
+            if stencil and li < len(levels) - 1:
+                lv.S = A.empty(int(L.gb_st27_bytes(*lv.dims)) // 4, torch.float32)
+                N.check(L.gb_st27_build(*lv.dims, A.ptr(lv.A.offsets), A.ptr(lv.A.columns), A.ptr(lv.A.values),
+                                        A.ptr(lv.S), st_status[li:].data_ptr(), stream), "st27_build")
+        for li, bad in enumerate(st_status.tolist()):
+            if bad:
+                levels[li].S = None  # entries outside the 27-neighbourhood: keep the CSR kernels
         # coarsest level: dense inverse (set-up only; a few hundred unknowns)
         last = levels[-1]
         dense = last.A.numpy_dense()
@@ -110,9 +127,16 @@ class MultigridPreconditioner:
 
     @property
     def kernels_per_apply(self) -> int:
-        """Kernel launches of one V-cycle (5 per level above the coarsest + the coarse solve)."""
-        extra = getattr(self.smoother, "kernels_per_apply", 0) - 1 if self.smoother is not None else 0
-        return 5 * (len(self.levels) - 1) + 1 + max(extra, 0)
+        """Kernel launches of one V-cycle: per level above the coarsest, the first smoothing step,
+        residual, restriction, prolongation and post-smoothing (stencil form: the first two fused),
+        plus the coarse solve."""
+        count = 1
+        for li, lv in enumerate(self.levels[:-1]):
+            if li == 0 and self.smoother is not None:
+                count += getattr(self.smoother, "kernels_per_apply", 1) + 4
+            else:
+                count += 4 if lv.S is not None else 5
+        return count
 
     def describe(self) -> str:
         return " -> ".join(f"{'x'.join(str(d) for d in lv.dims)}" for lv in self.levels)
@@ -130,15 +154,21 @@ class MultigridPreconditioner:
         nxt = self.levels[li + 1]
         w, t = A.ptr(lv.w), A.ptr(lv.t)
         Am = lv.A
-        # pre-smoothing from zero: learned step on the fine level when available, else Jacobi
+        # pre-smoothing from zero (learned step on the fine level when available, else Jacobi) and
+        # the residual t = r - A w
         if li == 0 and self.smoother is not None:
             self.smoother.launch(stream, r, w)
+            if lv.S is not None:
+                N.check(L.gb_st27_apply(0, *lv.dims, A.ptr(lv.S), w, r, None, self.omega, None, t, A.ptr(self.status),
+                                        stream), "residual")
+            else:
+                self._csr_residual(lv, w, r, t, stream)
+        elif lv.S is not None:
+            N.check(L.gb_st27_apply(1, *lv.dims, A.ptr(lv.S), None, r, A.ptr(lv.dinv), self.omega, w, t,
+                                    A.ptr(self.status), stream), "jacobi0+residual")
         else:
             N.check(L.gb_mg_jacobi0(lv.n, self.omega, A.ptr(lv.dinv), r, w, stream), "jacobi0")
-        # t = r - A w
-        N.check(L.gb_bsr_mv(1, 1, lv.n, lv.n, lv.nnz, Am.capacity, A.ptr(Am.offsets), None, A.ptr(Am.columns),
-                            A.ptr(Am.values), N.GB_F32, w, r, t, N.GB_F32, -1.0, 1.0, 0, 0, 0, -1, A.ptr(self.status),
-                            stream), "residual")
+            self._csr_residual(lv, w, r, t, stream)
         fx, fy, fz = lv.dims
         cx, cy, cz = nxt.dims
         rc, zc = A.ptr(nxt.rhs), A.ptr(nxt.sol)  # the coarse level's own w/t are its work vectors
@@ -146,9 +176,19 @@ class MultigridPreconditioner:
         self._vcycle(li + 1, rc, zc, stream)
         N.check(L.gb_mg_prolong_add(fx, fy, fz, cx, cy, cz, zc, A.ptr(lv.mask), 1.0, w, stream), "prolong")
         # post-smoothing fused with its residual: z = w + omega D^-1 (r - A w)
-        N.check(L.gb_bsr_jacobi_smooth(1, lv.n, lv.nnz, Am.capacity, A.ptr(Am.offsets), A.ptr(Am.columns),
-                                       A.ptr(Am.values), r, w, A.ptr(lv.dinv), self.omega, z, A.ptr(self.status),
-                                       stream), "smooth")
+        if lv.S is not None:
+            N.check(L.gb_st27_apply(2, *lv.dims, A.ptr(lv.S), w, r, A.ptr(lv.dinv), self.omega, None, z,
+                                    A.ptr(self.status), stream), "smooth")
+        else:
+            N.check(L.gb_bsr_jacobi_smooth(1, lv.n, lv.nnz, Am.capacity, A.ptr(Am.offsets), A.ptr(Am.columns),
+                                           A.ptr(Am.values), r, w, A.ptr(lv.dinv), self.omega, z, A.ptr(self.status),
+                                           stream), "smooth")
+
+    def _csr_residual(self, lv, w: int, r: int, t: int, stream) -> None:
+        Am = lv.A
+        N.check(N.lib().gb_bsr_mv(1, 1, lv.n, lv.n, lv.nnz, Am.capacity, A.ptr(Am.offsets), None, A.ptr(Am.columns),
+                                  A.ptr(Am.values), N.GB_F32, w, r, t, N.GB_F32, -1.0, 1.0, 0, 0, 0, -1,
+                                  A.ptr(self.status), stream), "residual")
 
     def apply(self, r: torch.Tensor, z: torch.Tensor | None = None) -> torch.Tensor:
         """Eager z = M r on the current stream (tests / diagnostics)."""
