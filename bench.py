@@ -373,6 +373,18 @@ def run_profile(args):
         assert int(st.item()) == 0
         print("profile run done", flush=True)
         return 0
+    if args.profile == "vcycle":  # 3 eager V-cycles (stencil-form levels) on the 97^3 node grid
+        from warp_gb300 import multigrid, problems
+
+        system = problems.diffusion(args.res, sigma=1.5, corr_length=0.1, seed=args.seed)
+        mg = multigrid.MultigridPreconditioner(system.A, system.geo, system.coef)
+        r = torch.randn(system.A.nrow, device="cuda") * (1 - mg.levels[0].mask)
+        for _ in range(3):
+            mg.apply(r)
+        torch.cuda.synchronize()
+        assert int(mg.status.item()) == 0
+        print("profile run done", flush=True)
+        return 0
     if args.profile == "batched":  # 512 uneven systems, two eager batched launches (fixed shape)
         from warp_gb300 import batched
 
@@ -438,12 +450,13 @@ def main():
     p.add_argument("--batch-count", type=int, default=4096)
     p.add_argument("--elasticity-res", type=int, default=64)
     p.add_argument("--weights", default=os.path.join(ROOT, "warp_gb300", "data", "smoother_q1_diffusion.npz"))
-    p.add_argument("--profile", choices=["spmv", "cg", "jacobi_solve", "solve", "conv", "batched"], default=None,
+    p.add_argument("--profile", choices=["spmv", "cg", "jacobi_solve", "solve", "conv", "batched", "vcycle"],
+                   default=None,
                    help="run a fixed kernel sequence for an ncu capture and exit (prints no bench line): "
                         "spmv = 8 bsr_mv launches, cg = 30 eager (non-graph) Jacobi-CG iterations, "
                         "jacobi_solve = one refined Jacobi-CG solve, solve = two learned-FCG solves (eager launches), "
                         "conv = 3 launches of one tcgen05 conv layer on the node grid, batched = two launches of "
-                        "the batched CG on 512 uneven systems")
+                        "the batched CG on 512 uneven systems, vcycle = 3 eager multigrid V-cycles (stencil levels)")
     args = p.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 

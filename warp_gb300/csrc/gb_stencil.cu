@@ -11,11 +11,12 @@
 // Neighbours outside the grid are skipped.
 //
 // The apply kernel is persistent: per 256-node tile one thread issues a 1-D bulk copy of the tile's
-// 27.6 KB of coefficients into a 3-stage shared-memory ring (one contiguous stream per CTA, as the
-// CSR kernel's staging); each thread reads its node's 27 coefficients from shared memory (word
-// stride 27, odd: no bank conflicts) and its neighbours' vector entries through the read-only path.
-// (A planar S[k][i] layout read with 27 plain loads per thread ran 1.5-2x slower than the CSR kernel:
-// 27 concurrent streams per warp.)
+// 27.6 KB of coefficients into a 2-stage shared-memory ring (one contiguous stream per CTA, as the
+// CSR kernel's staging), four CTAs per SM; each thread reads its node's 27 coefficients from shared
+// memory (word stride 27, odd: no bank conflicts) and its neighbours' vector entries through the
+// read-only path.  Measured at 97^3 (GB300): 22-24 us per pass (~5 TB/s); 3 stages x 2 CTAs per SM
+// (16 warps) was latency-bound at 31 us, and a planar S[k][i] layout read with 27 plain loads per
+// thread ran 1.5-2x slower than the CSR kernel (27 concurrent streams per warp).
 //
 // Kernels:
 //   gb_st27_build  CSR (1x1 fp32, compact) -> S; an entry outside the 27-neighbourhood sets
@@ -78,7 +79,8 @@ __global__ void k_st27_build(St27Grid g, const int* __restrict__ offsets, const 
 }
 
 constexpr int ST_TILE = 256;    // nodes per tile = threads per CTA
-constexpr int ST_STAGES = 3;
+constexpr int ST_STAGES = 2;     // 2 stages x 27.6 KB: four CTAs (32 warps) per SM
+constexpr int ST_CTAS_PER_SM = 4;
 constexpr size_t ST_STAGE_BYTES = (size_t)ST_TILE * 27 * sizeof(float);
 constexpr size_t ST_SMEM = ST_STAGES * ST_STAGE_BYTES + 64;
 
@@ -170,7 +172,7 @@ static int st27_apply_grid(int64_t n)
     int dev = 0, sms = kSmCount;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(n, ST_TILE), (int64_t)sms * 2));
+    return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(n, ST_TILE), (int64_t)sms * ST_CTAS_PER_SM));
 }
 
 }  // namespace gb
