@@ -22,7 +22,9 @@ __device__ __forceinline__ int64_t nidx(const NodeGrid& g, int x, int y, int z)
 }
 
 // rc[I] = mask_c[I] * sum_{d in {-1,0,1}^3} w(d) r[2I + d],  w = prod (1 if d=0 else 1/2); fine
-// nodes outside the grid or masked (Dirichlet) contribute nothing.
+// nodes outside the grid or masked (Dirichlet) contribute nothing.  Branch-free: every tap loads from
+// a clamped in-grid index and adds a zero when it does not count, so all 54 loads can be in flight
+// at once (the sum over the counted taps, in tap order, is unchanged).
 __global__ void k_restrict_fw(NodeGrid fg, NodeGrid cg, const float* __restrict__ r, const float* __restrict__ fmask,
                               const float* __restrict__ cmask, float* __restrict__ rc)
 {
@@ -33,32 +35,38 @@ __global__ void k_restrict_fw(NodeGrid fg, NodeGrid cg, const float* __restrict_
     const int X = (int)(I / ((int64_t)cg.ny * cg.nz));
     const int Y = (int)((I / cg.nz) % cg.ny);
     const int Z = (int)(I % cg.nz);
-    if (cmask && cmask[I] != 0.f) {
-        rc[I] = 0.f;
-        return;
-    }
+    const bool cmasked = cmask && __ldg(cmask + I) != 0.f;
     float s = 0.f;
+#pragma unroll
     for (int dx = -1; dx <= 1; ++dx) {
         const int x = 2 * X + dx;
-        if (x < 0 || x >= fg.nx) continue;
+        const bool vx = x >= 0 && x < fg.nx;
+        const int xc = min(max(x, 0), fg.nx - 1);
         const float wx = dx == 0 ? 1.f : 0.5f;
+#pragma unroll
         for (int dy = -1; dy <= 1; ++dy) {
             const int y = 2 * Y + dy;
-            if (y < 0 || y >= fg.ny) continue;
+            const bool vy = y >= 0 && y < fg.ny;
+            const int yc = min(max(y, 0), fg.ny - 1);
             const float wy = dy == 0 ? 1.f : 0.5f;
+#pragma unroll
             for (int dz = -1; dz <= 1; ++dz) {
                 const int z = 2 * Z + dz;
-                if (z < 0 || z >= fg.nz) continue;
-                const int64_t i = nidx(fg, x, y, z);
-                if (fmask && fmask[i] != 0.f) continue;
-                s += wx * wy * (dz == 0 ? 1.f : 0.5f) * r[i];
+                const bool vz = z >= 0 && z < fg.nz;
+                const int zc = min(max(z, 0), fg.nz - 1);
+                const int64_t i = nidx(fg, xc, yc, zc);
+                const float rv = __ldg(r + i);
+                const bool keep = vx && vy && vz && !(fmask && __ldg(fmask + i) != 0.f);
+                s += keep ? wx * wy * (dz == 0 ? 1.f : 0.5f) * rv : 0.f;
             }
         }
     }
-    rc[I] = s;
+    rc[I] = cmasked ? 0.f : s;
 }
 
-// z[i] += scale * sum_parents w * zc[parent]   (trilinear interpolation; masked fine nodes kept)
+// z[i] += scale * sum_parents w * zc[parent]   (trilinear interpolation; masked fine nodes kept).
+// Branch-free as the restriction: the 8 candidate parents are loaded from clamped indices and only
+// the real ones (1, 2, 4 or 8 of them, in the same order) are summed.
 __global__ void k_prolong_add(NodeGrid fg, NodeGrid cg, const float* __restrict__ zc, const float* __restrict__ fmask,
                               float scale, float* __restrict__ z)
 {
@@ -66,19 +74,26 @@ __global__ void k_prolong_add(NodeGrid fg, NodeGrid cg, const float* __restrict_
     const int64_t n = (int64_t)fg.nx * fg.ny * fg.nz;
     const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
-    if (fmask && fmask[i] != 0.f) return;
+    const bool masked = fmask && __ldg(fmask + i) != 0.f;
     const int x = (int)(i / ((int64_t)fg.ny * fg.nz));
     const int y = (int)((i / fg.nz) % fg.ny);
     const int zz = (int)(i % fg.nz);
-    const int x0 = x >> 1, x1 = (x + 1) >> 1, y0 = y >> 1, y1 = (y + 1) >> 1, z0 = zz >> 1, z1 = (zz + 1) >> 1;
+    const int xs[2] = {x >> 1, min((x + 1) >> 1, cg.nx - 1)};
+    const int ys[2] = {y >> 1, min((y + 1) >> 1, cg.ny - 1)};
+    const int zs[2] = {zz >> 1, min((zz + 1) >> 1, cg.nz - 1)};
     const float wx = (x & 1) ? 0.5f : 1.f, wy = (y & 1) ? 0.5f : 1.f, wz = (zz & 1) ? 0.5f : 1.f;
-    float s = 0.f;
-    const int xs[2] = {x0, x1}, ys[2] = {y0, y1}, zs[2] = {z0, z1};
     const int nxp = (x & 1) ? 2 : 1, nyp = (y & 1) ? 2 : 1, nzp = (zz & 1) ? 2 : 1;
-    for (int a = 0; a < nxp; ++a)
-        for (int b = 0; b < nyp; ++b)
-            for (int c = 0; c < nzp; ++c) s += zc[nidx(cg, xs[a], ys[b], zs[c])];
-    z[i] += scale * wx * wy * wz * s;
+    float s = 0.f;
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+#pragma unroll
+            for (int c = 0; c < 2; ++c) {
+                const float v = __ldg(zc + nidx(cg, xs[a], ys[b], zs[c]));
+                s += (a < nxp && b < nyp && c < nzp) ? v : 0.f;
+            }
+    if (!masked) z[i] += scale * wx * wy * wz * s;
 }
 
 // z = omega * dinv * r   (first damped Jacobi step from z = 0)
