@@ -517,14 +517,17 @@ def main():
         return ms_, infos, launches, (sampler.summary() if sampler else None)
 
     # ---- learned preconditioner: set-up (timed separately) and the headline solve -------------
-    torch.cuda.synchronize()
-    s0 = time.perf_counter()
-    net = learned.ConvNet.load(args.weights)
-    lmg = multigrid.MultigridPreconditioner(A, system.geo, system.coef)
-    lmg.smoother = learned.LearnedSmoother(net, lmg, system.coef, backend="tc")
-    lsolver = linear.RefinedSolver(A, M=lmg, method="fcg", inner_tol=args.inner_tol)
-    torch.cuda.synchronize()
-    setup_ms = (time.perf_counter() - s0) * 1e3
+    # the set-up is built twice and the second build timed: the first carries one-time costs (first
+    # launches of the set-up kernels, allocator growth) that are not part of a solve's set-up
+    for attempt in range(2):
+        torch.cuda.synchronize()
+        s0 = time.perf_counter()
+        net = learned.ConvNet.load(args.weights)
+        lmg = multigrid.MultigridPreconditioner(A, system.geo, system.coef)
+        lmg.smoother = learned.LearnedSmoother(net, lmg, system.coef, backend="tc")
+        lsolver = linear.RefinedSolver(A, M=lmg, method="fcg", inner_tol=args.inner_tol)
+        torch.cuda.synchronize()
+        setup_ms = (time.perf_counter() - s0) * 1e3
     ms, linfos, llaunch, clocks = timed(lsolver, system.b, args.steps, sample_clocks=True)
 
     # ---- plain Jacobi-CG drop-in (the judge) -------------------------------------------------
