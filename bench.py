@@ -301,6 +301,88 @@ def bench_elasticity(args, hbm_peak):
             "rel_residual": infos[-1]["rel_residual"]}
 
 
+def bench_elasticity_large(args, hbm_peak):
+    """128^3 Q1 vec3 elasticity (E lognormal sigma=1.5, GRF correlation length 0.05, nu=0.3, gravity,
+    x=0 clamped; 2.15 M nodes, 6.4 M dofs): assembly (triplet and row-compress constructions), 3x3
+    bsr_mv with fp32 and bf16 values, and the refined flexible-CG solve to 1e-8 with the vec3 multigrid
+    V-cycle (fp32 and bf16 inner values)."""
+    import numpy as np
+    import torch
+
+    from warp_gb300 import fem, multigrid, problems, sparse
+    from warp_gb300.optim import linear
+
+    res = args.elasticity_large_res
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s = problems.elasticity((res,) * 3, sigma=1.5, corr_length=0.05, seed=args.seed)
+    torch.cuda.synchronize()
+    problem_s = time.perf_counter() - t0
+    A = s.A
+    nnz = A.nnz_sync()
+    n = A.nrow * 3
+    ncells = res ** 3
+    # assembly alone (fem.integrate of the bilinear form), both constructions
+    lam, mu = fem.q1.lame_from_young(s.coef, 0.3)
+    lam_t = torch.from_numpy(lam.astype(np.float32)).cuda()
+    mu_t = torch.from_numpy(mu.astype(np.float32)).cuda()
+    space = fem.make_polynomial_space(s.geo, degree=1, dtype="vec3")
+    fields = {"u": fem.make_trial(space), "v": fem.make_test(space)}
+    asm = {}
+    for construction in ("triplets", "row_compress"):
+        def assemble():
+            M_ = fem.integrate(fem.linear_elasticity_form, fields=fields, values={"lame": (lam_t, mu_t)},
+                               bsr_options={"construction": construction})
+            M_.nnz_sync()
+        asm[construction] = _event_ms(assemble, 2, warmup=1)
+        torch.cuda.empty_cache()
+    triplets = ncells * 64
+    asm_bytes = triplets * (8 + 36) + nnz * (4 + 36) + (A.nrow + 1) * 4
+    # 3x3 SpMV, fp32 and bf16 values
+    xv = torch.randn(n, device="cuda")
+    yv = torch.empty_like(xv)
+    mv_ms = _event_ms(lambda: sparse.bsr_mv(A, xv, yv), 10, warmup=3)
+    mv_bytes = nnz * (36 + 4) + (A.nrow + 1) * 4 + 2 * n * 4
+    Ab = sparse.BsrMatrix(A.nrow, A.ncol, A.block_shape, torch.bfloat16)
+    Ab.offsets, Ab.columns, Ab.nnz = A.offsets, A.columns, A.nnz
+    Ab.values = A.values[:nnz].to(torch.bfloat16).contiguous()
+    mvb_ms = _event_ms(lambda: sparse.bsr_mv(Ab, xv, yv), 10, warmup=3)
+    mvb_bytes = nnz * (18 + 4) + (A.nrow + 1) * 4 + 2 * n * 4
+    # multigrid set-up and the refined flexible-CG solves
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    mg = multigrid.MultigridPreconditioner(A, s.geo, s.coef, faces=("x-",))
+    torch.cuda.synchronize()
+    mg_setup_s = time.perf_counter() - t0
+    out = {"workload": f"{res}^3 Q1 vec3 elasticity, {A.nrow} block rows ({n} dofs), {nnz} blocks, E lognormal "
+                       f"sigma 1.5 GRF l=0.05",
+           "problem_build_s": problem_s,
+           "assembly_ms": asm["triplets"], "assembly_row_compress_ms": asm["row_compress"],
+           "assembly_algorithmic_bytes": asm_bytes,
+           "assembly_frac_of_hbm": asm_bytes / (asm["triplets"] * 1e-3) / 1e9 / hbm_peak,
+           "bsr_mv_us": mv_ms * 1e3, "bsr_mv_gbs": mv_bytes / (mv_ms * 1e-3) / 1e9,
+           "bsr_mv_frac_of_hbm": mv_bytes / (mv_ms * 1e-3) / 1e9 / hbm_peak,
+           "bsr_mv_bf16_us": mvb_ms * 1e3, "bsr_mv_bf16_gbs": mvb_bytes / (mvb_ms * 1e-3) / 1e9,
+           "bsr_mv_bf16_frac_of_hbm": mvb_bytes / (mvb_ms * 1e-3) / 1e9 / hbm_peak,
+           "mg_levels": mg.describe(), "mg_setup_ms": mg_setup_s * 1e3,
+           "mg_omega": [round(lv.omega, 4) for lv in mg.levels]}
+    solver = linear.RefinedSolver(A, M=mg, method="fcg", inner_tol=args.inner_tol, inner_maxiter=5000)
+    solver.solve(s.b, tol=1e-8, max_outer=10)
+    infos = []
+    ms = _event_ms(lambda: infos.append(solver.solve(s.b, tol=1e-8, max_outer=10)[1]), 2, warmup=0)
+    out["mg_fcg_fp32_ms"] = ms
+    out["mg_fcg_fp32_inner_iterations"] = infos[-1]["inner_iterations"]
+    out["mg_fcg_fp32_outer_iterations"] = infos[-1]["outer"]
+    out["mg_fcg_fp32_rel_residual"] = infos[-1]["rel_residual"]
+    out["mg_fcg_fp32_converged"] = infos[-1]["converged"]
+    out["mg_fcg_fp32_fallbacks"] = solver.fallbacks
+    out["note"] = ("flexible CG with the vec3 geometric V-cycle (point-Jacobi smoothing, damping 4/(3 rho) per "
+                   "level), FP32 values; bf16 values are measured for the SpMV only -- as the inner operator of "
+                   "the refined solve they diverge on this field (sigma 1.5); the 3-channel conv-net smoother "
+                   "for this configuration is not built")
+    return out
+
+
 def run_reference(args):
     ws, rank = _dist()
     if rank != 0:
@@ -446,9 +528,11 @@ def main():
     p.add_argument("--ref-full-iters", type=int, default=2000)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-extras", action="store_true",
-                   help="skip the batched, assembly and elasticity measurements")
+                   help="skip the batched, assembly and elasticity (64^3 and 128^3) measurements")
     p.add_argument("--batch-count", type=int, default=4096)
     p.add_argument("--elasticity-res", type=int, default=64)
+    p.add_argument("--elasticity-large-res", type=int, default=128,
+                   help="cells per axis of the large elasticity extra (0 skips it)")
     p.add_argument("--weights", default=os.path.join(ROOT, "warp_gb300", "data", "smoother_q1_diffusion.npz"))
     p.add_argument("--profile", choices=["spmv", "cg", "jacobi_solve", "solve", "conv", "batched", "vcycle"],
                    default=None,
@@ -661,6 +745,8 @@ def main():
         extras["assembly_96cube"] = bench_assembly(args, system, hbm_peak)
         extras["batched_uneven"] = bench_batched(args, hbm_peak)
         extras["elasticity"] = bench_elasticity(args, hbm_peak)
+        if args.elasticity_large_res > 0:
+            extras["elasticity_large"] = bench_elasticity_large(args, hbm_peak)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

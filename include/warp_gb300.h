@@ -196,6 +196,11 @@ int gb_mg_restrict(int fnx, int fny, int fnz, int cnx, int cny, int cnz, const f
                    const float* cmask, float* rc, gb_stream_t stream);
 int gb_mg_prolong_add(int fnx, int fny, int fnz, int cnx, int cny, int cnz, const float* zc, const float* fmask,
                       float scale, float* z, gb_stream_t stream);
+/* Same transfers for vectors of ncomp (1 or 3) interleaved components per node, node masks. */
+int gb_mg_restrict_c(int ncomp, int fnx, int fny, int fnz, int cnx, int cny, int cnz, const float* r, const float* fmask,
+                     const float* cmask, float* rc, gb_stream_t stream);
+int gb_mg_prolong_add_c(int ncomp, int fnx, int fny, int fnz, int cnx, int cny, int cnz, const float* zc,
+                        const float* fmask, float scale, float* z, gb_stream_t stream);
 int gb_mg_jacobi0(int64_t n, float omega, const float* dinv, const float* r, float* z, gb_stream_t stream);
 int gb_mg_coarsen_cells(int fx, int fy, int fz, const float* a, float* ac, gb_stream_t stream);
 /* 27-point stencil form of a multigrid level's operator (no reference counterpart): node-major

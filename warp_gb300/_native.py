@@ -73,6 +73,8 @@ _SIGNATURES = {
     "gb_bsr_jacobi_smooth": (_c_int, [_c_int, _c_int, _c_i64, _c_i64, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_float,
                                       _vp, _vp, _vp]),
     "gb_mg_restrict": (_c_int, [_c_int] * 6 + [_vp, _vp, _vp, _vp, _vp]),
+    "gb_mg_restrict_c": (_c_int, [_c_int] * 7 + [_vp, _vp, _vp, _vp, _vp]),
+    "gb_mg_prolong_add_c": (_c_int, [_c_int] * 7 + [_vp, _vp, ctypes.c_float, _vp, _vp]),
     "gb_mg_prolong_add": (_c_int, [_c_int] * 6 + [_vp, _vp, ctypes.c_float, _vp, _vp]),
     "gb_mg_jacobi0": (_c_int, [_c_i64, ctypes.c_float, _vp, _vp, _vp, _vp]),
     "gb_st27_bytes": (_c_sz, [_c_int, _c_int, _c_int]),

@@ -25,6 +25,9 @@ __device__ __forceinline__ int64_t nidx(const NodeGrid& g, int x, int y, int z)
 // nodes outside the grid or masked (Dirichlet) contribute nothing.  Branch-free: every tap loads from
 // a clamped in-grid index and adds a zero when it does not count, so all 54 loads can be in flight
 // at once (the sum over the counted taps, in tap order, is unchanged).
+// Vectors hold C interleaved components per node (value of component c at node i: [i*C + c]); the
+// masks are per node.
+template <int C>
 __global__ void k_restrict_fw(NodeGrid fg, NodeGrid cg, const float* __restrict__ r, const float* __restrict__ fmask,
                               const float* __restrict__ cmask, float* __restrict__ rc)
 {
@@ -36,7 +39,9 @@ __global__ void k_restrict_fw(NodeGrid fg, NodeGrid cg, const float* __restrict_
     const int Y = (int)((I / cg.nz) % cg.ny);
     const int Z = (int)(I % cg.nz);
     const bool cmasked = cmask && __ldg(cmask + I) != 0.f;
-    float s = 0.f;
+    float s[C];
+#pragma unroll
+    for (int c = 0; c < C; ++c) s[c] = 0.f;
 #pragma unroll
     for (int dx = -1; dx <= 1; ++dx) {
         const int x = 2 * X + dx;
@@ -55,18 +60,23 @@ __global__ void k_restrict_fw(NodeGrid fg, NodeGrid cg, const float* __restrict_
                 const bool vz = z >= 0 && z < fg.nz;
                 const int zc = min(max(z, 0), fg.nz - 1);
                 const int64_t i = nidx(fg, xc, yc, zc);
-                const float rv = __ldg(r + i);
                 const bool keep = vx && vy && vz && !(fmask && __ldg(fmask + i) != 0.f);
-                s += keep ? wx * wy * (dz == 0 ? 1.f : 0.5f) * rv : 0.f;
+#pragma unroll
+                for (int c = 0; c < C; ++c) {
+                    const float rv = __ldg(r + i * C + c);
+                    s[c] += keep ? wx * wy * (dz == 0 ? 1.f : 0.5f) * rv : 0.f;
+                }
             }
         }
     }
-    rc[I] = cmasked ? 0.f : s;
+#pragma unroll
+    for (int c = 0; c < C; ++c) rc[I * C + c] = cmasked ? 0.f : s[c];
 }
 
 // z[i] += scale * sum_parents w * zc[parent]   (trilinear interpolation; masked fine nodes kept).
 // Branch-free as the restriction: the 8 candidate parents are loaded from clamped indices and only
 // the real ones (1, 2, 4 or 8 of them, in the same order) are summed.
+template <int C>
 __global__ void k_prolong_add(NodeGrid fg, NodeGrid cg, const float* __restrict__ zc, const float* __restrict__ fmask,
                               float scale, float* __restrict__ z)
 {
@@ -83,17 +93,27 @@ __global__ void k_prolong_add(NodeGrid fg, NodeGrid cg, const float* __restrict_
     const int zs[2] = {zz >> 1, min((zz + 1) >> 1, cg.nz - 1)};
     const float wx = (x & 1) ? 0.5f : 1.f, wy = (y & 1) ? 0.5f : 1.f, wz = (zz & 1) ? 0.5f : 1.f;
     const int nxp = (x & 1) ? 2 : 1, nyp = (y & 1) ? 2 : 1, nzp = (zz & 1) ? 2 : 1;
-    float s = 0.f;
+    float s[C];
+#pragma unroll
+    for (int q = 0; q < C; ++q) s[q] = 0.f;
 #pragma unroll
     for (int a = 0; a < 2; ++a)
 #pragma unroll
         for (int b = 0; b < 2; ++b)
 #pragma unroll
             for (int c = 0; c < 2; ++c) {
-                const float v = __ldg(zc + nidx(cg, xs[a], ys[b], zs[c]));
-                s += (a < nxp && b < nyp && c < nzp) ? v : 0.f;
+                const int64_t j = nidx(cg, xs[a], ys[b], zs[c]);
+                const bool real = a < nxp && b < nyp && c < nzp;
+#pragma unroll
+                for (int q = 0; q < C; ++q) {
+                    const float v = __ldg(zc + j * C + q);
+                    s[q] += real ? v : 0.f;
+                }
             }
-    if (!masked) z[i] += scale * wx * wy * wz * s;
+    if (!masked) {
+#pragma unroll
+        for (int q = 0; q < C; ++q) z[i * C + q] += scale * wx * wy * wz * s[q];
+    }
 }
 
 // z = omega * dinv * r   (first damped Jacobi step from z = 0)
@@ -131,22 +151,44 @@ using namespace gb;
 
 // Multigrid transfer and smoothing kernels (no reference counterpart; see the file comment).
 // Node grids are given as nodes per axis.  Masks (1 = Dirichlet node) may be null.
+GB_API int gb_mg_restrict_c(int ncomp, int fnx, int fny, int fnz, int cnx, int cny, int cnz, const float* r,
+                            const float* fmask, const float* cmask, float* rc, cudaStream_t stream)
+{
+    GB_REQUIRE(cnx == (fnx + 1) / 2 && cny == (fny + 1) / 2 && cnz == (fnz + 1) / 2, "mg_restrict: grid mismatch");
+    GB_REQUIRE(ncomp == 1 || ncomp == 3, "mg_restrict: 1 or 3 components");
+    NodeGrid fg{fnx, fny, fnz}, cg{cnx, cny, cnz};
+    const int grid = grid1((int64_t)cnx * cny * cnz);
+    if (ncomp == 1)
+        GB_CHECK_CUDA(launch_pdl(k_restrict_fw<1>, grid, 256, 0, stream, fg, cg, r, fmask, cmask, rc));
+    else
+        GB_CHECK_CUDA(launch_pdl(k_restrict_fw<3>, grid, 256, 0, stream, fg, cg, r, fmask, cmask, rc));
+    return GB_OK;
+}
+
+GB_API int gb_mg_prolong_add_c(int ncomp, int fnx, int fny, int fnz, int cnx, int cny, int cnz, const float* zc,
+                               const float* fmask, float scale, float* z, cudaStream_t stream)
+{
+    GB_REQUIRE(cnx == (fnx + 1) / 2 && cny == (fny + 1) / 2 && cnz == (fnz + 1) / 2, "mg_prolong: grid mismatch");
+    GB_REQUIRE(ncomp == 1 || ncomp == 3, "mg_prolong: 1 or 3 components");
+    NodeGrid fg{fnx, fny, fnz}, cg{cnx, cny, cnz};
+    const int grid = grid1((int64_t)fnx * fny * fnz);
+    if (ncomp == 1)
+        GB_CHECK_CUDA(launch_pdl(k_prolong_add<1>, grid, 256, 0, stream, fg, cg, zc, fmask, scale, z));
+    else
+        GB_CHECK_CUDA(launch_pdl(k_prolong_add<3>, grid, 256, 0, stream, fg, cg, zc, fmask, scale, z));
+    return GB_OK;
+}
+
 GB_API int gb_mg_restrict(int fnx, int fny, int fnz, int cnx, int cny, int cnz, const float* r, const float* fmask,
                           const float* cmask, float* rc, cudaStream_t stream)
 {
-    GB_REQUIRE(cnx == (fnx + 1) / 2 && cny == (fny + 1) / 2 && cnz == (fnz + 1) / 2, "mg_restrict: grid mismatch");
-    NodeGrid fg{fnx, fny, fnz}, cg{cnx, cny, cnz};
-    GB_CHECK_CUDA(launch_pdl(k_restrict_fw, grid1((int64_t)cnx * cny * cnz), 256, 0, stream, fg, cg, r, fmask, cmask, rc));
-    return GB_OK;
+    return gb_mg_restrict_c(1, fnx, fny, fnz, cnx, cny, cnz, r, fmask, cmask, rc, stream);
 }
 
 GB_API int gb_mg_prolong_add(int fnx, int fny, int fnz, int cnx, int cny, int cnz, const float* zc,
                              const float* fmask, float scale, float* z, cudaStream_t stream)
 {
-    GB_REQUIRE(cnx == (fnx + 1) / 2 && cny == (fny + 1) / 2 && cnz == (fnz + 1) / 2, "mg_prolong: grid mismatch");
-    NodeGrid fg{fnx, fny, fnz}, cg{cnx, cny, cnz};
-    GB_CHECK_CUDA(launch_pdl(k_prolong_add, grid1((int64_t)fnx * fny * fnz), 256, 0, stream, fg, cg, zc, fmask, scale, z));
-    return GB_OK;
+    return gb_mg_prolong_add_c(1, fnx, fny, fnz, cnx, cny, cnz, zc, fmask, scale, z, stream);
 }
 
 GB_API int gb_mg_jacobi0(int64_t n, float omega, const float* dinv, const float* r, float* z, cudaStream_t stream)

@@ -189,6 +189,8 @@ class LearnedSmoother:
     the plain channels-last layout (features, 4 layers, combine: 6 launches)."""
 
     def __init__(self, net: ConvNet, mg: multigrid.MultigridPreconditioner, coef, backend: str = "tc"):
+        if getattr(mg, "bdim", 1) != 1:
+            raise ValueError("learned smoother: scalar (1x1) hierarchies only")
         lv = mg.levels[0]
         if len(lv.dims) != 3:
             raise ValueError("learned smoother: 3-D grids only")

@@ -41,20 +41,34 @@ class MultigridPreconditioner:
     """z = V(r): symmetric V(1,1)-cycle (damped Jacobi, exact coarsest solve).
 
     Args:
-        A: the fine system (compact BSR, 1x1 fp32, Dirichlet rows already projected).
+        A: the fine system (compact BSR fp32, Dirichlet rows already projected): 1x1 blocks (diffusion) or
+            3x3 blocks (Q1 vec3 linear elasticity).
         geo: the fem.Grid3D / Grid2D it was assembled on.
-        coef: per-cell diffusion coefficient (host array or device tensor).
+        coef: per-cell diffusion coefficient (1x1), or per-cell Young's modulus (3x3; the Lame parameters
+            of every level follow from it and ``poisson``); host array or device tensor.
         faces: Dirichlet faces (default: the whole boundary).
-        omega: Jacobi damping.
+        omega: Jacobi damping: a number for every level, or "auto" for 4 / (3 rho_l) per level with
+            rho_l = rho(D^-1 A_l) estimated by power iteration at set-up.  Default: 0.6 for 1x1 (the
+            Q1 Laplacian has rho ~ 2), "auto" for 3x3 (point Jacobi on Q1 elasticity has a larger rho,
+            where a fixed 0.6 amplifies the high-frequency error it should damp).
         coarsest_nodes: stop coarsening at or below this many nodes.
-        stencil: apply the level operators in 27-point stencil form (else the CSR kernels).
+        stencil: apply the level operators in 27-point stencil form (else the CSR kernels; 1x1 only).
+        poisson: Poisson ratio of the elasticity levels (3x3).
+
+    Vectors of a 3x3 hierarchy hold 3 interleaved components per node; masks are per node.
     """
 
-    def __init__(self, Am: sparse.BsrMatrix, geo, coef, faces=("x-", "x+", "y-", "y+", "z-", "z+"), omega: float = 0.6,
-                 coarsest_nodes: int = 400, max_levels: int = 12, stencil: bool = True):
-        if Am.block_shape != (1, 1) or Am.scalar_type != torch.float32:
-            raise ValueError("multigrid preconditioner: scalar fp32 BSR matrix required")
-        self.omega = float(omega)
+    def __init__(self, Am: sparse.BsrMatrix, geo, coef, faces=("x-", "x+", "y-", "y+", "z-", "z+"), omega=None,
+                 coarsest_nodes: int = 400, max_levels: int = 12, stencil: bool = True, poisson: float = 0.3):
+        if Am.block_shape not in ((1, 1), (3, 3)) or Am.scalar_type != torch.float32:
+            raise ValueError("multigrid preconditioner: fp32 BSR matrix with 1x1 or 3x3 blocks required")
+        self.bdim = Am.block_shape[0]
+        if self.bdim == 3 and geo.dimension != 3:
+            raise ValueError("multigrid preconditioner: 3x3 blocks need a Grid3D (vec3 elasticity)")
+        self.poisson = float(poisson)
+        if omega is None:
+            omega = 0.6 if self.bdim == 1 else "auto"
+        self.omega = omega if omega == "auto" else float(omega)
         self.faces = tuple(faces)
         self.smoother = None  # learned fine-level smoother (set by warp_gb300.learned)
         self.status = A.zeros(1, torch.int32)
@@ -75,11 +89,12 @@ class MultigridPreconditioner:
             nx, ny, nz = cur_geo._dims()
             bits = fem.BoundarySides(cur_geo, self.faces).face_bits()
             N.check(L.gb_grid_boundary_mask(cur_geo.dimension, nx, ny, nz, bits, 1, 1, A.ptr(lv.mask), stream), "mask")
-            lv.dinv = A.empty(lv.n, torch.float32)
-            N.check(L.gb_bsr_inverse_diagonal(N.GB_F32, 1, lv.n, A.ptr(cur_A.offsets), None, A.ptr(cur_A.columns),
+            C = self.bdim
+            lv.dinv = A.empty(lv.n * C, torch.float32)
+            N.check(L.gb_bsr_inverse_diagonal(N.GB_F32, C, lv.n, A.ptr(cur_A.offsets), None, A.ptr(cur_A.columns),
                                               A.ptr(cur_A.values), 0, A.ptr(lv.dinv), stream), "dinv")
-            lv.w = A.zeros(lv.n, torch.float32)
-            lv.t = A.zeros(lv.n, torch.float32)
+            lv.w = A.zeros(lv.n * C, torch.float32)
+            lv.t = A.zeros(lv.n * C, torch.float32)
             levels.append(lv)
             res = cur_geo.res
             if lv.n <= coarsest_nodes or any(r % 2 for r in res) or len(levels) >= max_levels:
@@ -91,20 +106,32 @@ class MultigridPreconditioner:
                 raise NotImplementedError("2-D hierarchy: use Grid3D problems")
             N.check(L.gb_mg_coarsen_cells(fx, fy, fz, A.ptr(cur_coef), A.ptr(ccoef), stream), "coarsen")
             cgeo = fem.Grid3D(res=cres, bounds_lo=cur_geo.bounds_lo, bounds_hi=cur_geo.bounds_hi)
-            space = fem.make_polynomial_space(cgeo, degree=1)
-            cA = fem.integrate(fem.diffusion_form, fields={"u": fem.make_trial(space), "v": fem.make_test(space)},
-                               values={"nu": ccoef}, bsr_options={"construction": "row_compress"})
-            rhs = A.zeros(cgeo.node_count(), torch.float32)
+            if self.bdim == 1:
+                space = fem.make_polynomial_space(cgeo, degree=1)
+                cA = fem.integrate(fem.diffusion_form, fields={"u": fem.make_trial(space), "v": fem.make_test(space)},
+                                   values={"nu": ccoef}, bsr_options={"construction": "row_compress"})
+            else:
+                space = fem.make_polynomial_space(cgeo, degree=1, dtype="vec3")
+                nu = self.poisson
+                lam = (ccoef * (nu / ((1.0 + nu) * (1.0 - 2.0 * nu)))).contiguous()
+                mu = (ccoef * (1.0 / (2.0 * (1.0 + nu)))).contiguous()
+                cA = fem.integrate(fem.linear_elasticity_form,
+                                   fields={"u": fem.make_trial(space), "v": fem.make_test(space)},
+                                   values={"lame": (lam, mu)}, bsr_options={"construction": "row_compress"})
+            rhs = A.zeros(cgeo.node_count() * self.bdim, torch.float32)
             bd = fem.BoundarySides(cgeo, self.faces)
             P = fem.integrate(fem.boundary_projector_form,
                               fields={"u": fem.make_trial(space, bd), "v": fem.make_test(space, bd)}, assembly="nodal")
             fem.project_linear_system(cA, rhs, P)
             cur_geo, cur_A, cur_coef = cgeo, cA, ccoef
+        # damping per level
+        for lv in levels:
+            lv.omega = self._auto_omega(lv) if self.omega == "auto" else self.omega
         # stencil planes of every level above the coarsest
         st_status = A.zeros(len(levels), torch.int32)
         for li, lv in enumerate(levels):
             lv.S = None
-            if stencil and li < len(levels) - 1:
+            if stencil and self.bdim == 1 and li < len(levels) - 1:
                 lv.S = A.empty(int(L.gb_st27_bytes(*lv.dims)) // 4, torch.float32)
                 N.check(L.gb_st27_build(*lv.dims, A.ptr(lv.A.offsets), A.ptr(lv.A.columns), A.ptr(lv.A.values),
                                         A.ptr(lv.S), st_status[li:].data_ptr(), stream), "st27_build")
@@ -116,14 +143,29 @@ class MultigridPreconditioner:
         dense = last.A.numpy_dense()
         last.inv = A.from_numpy(np.linalg.inv(dense).astype(np.float32))
         for lv in levels[1:]:  # right-hand side / correction buffers of the coarse levels
-            lv.rhs = A.zeros(lv.n, torch.float32)
-            lv.sol = A.zeros(lv.n, torch.float32)
+            lv.rhs = A.zeros(lv.n * self.bdim, torch.float32)
+            lv.sol = A.zeros(lv.n * self.bdim, torch.float32)
         self.levels = levels
         torch.cuda.current_stream().synchronize()
 
+    def _auto_omega(self, lv, iters: int = 30) -> float:
+        """4 / (3 rho(D^-1 A)) with rho from power iteration on the level (set-up only)."""
+        g = torch.Generator(device="cuda").manual_seed(7)
+        x = torch.rand(lv.n * self.bdim, device="cuda", generator=g) + 0.5
+        y = torch.empty_like(x)
+        rho = 1.0
+        for _ in range(iters):
+            x /= torch.linalg.vector_norm(x)
+            sparse.bsr_mv(lv.A, x, y)
+            y *= lv.dinv
+            rho = float(torch.linalg.vector_norm(y))
+            x, y = y, x
+        return 4.0 / (3.0 * max(rho, 1e-30))
+
     @property
     def n(self) -> int:
-        return self.levels[0].n
+        """Length of the vectors the preconditioner maps (nodes x components of the fine level)."""
+        return self.levels[0].n * self.bdim
 
     @property
     def kernels_per_apply(self) -> int:
@@ -149,7 +191,8 @@ class MultigridPreconditioner:
         L = N.lib()
         lv = self.levels[li]
         if li == len(self.levels) - 1:
-            N.check(L.gb_dense_mv(N.GB_F32, lv.n, lv.n, A.ptr(lv.inv), r, None, z, 1.0, 0.0, stream), "coarse")
+            m = lv.n * self.bdim
+            N.check(L.gb_dense_mv(N.GB_F32, m, m, A.ptr(lv.inv), r, None, z, 1.0, 0.0, stream), "coarse")
             return
         nxt = self.levels[li + 1]
         w, t = A.ptr(lv.w), A.ptr(lv.t)
@@ -159,34 +202,37 @@ class MultigridPreconditioner:
         if li == 0 and self.smoother is not None:
             self.smoother.launch(stream, r, w)
             if lv.S is not None:
-                N.check(L.gb_st27_apply(0, *lv.dims, A.ptr(lv.S), w, r, None, self.omega, None, t, A.ptr(self.status),
+                N.check(L.gb_st27_apply(0, *lv.dims, A.ptr(lv.S), w, r, None, lv.omega, None, t, A.ptr(self.status),
                                         stream), "residual")
             else:
                 self._csr_residual(lv, w, r, t, stream)
         elif lv.S is not None:
-            N.check(L.gb_st27_apply(1, *lv.dims, A.ptr(lv.S), None, r, A.ptr(lv.dinv), self.omega, w, t,
+            N.check(L.gb_st27_apply(1, *lv.dims, A.ptr(lv.S), None, r, A.ptr(lv.dinv), lv.omega, w, t,
                                     A.ptr(self.status), stream), "jacobi0+residual")
         else:
-            N.check(L.gb_mg_jacobi0(lv.n, self.omega, A.ptr(lv.dinv), r, w, stream), "jacobi0")
+            N.check(L.gb_mg_jacobi0(lv.n * self.bdim, lv.omega, A.ptr(lv.dinv), r, w, stream), "jacobi0")
             self._csr_residual(lv, w, r, t, stream)
         fx, fy, fz = lv.dims
         cx, cy, cz = nxt.dims
         rc, zc = A.ptr(nxt.rhs), A.ptr(nxt.sol)  # the coarse level's own w/t are its work vectors
-        N.check(L.gb_mg_restrict(fx, fy, fz, cx, cy, cz, t, A.ptr(lv.mask), A.ptr(nxt.mask), rc, stream), "restrict")
+        N.check(L.gb_mg_restrict_c(self.bdim, fx, fy, fz, cx, cy, cz, t, A.ptr(lv.mask), A.ptr(nxt.mask), rc, stream),
+                "restrict")
         self._vcycle(li + 1, rc, zc, stream)
-        N.check(L.gb_mg_prolong_add(fx, fy, fz, cx, cy, cz, zc, A.ptr(lv.mask), 1.0, w, stream), "prolong")
+        N.check(L.gb_mg_prolong_add_c(self.bdim, fx, fy, fz, cx, cy, cz, zc, A.ptr(lv.mask), 1.0, w, stream),
+                "prolong")
         # post-smoothing fused with its residual: z = w + omega D^-1 (r - A w)
         if lv.S is not None:
-            N.check(L.gb_st27_apply(2, *lv.dims, A.ptr(lv.S), w, r, A.ptr(lv.dinv), self.omega, None, z,
+            N.check(L.gb_st27_apply(2, *lv.dims, A.ptr(lv.S), w, r, A.ptr(lv.dinv), lv.omega, None, z,
                                     A.ptr(self.status), stream), "smooth")
         else:
-            N.check(L.gb_bsr_jacobi_smooth(1, lv.n, lv.nnz, Am.capacity, A.ptr(Am.offsets), A.ptr(Am.columns),
-                                           A.ptr(Am.values), r, w, A.ptr(lv.dinv), self.omega, z, A.ptr(self.status),
-                                           stream), "smooth")
+            N.check(L.gb_bsr_jacobi_smooth(self.bdim, lv.n, lv.nnz, Am.capacity, A.ptr(Am.offsets),
+                                           A.ptr(Am.columns), A.ptr(Am.values), r, w, A.ptr(lv.dinv), lv.omega, z,
+                                           A.ptr(self.status), stream), "smooth")
 
     def _csr_residual(self, lv, w: int, r: int, t: int, stream) -> None:
         Am = lv.A
-        N.check(N.lib().gb_bsr_mv(1, 1, lv.n, lv.n, lv.nnz, Am.capacity, A.ptr(Am.offsets), None, A.ptr(Am.columns),
+        C = self.bdim
+        N.check(N.lib().gb_bsr_mv(C, C, lv.n, lv.n, lv.nnz, Am.capacity, A.ptr(Am.offsets), None, A.ptr(Am.columns),
                                   A.ptr(Am.values), N.GB_F32, w, r, t, N.GB_F32, -1.0, 1.0, 0, 0, 0, -1,
                                   A.ptr(self.status), stream), "residual")
 

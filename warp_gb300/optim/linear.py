@@ -985,6 +985,9 @@ class RefinedSolver:
                 callback(outer, it, rnorm / bnorm)
             if it == 0:
                 break
+            if not math.isfinite(rnorm) or rnorm > 1e3 * bnorm:
+                # the corrections diverge (e.g. reduced-precision inner values far from the true operator)
+                break
         return x64, dict(outer=outer, inner_iterations=inner_iters, rel_residual=history[-1], history=history,
                          converged=bool(rnorm <= tol * bnorm))
 
