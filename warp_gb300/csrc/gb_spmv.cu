@@ -148,9 +148,10 @@ SpmvShape default_shape(int br, int bc, int val_dtype, int nrow, int64_t nnzb, i
     const int bb = br * bc;
     const int vbytes = (val_dtype == GB_F64) ? 8 : (val_dtype == GB_BF16 ? 2 : 4);
     // Tile shapes measured on GB300 (sweep over lanes per row x rows per tile on the 96^3 Q1
-    // scalar and 64^3 Q1 vector matrices): scalar blocks run best with ~28 KB tiles (two CTAs of
-    // 17 warps per SM, 3-deep rings) and 4 lanes per row; 3x3 blocks with 8 lanes per block row
-    // and ~70 KB tiles (one CTA per SM).  Long rows get more lanes (<= 8 blocks per lane).
+    // scalar and 64^3 / 128^3 Q1 vector matrices): scalar blocks run best with ~28 KB tiles (two CTAs
+    // of 17 warps per SM, 3-deep rings) and 4 lanes per row; 3x3 blocks with ~70-80 KB tiles (one CTA
+    // per SM): 8 lanes per block row at 64 rows (fp32), 4 at 128 rows (bf16).  Long rows get more lanes
+    // (<= 8 blocks per lane).
     int G, rows;
     const double bytes_per_row = std::max(avg, 1.0) * (4.0 + bb * vbytes);
     if (bb == 1) {
@@ -160,7 +161,11 @@ SpmvShape default_shape(int br, int bc, int val_dtype, int nrow, int64_t nnzb, i
     } else {
         rows = 64;
         while (rows > 4 && rows * bytes_per_row * 1.05 > 104 * 1024) rows >>= 1;
-        G = std::max(8, SPMV_CONSUMERS / (rows * 2));
+        // smaller value types (bf16): grow the tile while it stays under ~80 KB; measured on the 128^3
+        // elasticity matrix: bf16 values 128 rows x 4 lanes 294 us against 360 us at 64 x 8
+        // (fp32 values stay at 64 rows x 8 lanes, the best of the same sweep)
+        while (rows < 128 && 2.0 * rows * bytes_per_row * 1.05 <= 80 * 1024) rows <<= 1;
+        G = rows >= 128 ? 4 : std::max(8, SPMV_CONSUMERS / (rows * 2));
     }
     while (G < 32 && avg > 8.0 * G) G <<= 1;
     G = std::min(G, 32);
