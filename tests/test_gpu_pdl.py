@@ -17,18 +17,21 @@ def pdl_switch():
     from warp_gb300 import _native as N
 
     before = N.lib().gb_get_pdl()
-    yield lambda on: N.call("gb_set_pdl", int(on))
+    yield lambda mode: N.call("gb_set_pdl", int(mode))
     N.call("gb_set_pdl", before)
 
 
 def test_pdl_is_on_by_default_and_switchable(cuda, pdl_switch):
     from warp_gb300 import _native as N
 
-    assert N.lib().gb_get_pdl() in (0, 1)
-    pdl_switch(False)
+    assert N.lib().gb_get_pdl() in (0, 1, 2)
+    pdl_switch(0)
     assert N.lib().gb_get_pdl() == 0
-    pdl_switch(True)
+    pdl_switch(2)
+    assert N.lib().gb_get_pdl() == 2
+    pdl_switch(1)
     assert N.lib().gb_get_pdl() == 1
+    assert N.lib().gb_set_pdl(3) != 0  # out of range
 
 
 def _solve(system, method, graph, pdl_switch, on):
@@ -54,16 +57,17 @@ def _solve(system, method, graph, pdl_switch, on):
     return x, info, z
 
 
+@pytest.mark.parametrize("mode", [1, 2])
 @pytest.mark.parametrize("graph", [False, True])
 @pytest.mark.parametrize("method", ["jacobi", "mg", "learned"])
-def test_pdl_results_are_bit_identical(cuda, pdl_switch, method, graph):
-    """Eager launches (graph=False) run with the programmatic-serialization attribute; graph captures
-    stay plain.  Either way the switch must not change a bit."""
+def test_pdl_results_are_bit_identical(cuda, pdl_switch, method, graph, mode):
+    """Mode 1: eager launches (graph=False) run with the programmatic-serialization attribute, graph
+    captures stay plain; mode 2: captures carry it too.  No mode may change a bit."""
     from warp_gb300 import problems
 
     system = problems.diffusion((24, 24, 24), sigma=1.5, corr_length=0.15, seed=4)
-    x_off, info_off, z_off = _solve(system, method, graph, pdl_switch, False)
-    x_on, info_on, z_on = _solve(system, method, graph, pdl_switch, True)
+    x_off, info_off, z_off = _solve(system, method, graph, pdl_switch, 0)
+    x_on, info_on, z_on = _solve(system, method, graph, pdl_switch, mode)
     assert info_on["converged"] and info_off["converged"]
     assert info_on["inner_iterations"] == info_off["inner_iterations"]
     assert torch.equal(x_on, x_off)
