@@ -8,7 +8,7 @@ whose preconditioner is a multigrid V-cycle with the trained conv-net fine-level
 tcgen05 layers), inside FP64 iterative refinement; operator and preconditioner resident in HBM
 (their set-up is timed separately).  The matrix (204 MB of values + columns) is larger than the
 129 MB L2, so no L2 flush is needed between steps.  The same system is also solved by the plain
-Jacobi-CG drop-in (the judge of the learned method) and by flexible CG with the Jacobi-smoothed
+Jacobi-CG drop-in (the method the learned one is measured against) and by flexible CG with the Jacobi-smoothed
 V-cycle (the method without the network).
 
 Printed (rank 0, one JSON line): value = learned-FCG solve time (ms); e2e = the same solve through
@@ -31,6 +31,7 @@ import math
 import os
 import statistics
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -65,7 +66,9 @@ class ClockSampler:
 
     def __init__(self, gpu_index: int = 0):
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        # raw samples: GB_CLOCKS_DIR if set, else the system temporary directory (the summary goes into
+        # the bench line either way)
+        self.path = os.path.join(os.environ.get("GB_CLOCKS_DIR") or tempfile.gettempdir(), f"clocks_{os.getpid()}.csv")
         self.gpu = gpu_index
         self.window = None
 
@@ -613,7 +616,7 @@ def main():
         setup_ms = (time.perf_counter() - s0) * 1e3
     ms, linfos, llaunch, clocks = timed(lsolver, system.b, args.steps, sample_clocks=True)
 
-    # ---- plain Jacobi-CG drop-in (the judge) -------------------------------------------------
+    # ---- plain Jacobi-CG drop-in (the reference method for the speed-up) ----------------------
     M = linear.preconditioner(A, "diag")
     jsolver = linear.RefinedSolver(A, M=M, inner_tol=args.inner_tol)
     jms, jinfos, _, jclocks = timed(jsolver, system.b, args.steps, sample_clocks=True)

@@ -967,7 +967,7 @@ class RefinedSolver:
             if self.method == "fcg":
                 status = int(self.inner._dev_status.item())
                 if status & (N.DEV_STAGNATION | N.DEV_BREAKDOWN | N.DEV_NONFINITE):
-                    # the flexible solve stalled: finish this correction with Jacobi-CG (the judge)
+                    # the flexible solve stalled: finish this correction with plain Jacobi-CG
                     self.fallbacks += 1
                     self._jacobi._tol = self.inner._tol
                     self._jacobi._run_fused(Aop, self._r32, self._d, self._jacobi_M, x_is_zero=False)
