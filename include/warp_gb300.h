@@ -285,6 +285,13 @@ int gb_batched_pcg(int nbatch, const int* batch_offsets, const int* order, int64
                    double atol, int maxiter, int x_is_zero, int threads, int lanes_per_row, int small_rows, int grid,
                    int* iters, float* rr, float* atol_sq, void* workspace, size_t workspace_bytes, int* status,
                    gb_stream_t stream);
+/* Same solve; smem_rows > 0: CTA-mode subproblems of at most smem_rows rows keep p, r, Ap in shared
+ * memory (3 * 4 * smem_rows bytes per CTA, at most 200 KB; results identical to smem_rows = 0). */
+int gb_batched_pcg2(int nbatch, const int* batch_offsets, const int* order, int64_t n, const int* offsets,
+                    const int* columns, const float* values, const float* dinv, const float* b, float* x, double rtol,
+                    double atol, int maxiter, int x_is_zero, int threads, int lanes_per_row, int small_rows,
+                    int smem_rows, int grid, int* iters, float* rr, float* atol_sq, void* workspace,
+                    size_t workspace_bytes, int* status, gb_stream_t stream);
 int gb_q1_batched_assemble_2d(int nbatch, const int* ncell, const int* row_off, const int* nnz_off,
                               const int* cell_off, const float* coef, const float* f, int total_rows, int* offsets,
                               int* columns, float* values, float* rhs, gb_stream_t stream);

@@ -65,7 +65,9 @@ def _batched_residuals(Am, b, x, offs, tol, iters, scale=32.0):
 
 
 @pytest.mark.parametrize("config", [None, {"threads": 256, "lanes_per_row": 1, "small_rows": 0},
-                                    {"threads": 512, "lanes_per_row": 4, "small_rows": 4096}])
+                                    {"threads": 512, "lanes_per_row": 4, "small_rows": 4096},
+                                    {"threads": 256, "lanes_per_row": 2, "small_rows": 0, "smem_rows": 16896},
+                                    {"threads": 512, "lanes_per_row": 1, "small_rows": 0, "smem_rows": 512}])
 def test_batched_cg_each_subproblem_converges(cuda, config):
     """Uneven Q1 subproblems in one launch: every subproblem meets its own tolerance (the reference's
     per-batch check, scale 32 for fp32) and takes the iterations of the same Jacobi-CG run alone
@@ -204,3 +206,28 @@ def test_autotuner_picks_a_candidate_and_caches_it(cuda):
     eager = batched.BatchedCG(Am, offs, M._inv_diag, 1e-6, 0.0, 2000, config=cfg, use_cuda_graph=False)
     eager.solve(b, x2)
     assert torch.equal(x, x2)
+
+
+@pytest.mark.parametrize("lanes", [1, 2, 4])
+def test_batched_shared_vectors_are_bit_identical(cuda, lanes):
+    """Keeping p, r, Ap in shared memory changes where the vectors live, not the arithmetic: the
+    iterates, iteration counts and residuals equal the global-memory solve bit for bit, including a
+    batch where only some subproblems fit."""
+    from warp_gb300 import batched
+    from warp_gb300.optim import linear
+
+    ncells = [16, 3, 40, 8, 25, 12, 2, 33, 20, 6]
+    Am, b, offs = batched.q1_batch_2d(ncells, seed=11)
+    M = linear.preconditioner(Am, "diag")
+    out = {}
+    for sv in (0, 600, 16896):
+        cfg = {"threads": 256, "lanes_per_row": lanes, "small_rows": 0, "smem_rows": sv}
+        s_ = batched.BatchedCG(Am, offs, M._inv_diag, 1e-6, 0.0, 1000, config=cfg)
+        x = torch.zeros_like(b)
+        s_.solve(b, x)
+        torch.cuda.synchronize()
+        assert int(s_.status.item()) == 0
+        out[sv] = (x.clone(), s_.iters.clone(), s_.rr.clone())
+    for sv in (600, 16896):
+        assert torch.equal(out[sv][0], out[0][0]) and torch.equal(out[sv][1], out[0][1])
+        assert torch.equal(out[sv][2], out[0][2])

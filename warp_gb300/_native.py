@@ -105,6 +105,8 @@ _SIGNATURES = {
     "gb_batched_pcg_workspace_bytes": (_c_sz, [_c_i64]),
     "gb_batched_pcg": (_c_int, [_c_int, _vp, _vp, _c_i64, _vp, _vp, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _c_int, _c_int,
                                 _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_sz, _vp, _vp]),
+    "gb_batched_pcg2": (_c_int, [_c_int, _vp, _vp, _c_i64, _vp, _vp, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _c_int,
+                                 _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_sz, _vp, _vp]),
     "gb_multi_dot_workspace_bytes": (_c_sz, [_c_int]),
     "gb_multi_dot": (_c_int, [_c_int, _c_i64, _c_int, _vp, _c_i64, _vp, _vp, _vp, _c_sz, _vp]),
     "gb_multi_axpy": (_c_int, [_c_int, _c_i64, _c_int, _vp, _c_i64, _vp, _c_dbl, _c_dbl, _vp, _vp]),

@@ -25,8 +25,13 @@ from . import _arrays as A
 from . import _native as N
 from . import sparse
 
-DEFAULT_CONFIG = {"threads": 512, "lanes_per_row": 2, "small_rows": 2048}
-CANDIDATES = {"threads": (128, 256, 512), "lanes_per_row": (1, 2, 4), "small_rows": (0, 1024, 4096)}
+DEFAULT_CONFIG = {"threads": 512, "lanes_per_row": 2, "small_rows": 2048, "smem_rows": 0}
+# smem_rows: CTA-mode subproblems of at most this many rows keep p, r, Ap in shared memory (16896 rows =
+# 198 KB: every subproblem of a 128 x 128-cell batch fits, one CTA per SM; 8192: two CTAs per SM).  On
+# the 4096-system workload it measured slower (194-454 ms against 161 ms: one or two CTAs per SM hide
+# the matrix stream's latency worse than eight), so the default candidate set leaves it off.
+CANDIDATES = {"threads": (128, 256, 512), "lanes_per_row": (1, 2, 4), "small_rows": (0, 1024, 4096),
+              "smem_rows": (0,)}
 _TUNED: dict = {}
 
 
@@ -91,10 +96,11 @@ class BatchedCG:
 
     def _launch(self, b: torch.Tensor, x: torch.Tensor, cfg, stream) -> None:
         Am = self.A
-        N.check(N.lib().gb_batched_pcg(
+        N.check(N.lib().gb_batched_pcg2(
             self.nbatch, A.ptr(self.batch_offsets), A.ptr(self.order), self.n, A.ptr(Am.offsets), A.ptr(Am.columns),
             A.ptr(Am.values), A.ptr(self.inv_diag), A.ptr(b), A.ptr(x), self.rtol, self.atol, self.maxiter, 0,
-            int(cfg["threads"]), int(cfg["lanes_per_row"]), int(cfg["small_rows"]), int(cfg.get("grid", 0)),
+            int(cfg["threads"]), int(cfg["lanes_per_row"]), int(cfg["small_rows"]), int(cfg.get("smem_rows", 0)),
+            int(cfg.get("grid", 0)),
             A.ptr(self.iters), A.ptr(self.rr), A.ptr(self.atol_sq), A.ptr(self._ws), self._ws.numel(),
             A.ptr(self.status), stream), "batched_pcg")
         self.launches += 2  # queue reset + the persistent kernel
@@ -138,8 +144,9 @@ def autotune(solver: BatchedCG, b: torch.Tensor, x: torch.Tensor, candidates=Non
     x0 = x.clone()
     best, best_ms = None, float("inf")
     stream = A.stream()
-    for th, lpr, sm in itertools.product(cands["threads"], cands["lanes_per_row"], cands["small_rows"]):
-        cfg = {"threads": th, "lanes_per_row": lpr, "small_rows": sm}
+    for th, lpr, sm, sv in itertools.product(cands["threads"], cands["lanes_per_row"], cands["small_rows"],
+                                             cands.get("smem_rows", (0,))):
+        cfg = {"threads": th, "lanes_per_row": lpr, "small_rows": sm, "smem_rows": sv}
         x.copy_(x0)
         solver._launch(b, x, cfg, stream)  # warm-up (module load, caches)
         times = []
@@ -153,7 +160,7 @@ def autotune(solver: BatchedCG, b: torch.Tensor, x: torch.Tensor, candidates=Non
             times.append(e0.elapsed_time(e1))
         ms = min(times)
         if log:
-            log(f"  threads={th:4d} lanes/row={lpr} small_rows={sm:5d}: {ms:8.3f} ms")
+            log(f"  threads={th:4d} lanes/row={lpr} small_rows={sm:5d} smem_rows={sv:5d}: {ms:8.3f} ms")
         if ms < best_ms:
             best, best_ms = cfg, ms
     x.copy_(x0)

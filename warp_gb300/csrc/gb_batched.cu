@@ -38,6 +38,7 @@ struct BatchArgs {
     int maxiter;
     int x_is_zero;
     int small_rows;
+    int smem_rows;             // CTA-mode subproblems of at most this many rows keep p, r, Ap in shared memory
     int* queue;                // work counter, zero at launch
     int* iters;                // [B]
     float* rr_out;             // [B] final ||r||^2
@@ -74,25 +75,35 @@ __device__ __forceinline__ void warp_allreduce(const float (&in)[NV], double (&o
 }
 
 // One CG of subproblem pid by a group of `nthr` threads (tid in [0, nthr)); WARP: the group is one
-// warp (warp reductions, __syncwarp between phases), else the whole CTA.
-template <int LPR, bool WARP>
-__device__ void solve_one(const BatchArgs& a, int pid, int tid, int nthr, double* red)
+// warp (warp reductions, __syncwarp between phases), else the whole CTA.  SV: p, r and Ap live in
+// `svec` (shared memory, 3 x smem_rows floats, indexed by row - r0): per iteration HBM then carries
+// the matrix, x and D^-1 only; gathers of p stay on chip.  Column indices outside the subproblem's rows
+// (none in a block-diagonal batch) read zero in that mode.
+template <int LPR, bool WARP, bool SV>
+__device__ void solve_one(const BatchArgs& a, int pid, int tid, int nthr, double* red, float* svec)
 {
     const int r0 = a.batch_offsets[pid], r1 = a.batch_offsets[pid + 1];
     const int gid = tid / LPR, sub = tid % LPR;
     const int rows_per_pass = nthr / LPR;
+    // vector p, r, Ap: element of global row i at vp[i - vb]
+    const int vb = SV ? r0 : 0;
+    float* vp = SV ? svec : a.p;
+    float* vr = SV ? svec + a.smem_rows : a.r;
+    float* vAp = SV ? svec + 2 * a.smem_rows : a.Ap;
+    const unsigned nloc = (unsigned)(r1 - r0);
     auto sync = [&]() {
         if (WARP)
             __syncwarp();
         else
             __syncthreads();
     };
-    // A v on this group's rows; returns (per thread) the partial sum of w[row] * (A v)[row] and
-    // stores (A v) into out (sub-lane 0 only); residual: out = b - A v.  Two rows per group per
-    // pass, and each row's nonzeros of this lane are loaded as one predicated batch of U, so a lane
-    // keeps 2 U column / value loads and then 2 U gathers in flight instead of walking a chain.
+    // A v on this group's rows (v indexed from vbase); returns (per thread) the partial sum of
+    // w[row] * (A v)[row] and stores (A v) into out (sub-lane 0 only; out and w indexed from vb);
+    // residual: out = b - A v.  Two rows per group per pass, and each row's nonzeros of this lane are
+    // loaded as one predicated batch of U, so a lane keeps 2 U column / value loads and then 2 U
+    // gathers in flight instead of walking a chain.
     constexpr int U = LPR == 1 ? 9 : (LPR == 2 ? 5 : (LPR == 4 ? 3 : 2));
-    auto matvec = [&](const float* v, float* out, const float* w, bool residual) -> float {
+    auto matvec = [&](const float* v, int vbase, bool v_local, float* out, const float* w, bool residual) -> float {
         float part = 0.f;
         for (int base = r0; base < r1; base += 2 * rows_per_pass) {
             int row[2], k1[2], kb[2];
@@ -120,7 +131,13 @@ __device__ void solve_one(const BatchArgs& a, int pid, int tid, int nthr, double
 #pragma unroll
                 for (int h = 0; h < 2; ++h)
 #pragma unroll
-                    for (int u = 0; u < U; ++u) xv[h][u] = cc[h][u] >= 0 ? v[cc[h][u]] : 0.f;
+                    for (int u = 0; u < U; ++u) {
+                        const int c = cc[h][u];
+                        if (v_local)
+                            xv[h][u] = (unsigned)(c - r0) < nloc ? v[c - vbase] : 0.f;
+                        else
+                            xv[h][u] = c >= 0 ? v[c - vbase] : 0.f;
+                    }
 #pragma unroll
                 for (int h = 0; h < 2; ++h) {
 #pragma unroll
@@ -133,8 +150,8 @@ __device__ void solve_one(const BatchArgs& a, int pid, int tid, int nthr, double
                 const float sh = group_sum<LPR>(s[h]);
                 if (row[h] < r1 && sub == 0) {
                     const float o = residual ? a.b[row[h]] - sh : sh;
-                    out[row[h]] = o;
-                    if (w) part += w[row[h]] * o;
+                    out[row[h] - vb] = o;
+                    if (w) part += w[row[h] - vb] * o;
                 }
             }
         }
@@ -145,17 +162,17 @@ __device__ void solve_one(const BatchArgs& a, int pid, int tid, int nthr, double
     if (a.x_is_zero) {
         for (int i = r0 + tid; i < r1; i += nthr) {
             a.x[i] = 0.f;
-            a.r[i] = a.b[i];
+            vr[i - vb] = a.b[i];
         }
     } else {
-        matvec(a.x, a.r, nullptr, true);
+        matvec(a.x, 0, false, vr, nullptr, true);
     }
     sync();
     float part3[3] = {0.f, 0.f, 0.f};
     for (int i = r0 + tid; i < r1; i += nthr) {
-        const float ri = a.r[i], bi = a.b[i];
+        const float ri = vr[i - vb], bi = a.b[i];
         const float zi = a.dinv ? a.dinv[i] * ri : ri;
-        a.p[i] = zi;
+        vp[i - vb] = zi;
         part3[0] += bi * bi;
         part3[1] += ri * ri;
         part3[2] += ri * zi;
@@ -173,7 +190,7 @@ __device__ void solve_one(const BatchArgs& a, int pid, int tid, int nthr, double
     bool broke = false;
     while (it < a.maxiter && rr > atol_sq) {
         // ---- A p and p.Ap ----------------------------------------------------------------------
-        float part1[1] = {matvec(a.p, a.Ap, a.p, false)};
+        float part1[1] = {matvec(vp, vb, SV, vAp, vp, false)};
         double pAp[1];
         if (WARP)
             warp_allreduce<1>(part1, pAp);
@@ -189,10 +206,10 @@ __device__ void solve_one(const BatchArgs& a, int pid, int tid, int nthr, double
         float part2[2] = {0.f, 0.f};
 #pragma unroll 4
         for (int i = r0 + tid; i < r1; i += nthr) {
-            const float pi = a.p[i];
+            const float pi = vp[i - vb];
             a.x[i] += alpha * pi;
-            const float ri = a.r[i] - alpha * a.Ap[i];
-            a.r[i] = ri;
+            const float ri = vr[i - vb] - alpha * vAp[i - vb];
+            vr[i - vb] = ri;
             const float zi = a.dinv ? a.dinv[i] * ri : ri;
             part2[0] += ri * ri;
             part2[1] += ri * zi;
@@ -210,9 +227,9 @@ __device__ void solve_one(const BatchArgs& a, int pid, int tid, int nthr, double
         // ---- p = z + beta p --------------------------------------------------------------------
 #pragma unroll 4
         for (int i = r0 + tid; i < r1; i += nthr) {
-            const float ri = a.r[i];
+            const float ri = vr[i - vb];
             const float zi = a.dinv ? a.dinv[i] * ri : ri;
-            a.p[i] = zi + beta * a.p[i];
+            vp[i - vb] = zi + beta * vp[i - vb];
         }
         sync();
         rr = tot2[0];
@@ -231,6 +248,7 @@ __device__ void solve_one(const BatchArgs& a, int pid, int tid, int nthr, double
 template <int LPR>
 __global__ void __launch_bounds__(512) k_batched_pcg(const BatchArgs a)
 {
+    extern __shared__ __align__(16) float svec[];  // 3 * smem_rows floats (p, r, Ap) when enabled
     __shared__ double red[32 * 3];
     __shared__ int s_item;
     for (;;) {
@@ -242,7 +260,10 @@ __global__ void __launch_bounds__(512) k_batched_pcg(const BatchArgs a)
         const int pid = a.order[item];
         const int nrows = a.batch_offsets[pid + 1] - a.batch_offsets[pid];
         if (nrows > a.small_rows) {
-            solve_one<LPR, false>(a, pid, threadIdx.x, blockDim.x, red);
+            if (nrows <= a.smem_rows)
+                solve_one<LPR, false, true>(a, pid, threadIdx.x, blockDim.x, red, svec);
+            else
+                solve_one<LPR, false, false>(a, pid, threadIdx.x, blockDim.x, red, nullptr);
             continue;
         }
         // from here on every subproblem is small (the queue is ordered by size): one warp each
@@ -255,7 +276,7 @@ __global__ void __launch_bounds__(512) k_batched_pcg(const BatchArgs a)
                 cur = __shfl_sync(0xffffffffu, got, 0);
             }
             if (cur >= a.nbatch) break;
-            solve_one<LPR, true>(a, a.order[cur], lane, 32, nullptr);
+            solve_one<LPR, true, false>(a, a.order[cur], lane, 32, nullptr, nullptr);
             cur = -1;
         }
         return;
@@ -335,14 +356,18 @@ GB_API size_t gb_batched_pcg_workspace_bytes(int64_t n) { return 3 * sizeof(floa
 // Persistent batched Jacobi-CG (see the file comment).  n: total rows (inactive tail included);
 // dinv may be null (no preconditioner); x is read as the initial guess unless x_is_zero;
 // threads in {128, 256, 512}; lanes_per_row in {1, 2, 4, 8}; small_rows: subproblems of at most
-// this many rows are solved by one warp.  iters / rr / atol_sq: per-subproblem results (device).
+// this many rows are solved by one warp; smem_rows: larger subproblems of at most this many rows keep
+// their CG vectors p, r, Ap in shared memory (3 * 4 * smem_rows bytes per CTA; 0 = off).
+// iters / rr / atol_sq: per-subproblem results (device).
 
-GB_API int gb_batched_pcg(int nbatch, const int* batch_offsets, const int* order, int64_t n, const int* offsets,
-                          const int* columns, const float* values, const float* dinv, const float* b, float* x,
-                          double rtol, double atol, int maxiter, int x_is_zero, int threads, int lanes_per_row,
-                          int small_rows, int grid, int* iters, float* rr, float* atol_sq, void* workspace,
-                          size_t workspace_bytes, int* status, cudaStream_t stream)
+GB_API int gb_batched_pcg2(int nbatch, const int* batch_offsets, const int* order, int64_t n, const int* offsets,
+                           const int* columns, const float* values, const float* dinv, const float* b, float* x,
+                           double rtol, double atol, int maxiter, int x_is_zero, int threads, int lanes_per_row,
+                           int small_rows, int smem_rows, int grid, int* iters, float* rr, float* atol_sq,
+                           void* workspace, size_t workspace_bytes, int* status, cudaStream_t stream)
 {
+    GB_REQUIRE(smem_rows >= 0 && (size_t)smem_rows * 3 * sizeof(float) <= 200 * 1024,
+               "batched_pcg: smem_rows must be in [0, %d]", (int)(200 * 1024 / (3 * sizeof(float))));
     GB_REQUIRE(nbatch >= 0 && n >= 0, "batched_pcg: negative sizes");
     GB_REQUIRE(threads == 128 || threads == 256 || threads == 512, "batched_pcg: threads must be 128, 256 or 512");
     GB_REQUIRE(workspace_bytes >= gb_batched_pcg_workspace_bytes(n), "batched_pcg: workspace too small");
@@ -369,27 +394,45 @@ GB_API int gb_batched_pcg(int nbatch, const int* batch_offsets, const int* order
     a.maxiter = maxiter;
     a.x_is_zero = x_is_zero;
     a.small_rows = small_rows;
+    a.smem_rows = smem_rows;
     a.iters = iters;
     a.rr_out = rr;
     a.atol_sq_out = atol_sq;
     a.status = status;
+    void (*kern)(const BatchArgs) = nullptr;
+    switch (lanes_per_row) {
+    case 1: kern = k_batched_pcg<1>; break;
+    case 2: kern = k_batched_pcg<2>; break;
+    case 4: kern = k_batched_pcg<4>; break;
+    case 8: kern = k_batched_pcg<8>; break;
+    default: gb::set_error("batched_pcg: lanes_per_row must be 1, 2, 4 or 8"); return GB_ERR_INVALID;
+    }
+    const size_t smem = (size_t)smem_rows * 3 * sizeof(float);
+    GB_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     if (grid <= 0) {
-        int dev = 0, sms = kSmCount;
+        int dev = 0, sms = kSmCount, per_sm = 1;
         GB_CHECK_CUDA(cudaGetDevice(&dev));
         GB_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        grid = sms * std::max(1, 2048 / threads);
+        GB_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
+        grid = sms * std::max(1, std::min(per_sm, 2048 / threads));
     }
     grid = std::min(grid, nbatch);
     GB_CHECK_CUDA(cudaMemsetAsync(a.queue, 0, sizeof(int), stream));
-    switch (lanes_per_row) {
-    case 1: k_batched_pcg<1><<<grid, threads, 0, stream>>>(a); break;
-    case 2: k_batched_pcg<2><<<grid, threads, 0, stream>>>(a); break;
-    case 4: k_batched_pcg<4><<<grid, threads, 0, stream>>>(a); break;
-    case 8: k_batched_pcg<8><<<grid, threads, 0, stream>>>(a); break;
-    default: gb::set_error("batched_pcg: lanes_per_row must be 1, 2, 4 or 8"); return GB_ERR_INVALID;
-    }
+    kern<<<grid, threads, smem, stream>>>(a);
     GB_CHECK_CUDA(cudaGetLastError());
     return GB_OK;
+}
+
+// The same solve with global-memory work vectors only (smem_rows = 0).
+GB_API int gb_batched_pcg(int nbatch, const int* batch_offsets, const int* order, int64_t n, const int* offsets,
+                          const int* columns, const float* values, const float* dinv, const float* b, float* x,
+                          double rtol, double atol, int maxiter, int x_is_zero, int threads, int lanes_per_row,
+                          int small_rows, int grid, int* iters, float* rr, float* atol_sq, void* workspace,
+                          size_t workspace_bytes, int* status, cudaStream_t stream)
+{
+    return gb_batched_pcg2(nbatch, batch_offsets, order, n, offsets, columns, values, dinv, b, x, rtol, atol, maxiter,
+                           x_is_zero, threads, lanes_per_row, small_rows, 0, grid, iters, rr, atol_sq, workspace,
+                           workspace_bytes, status, stream);
 }
 
 // Batched 2-D Q1 assembly (see k_q1_batched_2d): ncell[B] cells per side, row_off / nnz_off / cell_off
