@@ -30,6 +30,7 @@
 // copies and MMAs (bounded) and frees its TMEM before returning.
 #include "gb_bulk.cuh"
 #include "gb_common.cuh"
+#include "gb_spmv.cuh"  // sm_count()
 
 namespace gb {
 
@@ -590,18 +591,17 @@ GB_API int gb_conv3_fwd_tc(int nx, int ny, int nz, int last, const void* in, con
     c.mask = mask;
     c.omega = omega;
     c.status = status;
-    int dev = 0, sms = kSmCount, per_sm = 1;
-    GB_CHECK_CUDA(cudaGetDevice(&dev));
-    GB_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    if (last) {
-        GB_CHECK_CUDA(cudaFuncSetAttribute(k_conv3_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        GB_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3_tc<true>, TC_THREADS, smem));
-    } else {
-        GB_CHECK_CUDA(cudaFuncSetAttribute(k_conv3_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        GB_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3_tc<false>, TC_THREADS, smem));
+    // one-time per process: the largest dynamic shared memory either variant may use
+    static bool attr_set = false;
+    if (!attr_set) {
+        GB_CHECK_CUDA(cudaFuncSetAttribute(k_conv3_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)TC_SMEM_LIMIT));
+        GB_CHECK_CUDA(cudaFuncSetAttribute(k_conv3_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)TC_SMEM_LIMIT));
+        attr_set = true;
     }
-    per_sm = 1;  // one CTA per SM: it holds all 512 TMEM columns
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(c.nitems, (int64_t)sms * per_sm));
+    // one CTA per SM: it holds all 512 TMEM columns
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(c.nitems, (int64_t)sm_count()));
     if (last)
         GB_CHECK_CUDA(launch_pdl(k_conv3_tc<true>, grid, TC_THREADS, smem, stream, c));
     else

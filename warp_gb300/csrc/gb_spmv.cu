@@ -121,7 +121,11 @@ static int launch_mv(int nrow, SpmvShape sh, const int* offsets, const int* row_
     const size_t smem = spmv_smem_bytes<BR, BC, VT>(sh.rows, sh.cap, sh.stages);
     finalize_shape(sh, nrow, smem, offsets);
     auto kern = k_bsr_mv<BR, BC, VT, XT, AT>;
-    if (smem > 48 * 1024) GB_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    static size_t attr_bytes = 48 * 1024;  // per instantiation: raise the limit only when a launch needs more
+    if (smem > attr_bytes) {
+        GB_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr_bytes = smem;
+    }
     GB_CHECK_CUDA(launch_pdl(kern, sh.grid, SPMV_THREADS, smem, stream, nrow, sh, offsets, row_counts, columns,
                              (const VT*)values, (const XT*)x, (const XT*)y_in, (XT*)y_out, (AT)alpha, (AT)beta, status));
     return GB_OK;
@@ -336,14 +340,19 @@ GB_API int gb_bsr_jacobi_smooth(int bdim, int nrow, int64_t nnz, int64_t ncap, c
     size_t smem = (bdim == 1) ? spmv_smem_bytes<1, 1, float>(sh.rows, sh.cap, sh.stages)
                               : spmv_smem_bytes<3, 3, float>(sh.rows, sh.cap, sh.stages);
     finalize_shape(sh, nrow, smem, offsets);
+    static size_t attr_bytes[2] = {48 * 1024, 48 * 1024};  // raised only when a launch needs more
     if (bdim == 1) {
-        if (smem > 48 * 1024)
+        if (smem > attr_bytes[0]) {
             GB_CHECK_CUDA(cudaFuncSetAttribute(k_bsr_smooth<1, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            attr_bytes[0] = smem;
+        }
         GB_CHECK_CUDA(launch_pdl(k_bsr_smooth<1, float>, sh.grid, SPMV_THREADS, smem, stream, nrow, sh, offsets,
                                  columns, values, z, r, dinv, omega, z_out, status));
     } else {
-        if (smem > 48 * 1024)
+        if (smem > attr_bytes[1]) {
             GB_CHECK_CUDA(cudaFuncSetAttribute(k_bsr_smooth<3, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            attr_bytes[1] = smem;
+        }
         GB_CHECK_CUDA(launch_pdl(k_bsr_smooth<3, float>, sh.grid, SPMV_THREADS, smem, stream, nrow, sh, offsets,
                                  columns, values, z, r, dinv, omega, z_out, status));
     }

@@ -26,6 +26,7 @@
 //                  mode 2: z = w + omega D^-1 (r - A w)               (Jacobi step fused with residual)
 #include "gb_bulk.cuh"
 #include "gb_common.cuh"
+#include "gb_spmv.cuh"  // sm_count()
 
 namespace gb {
 
@@ -169,10 +170,7 @@ static int st27_grid(int64_t n) { return (int)std::max<int64_t>(1, std::min<int6
 
 static int st27_apply_grid(int64_t n)
 {
-    int dev = 0, sms = kSmCount;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(n, ST_TILE), (int64_t)sms * ST_CTAS_PER_SM));
+    return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(n, ST_TILE), (int64_t)sm_count() * ST_CTAS_PER_SM));
 }
 
 }  // namespace gb
@@ -211,16 +209,20 @@ GB_API int gb_st27_apply(int mode, int nx, int ny, int nz, const float* S, const
     const St27Grid g{nx, ny, nz, (int64_t)nx * ny * nz};
     GB_REQUIRE(g.n < (int64_t(1) << 31), "st27_apply: grid too large");
     const int grid = st27_apply_grid(g.n);
-    if (mode == 0) {
+    static bool attr_set = false;  // one-time per process
+    if (!attr_set) {
         GB_CHECK_CUDA(cudaFuncSetAttribute(k_st27_apply<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ST_SMEM));
+        GB_CHECK_CUDA(cudaFuncSetAttribute(k_st27_apply<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ST_SMEM));
+        GB_CHECK_CUDA(cudaFuncSetAttribute(k_st27_apply<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ST_SMEM));
+        attr_set = true;
+    }
+    if (mode == 0) {
         GB_CHECK_CUDA(launch_pdl(k_st27_apply<0>, grid, ST_TILE, ST_SMEM, stream, g, S, w, r, dinv, omega, w_out, out,
                                  status));
     } else if (mode == 1) {
-        GB_CHECK_CUDA(cudaFuncSetAttribute(k_st27_apply<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ST_SMEM));
         GB_CHECK_CUDA(launch_pdl(k_st27_apply<1>, grid, ST_TILE, ST_SMEM, stream, g, S, w, r, dinv, omega, w_out, out,
                                  status));
     } else if (mode == 2) {
-        GB_CHECK_CUDA(cudaFuncSetAttribute(k_st27_apply<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ST_SMEM));
         GB_CHECK_CUDA(launch_pdl(k_st27_apply<2>, grid, ST_TILE, ST_SMEM, stream, g, S, w, r, dinv, omega, w_out, out,
                                  status));
     } else {
