@@ -103,9 +103,11 @@ def test_conv3_bf16_tensor_core_matches_oracle(cuda, dims, cout, relu):
 
 
 # (64, 40, 40) and (300, 10, 10): more work items (columns x slabs) than CTAs, so CTAs walk several
-# x-slabs and cross column boundaries in their shared-memory ring of x-plane blocks
+# x-slabs and cross column boundaries in their shared-memory ring of x-plane blocks; (160, 4, 300) and
+# (160, 3, 450): long z rows shrink the ring to 5 and to the minimum of 4 slots, and CTAs walk
+# several slabs through them
 @pytest.mark.parametrize("dims", [(1, 1, 1), (2, 4, 16), (7, 9, 11), (9, 7, 35), (33, 17, 20), (20, 12, 97),
-                                  (64, 40, 40), (300, 10, 10)])
+                                  (64, 40, 40), (300, 10, 10), (160, 4, 300), (160, 3, 450)])
 def test_conv3_tcgen05_layer_matches_oracle(cuda, dims):
     """tcgen05 implicit-GEMM layer on the planar padded layout: equal to the oracle on bf16-rounded
     operands up to output rounding; border rows stay zero; no device status raised."""
