@@ -14,7 +14,6 @@ caches the winner per batch layout.
 
 from __future__ import annotations
 
-import ctypes
 import hashlib
 import itertools
 

@@ -9,7 +9,6 @@ runs in the sm_103a library ``libwarp_gb300.so``.
 
 from __future__ import annotations
 
-import ctypes
 from typing import Any
 
 import numpy as np
