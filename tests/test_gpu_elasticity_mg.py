@@ -103,7 +103,8 @@ def test_elasticity_mg_fcg_beats_jacobi_cg(cuda, values):
 def test_refined_solver_stops_when_reduced_precision_corrections_diverge(cuda):
     """bf16 inner values on a rough lognormal field (sigma 1.5, correlation length 0.05) make the inner
     operator indefinite at its smallest eigenvalues: the outer residual grows, and the refined solve
-    stops and reports non-convergence instead of running its outer steps out."""
+    stops (the first correction makes the true residual over 100x worse) and reports non-convergence
+    instead of running its outer steps out."""
     from warp_gb300 import multigrid
     from warp_gb300.optim import linear
 
@@ -116,7 +117,7 @@ def test_refined_solver_stops_when_reduced_precision_corrections_diverge(cuda):
     sol = linear.RefinedSolver(A, M=mg, method="fcg", inner_tol=1e-5, inner_maxiter=3000,
                                inner_values=A.values[:nnz].to(torch.bfloat16).contiguous())
     _, info = sol.solve(s.b, tol=1e-8)
-    assert not info["converged"] and info["outer"] <= 4, info["history"]
+    assert not info["converged"] and info["outer"] <= 2, info["history"]
     # the same solve with FP32 inner values converges
     sol32 = linear.RefinedSolver(A, M=mg, method="fcg", inner_tol=1e-5, inner_maxiter=3000)
     _, info32 = sol32.solve(s.b, tol=1e-8)

@@ -978,6 +978,7 @@ class RefinedSolver:
                     "update_solution")
             self.kernel_launches += 1
             inner_iters += it
+            prev = rnorm
             rnorm, _ = self.residual(x64, b)
             outer += 1
             history.append(rnorm / bnorm)
@@ -985,8 +986,9 @@ class RefinedSolver:
                 callback(outer, it, rnorm / bnorm)
             if it == 0:
                 break
-            if not math.isfinite(rnorm) or rnorm > 1e3 * bnorm:
-                # the corrections diverge (e.g. reduced-precision inner values far from the true operator)
+            if not math.isfinite(rnorm) or rnorm > 100.0 * prev:
+                # the correction made the true residual 100x worse: the corrections diverge (e.g.
+                # reduced-precision inner values far from the true operator)
                 break
         return x64, dict(outer=outer, inner_iterations=inner_iters, rel_residual=history[-1], history=history,
                          converged=bool(rnorm <= tol * bnorm))
