@@ -36,10 +36,10 @@ const char* gb_last_error(void);
 void gb_clear_error(void);
 int gb_version(void);
 
-/* Programmatic dependent launch of the eagerly launched solver-loop kernels (default on; launches
- * into a capturing stream stay plain).  No reference counterpart:
- * a launch option of this library; results are identical either way. */
-int gb_set_pdl(int enabled);
+/* Programmatic dependent launch of the solver-loop kernels: mode 0 off, 1 (default) eager launches only,
+ * 2 eager launches and launches into a capturing stream.  No reference counterpart: a launch option of
+ * this library; results are identical in every mode.  Returns nonzero for a mode outside 0..2. */
+int gb_set_pdl(int mode);
 int gb_get_pdl(void);
 int gb_device_arch(void);
 
