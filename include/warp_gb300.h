@@ -49,11 +49,12 @@ size_t gb_scan_i32_workspace_bytes(int64_t n);
 int gb_scan_i32(const int* in, int* out, int64_t n, int inclusive, void* workspace, size_t workspace_bytes,
                 gb_stream_t stream);
 
-/* Allocation-free variant of gb_scan_i32 (no counterpart in the reference): for callers that must
- * not allocate device memory (a host arena owning all device memory, or offsets built during a
- * stream capture).  Its scratch is a fixed ~256 KB device array inside the library, shared by all
- * calls: n <= gb_scan_i32_noalloc_max_n() (2^28) or GB_ERR_CAPACITY; calls that overlap on the GPU
- * race on the array; the first call on a device looks the array up (make it outside a capture). */
+/* Allocation-free variant of gb_scan_i32 (no counterpart in the reference): for callers that cannot
+ * allocate device memory at all (a host application whose own arena owns all device memory and that
+ * lets no library call cudaMalloc).  Its scratch is a fixed ~256 KB device array inside the library,
+ * held by every GPU that loads it and shared by all calls: n <= gb_scan_i32_noalloc_max_n() (2^28) or
+ * GB_ERR_CAPACITY; calls that overlap on the GPU race on the array.  The first call in a CUDA context
+ * looks the array's address up (make that call before any stream capture). */
 int64_t gb_scan_i32_noalloc_max_n(void);
 int gb_scan_i32_noalloc(const int* in, int* out, int64_t n, int inclusive, gb_stream_t stream);
 
@@ -215,8 +216,8 @@ int gb_st27_apply(int mode, int nx, int ny, int nz, const float* S, const float*
                   float omega, float* w_out, float* out, int* status, gb_stream_t stream);
 /* 3x3x3 convolutions on a node grid, channels-last activations act[v][C], v = (x*ny + y)*nz + z,
  * weights W[t][ci][co] (t = 9(dx+1) + 3(dy+1) + (dz+1)), zero padding.  fp32 training kernels
- * (gb_conv3_bwd_weight_f32 accumulates into gW, deterministic), Adam, and the bf16 tensor-core
- * forward (Wt[t][co][16] bf16, cout 16 or 8, fp32 accumulation). */
+ * (gb_conv3_bwd_weight_f32 accumulates into gW, deterministic), Adam, features and the combine step
+ * of the training forward. */
 int gb_conv3_fwd_f32(int nx, int ny, int nz, int cin, int cout, const float* in, const float* W, int relu, float* out,
                      gb_stream_t stream);
 int gb_conv3_bwd_data_f32(int nx, int ny, int nz, int cin, int cout, const float* gout, const float* W, float* gin,
@@ -233,8 +234,6 @@ int gb_net_cell_features(int nx, int ny, int nz, const float* cell_coef, float m
                          gb_stream_t stream);
 int gb_net_combine(int dtype, int64_t n, int stride, const void* act, const float* mask, float omega, const float* dinv,
                    const float* r, float* out, gb_stream_t stream);
-int gb_conv3_fwd_bf16(int nx, int ny, int nz, int cout, int relu, const void* in, const void* Wt, void* out,
-                      gb_stream_t stream);
 /* tcgen05 implicit-GEMM layers on the planar padded layout: the grid padded by one zero voxel per side,
  * row p = ((x+1)(ny+2) + (y+1))(nz+2) + (z+1), channels 0-7 in plane 0 and 8-15 in plane 1 (16 B per row),
  * planes gb_conv3_planar_rows() rows apart, border rows zero.  last = 0: ReLU layer, planar bf16 out;

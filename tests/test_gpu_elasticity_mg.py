@@ -117,8 +117,17 @@ def test_refined_solver_stops_when_reduced_precision_corrections_diverge(cuda):
     sol = linear.RefinedSolver(A, M=mg, method="fcg", inner_tol=1e-5, inner_maxiter=3000,
                                inner_values=A.values[:nnz].to(torch.bfloat16).contiguous())
     _, info = sol.solve(s.b, tol=1e-8)
-    assert not info["converged"] and info["outer"] <= 2, info["history"]
+    assert not info["converged"] and info["diverged"] and info["outer"] <= 2, info["history"]
+    # the iterate returned is the last accepted one, not the one a diverging correction made
+    assert info["rel_residual"] <= info["history"][0] * (1 + 1e-9), info["history"]
     # the same solve with FP32 inner values converges
     sol32 = linear.RefinedSolver(A, M=mg, method="fcg", inner_tol=1e-5, inner_maxiter=3000)
-    _, info32 = sol32.solve(s.b, tol=1e-8)
-    assert info32["converged"] and info32["rel_residual"] <= 1e-8
+    x32, info32 = sol32.solve(s.b, tol=1e-8)
+    assert info32["converged"] and info32["rel_residual"] <= 1e-8 and not info32["diverged"]
+    # warm start from a good solution: the bf16 corrections cannot improve it; the solve must stop
+    # without running its outer steps out and hand back an iterate no worse than the start
+    x0 = x32.clone()
+    xw, infow = sol.solve(s.b, x64=x0, tol=1e-12, max_outer=50)
+    assert not infow["converged"] and infow["outer"] < 10, infow["history"]
+    assert infow["rel_residual"] <= infow["history"][0] * (1 + 1e-6) or infow["rel_residual"] <= 1e-8, \
+        infow["history"]

@@ -98,7 +98,6 @@ _SIGNATURES = {
     "gb_net_features": (_c_int, [_c_int, _c_i64, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gb_net_cell_features": (_c_int, [_c_int, _c_int, _c_int, _vp, ctypes.c_float, ctypes.c_float, _vp, _vp]),
     "gb_net_combine": (_c_int, [_c_int, _c_i64, _c_int, _vp, _vp, ctypes.c_float, _vp, _vp, _vp, _vp]),
-    "gb_conv3_fwd_bf16": (_c_int, [_c_int] * 5 + [_vp, _vp, _vp, _vp]),
     "gb_conv3_planar_rows": (_c_i64, [_c_int] * 3),
     "gb_net_features_planar": (_c_int, [_c_int] * 3 + [_vp, _vp, _vp, _vp, _vp, _vp]),
     "gb_conv3_fwd_tc": (_c_int, [_c_int] * 4 + [_vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_float, _vp, _vp]),

@@ -35,9 +35,10 @@ GB_API void gb_clear_error(void) { gb::g_last_error[0] = 0; }
 GB_API int gb_version(void) { return 100; }  // 1.0.0
 
 // Programmatic dependent launch of the solver-loop kernels (multigrid transfers and smoothing,
-// SpMV, Krylov updates, conv-net layers): on by default.  Off launches the same kernels with plain
-// stream ordering.  Takes effect for eager launches made after the call; launches into a capturing
-// stream are plain either way.
+// SpMV, Krylov updates, conv-net layers).  Mode 0: every launch uses plain stream ordering.
+// Mode 1 (default): eager launches carry the programmatic-serialization attribute, launches into a
+// capturing stream stay plain.  Mode 2: both eager launches and launches into a capturing stream
+// carry it.  Takes effect for launches made after the call; results are identical in every mode.
 GB_API int gb_set_pdl(int mode)
 {
     GB_REQUIRE(mode >= 0 && mode <= 2, "set_pdl: mode must be 0, 1 or 2");

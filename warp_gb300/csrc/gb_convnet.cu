@@ -9,11 +9,8 @@
 //
 // Training (fp32, CUDA cores): k_conv_fwd_f32, k_conv_bwd_data_f32 (gradient w.r.t. the input =
 // correlation with the flipped, transposed kernel), k_conv_bwd_weight_f32 (per-CTA partial sums
-// reduced in a fixed order: deterministic), ReLU backward and Adam.  Inference (bf16 operands,
-// fp32 accumulation): k_conv_fwd_bf16_mma, an implicit GEMM on the tensor cores -- a CTA owns a
-// 2 x 4 x 16 voxel brick, stages its halo (4 x 6 x 18 voxels x 16 channels, swizzled so that
-// ldmatrix reads are bank-conflict free) and the layer's weights in shared memory, and each warp
-// accumulates 32 voxels x 16 output channels over the 27 taps with m16n8k16 MMAs.
+// reduced in a fixed order: deterministic), ReLU backward and Adam.  Inference runs on the tcgen05
+// tensor cores (gb_conv_tc.cu).
 #include "gb_common.cuh"
 
 namespace gb {
@@ -255,121 +252,6 @@ __global__ void k_net_combine(int64_t n, int stride, const T* __restrict__ act, 
     }
 }
 
-// ---------------------------------------------------------------------------------------------
-// bf16 tensor-core forward (m16n8k16, fp32 accumulation)
-// ---------------------------------------------------------------------------------------------
-constexpr int BX = 2, BY = 4, BZ = 16;                         // brick of 128 voxels
-constexpr int HX = BX + 2, HY = BY + 2, HZ = BZ + 2;           // halo 4 x 6 x 18
-constexpr int HVOX = HX * HY * HZ;                             // 432 voxels, 32 B each
-
-// shared-memory byte offset of 16-byte chunk h (0/1) of halo voxel hv, swizzled: chunk h of voxel
-// hv lives in slot h ^ ((hv >> 2) & 1), so the 8 rows of an ldmatrix phase (8 consecutive z, 32 B
-// apart) cover all 32 banks.
-__device__ __forceinline__ uint32_t halo_off(int hv, int h) { return (uint32_t)(hv * 32 + ((h ^ ((hv >> 2) & 1)) << 4)); }
-
-__device__ __forceinline__ void ldmatrix_x4(uint32_t addr, uint32_t& r0, uint32_t& r1, uint32_t& r2, uint32_t& r3)
-{
-    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0, %1, %2, %3}, [%4];"
-                 : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
-                 : "r"(addr));
-}
-
-__device__ __forceinline__ void mma_bf16_16816(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
-                                               uint32_t b0, uint32_t b1)
-{
-    asm volatile(
-        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
-        "{%0, %1, %2, %3};"
-        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
-        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
-}
-
-// in: [V][16] bf16; Wt: [27][cout][16] bf16 (co-major, ci contiguous); out: [V][cout_store] bf16
-// (cout = 16 with ReLU for hidden layers; cout = 8 for the last layer, only channel 0 meaningful).
-template <int COUT, bool RELU>
-__global__ __launch_bounds__(128) void k_conv_fwd_bf16_mma(Grid3 g, const __nv_bfloat16* __restrict__ in,
-                                                           const __nv_bfloat16* __restrict__ Wt,
-                                                           __nv_bfloat16* __restrict__ out)
-{
-    __shared__ __align__(128) unsigned char s_halo[HVOX * 32];
-    __shared__ __align__(16) __nv_bfloat16 s_w[27 * COUT * CN];
-    const int bx = blockIdx.x, by = blockIdx.y, bz = blockIdx.z;
-    const int x0 = bx * BX, y0 = by * BY, z0 = bz * BZ;
-    // stage weights
-    for (int i = threadIdx.x; i < 27 * COUT * CN / 8; i += blockDim.x)
-        reinterpret_cast<uint4*>(s_w)[i] = reinterpret_cast<const uint4*>(Wt)[i];
-    // stage the halo brick (zero outside the grid)
-    for (int i = threadIdx.x; i < HVOX * 2; i += blockDim.x) {
-        const int hv = i >> 1, h = i & 1;
-        const int hz = hv % HZ, hy = (hv / HZ) % HY, hx = hv / (HZ * HY);
-        const int x = x0 + hx - 1, y = y0 + hy - 1, z = z0 + hz - 1;
-        uint4 val = make_uint4(0u, 0u, 0u, 0u);
-        if (x >= 0 && y >= 0 && z >= 0 && x < g.nx && y < g.ny && z < g.nz)
-            val = reinterpret_cast<const uint4*>(in + (((int64_t)x * g.ny + y) * g.nz + z) * CN)[h];
-        *reinterpret_cast<uint4*>(s_halo + halo_off(hv, h)) = val;
-    }
-    __syncthreads();
-
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t halo_base = static_cast<uint32_t>(__cvta_generic_to_shared(s_halo));
-    // warp w owns the two z-lines (hx = 1 + w/2, hy = 1 + 2*(w%2) + {0, 1}) of the brick
-    const int lx = warp >> 1;
-    float acc[2][COUT / 8][4];
-#pragma unroll
-    for (int m = 0; m < 2; ++m)
-#pragma unroll
-        for (int nt = 0; nt < COUT / 8; ++nt)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) acc[m][nt][q] = 0.f;
-    // ldmatrix.x4 row assignment: lanes 0-15 -> rows 0-15 of chunk 0, lanes 16-31 -> rows 0-15 of chunk 1
-    const int arow = lane & 15, achunk = lane >> 4;
-#pragma unroll 1
-    for (int t = 0; t < 27; ++t) {
-        const int dx = t / 9 - 1, dy = (t / 3) % 3 - 1, dz = t % 3 - 1;
-        // B fragments for this tap: b0,b1 = W[t][co = n0 + lane/4][ci = 2*(lane%4) .. +1 and +8 ..]
-        uint32_t b[COUT / 8][2];
-#pragma unroll
-        for (int nt = 0; nt < COUT / 8; ++nt) {
-            const __nv_bfloat16* wrow = s_w + ((size_t)t * COUT + nt * 8 + (lane >> 2)) * CN;
-            b[nt][0] = *reinterpret_cast<const uint32_t*>(wrow + 2 * (lane & 3));
-            b[nt][1] = *reinterpret_cast<const uint32_t*>(wrow + 8 + 2 * (lane & 3));
-        }
-#pragma unroll
-        for (int m = 0; m < 2; ++m) {
-            const int ly = 2 * (warp & 1) + m;
-            const int hv = ((1 + lx + dx) * HY + (1 + ly + dy)) * HZ + (1 + arow + dz);
-            uint32_t a0, a1, a2, a3;
-            ldmatrix_x4(halo_base + halo_off(hv, achunk), a0, a1, a2, a3);
-            // x4 order: (rows 0-7, k 0-7), (rows 8-15, k 0-7), (rows 0-7, k 8-15), (rows 8-15, k 8-15)
-#pragma unroll
-            for (int nt = 0; nt < COUT / 8; ++nt) mma_bf16_16816(acc[m][nt], a0, a1, a2, a3, b[nt][0], b[nt][1]);
-        }
-    }
-    // epilogue: c0,c1 -> (row lane/4, cols 2*(lane%4), +1); c2,c3 -> row + 8
-#pragma unroll
-    for (int m = 0; m < 2; ++m) {
-        const int ly = 2 * (warp & 1) + m;
-        const int x = x0 + lx, y = y0 + ly;
-        if (x >= g.nx || y >= g.ny) continue;
-#pragma unroll
-        for (int half = 0; half < 2; ++half) {
-            const int z = z0 + (lane >> 2) + 8 * half;
-            if (z >= g.nz) continue;
-            const int64_t v = ((int64_t)x * g.ny + y) * g.nz + z;
-#pragma unroll
-            for (int nt = 0; nt < COUT / 8; ++nt) {
-                float c0 = acc[m][nt][2 * half], c1 = acc[m][nt][2 * half + 1];
-                if (RELU) {
-                    c0 = fmaxf(c0, 0.f);
-                    c1 = fmaxf(c1, 0.f);
-                }
-                *reinterpret_cast<__nv_bfloat162*>(out + v * COUT + nt * 8 + 2 * (lane & 3)) =
-                    __floats2bfloat162_rn(c0, c1);
-            }
-        }
-    }
-}
-
 static int g1(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(n, 256), kSmCount * 16)); }
 
 }  // namespace gb
@@ -480,32 +362,6 @@ GB_API int gb_net_combine(int dtype, int64_t n, int stride, const void* act, con
     else
         k_net_combine<__nv_bfloat16><<<g1(n), 256, 0, stream>>>(n, stride, static_cast<const __nv_bfloat16*>(act), mask,
                                                                 omega, dinv, r, out);
-    GB_CHECK_CUDA(cudaGetLastError());
-    return GB_OK;
-}
-
-// bf16 tensor-core layer: cout 16 (hidden, ReLU) or 8 (last layer, linear).
-// in [V][16] bf16, Wt [27][cout][16] bf16 (16-byte aligned), out [V][cout] bf16.
-GB_API int gb_conv3_fwd_bf16(int nx, int ny, int nz, int cout, int relu, const void* in, const void* Wt, void* out,
-                             cudaStream_t stream)
-{
-    GB_REQUIRE(((uintptr_t)in % 16 == 0) && ((uintptr_t)Wt % 16 == 0) && ((uintptr_t)out % 4 == 0),
-               "conv3_fwd_bf16: misaligned arrays");
-    Grid3 g{nx, ny, nz};
-    dim3 grid(ceil_div(nx, BX), ceil_div(ny, BY), ceil_div(nz, BZ));
-    const __nv_bfloat16* i = static_cast<const __nv_bfloat16*>(in);
-    const __nv_bfloat16* w = static_cast<const __nv_bfloat16*>(Wt);
-    __nv_bfloat16* o = static_cast<__nv_bfloat16*>(out);
-    if (cout == 16 && relu)
-        k_conv_fwd_bf16_mma<16, true><<<grid, 128, 0, stream>>>(g, i, w, o);
-    else if (cout == 16)
-        k_conv_fwd_bf16_mma<16, false><<<grid, 128, 0, stream>>>(g, i, w, o);
-    else if (cout == 8 && !relu)
-        k_conv_fwd_bf16_mma<8, false><<<grid, 128, 0, stream>>>(g, i, w, o);
-    else {
-        gb::set_error("conv3_fwd_bf16: cout must be 16 (hidden) or 8 (last layer, linear)");
-        return GB_ERR_UNSUPPORTED;
-    }
     GB_CHECK_CUDA(cudaGetLastError());
     return GB_OK;
 }

@@ -12,6 +12,7 @@ namespace gb {
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_IPT = 16;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_IPT;
+static_assert(SCAN_TILE == kScanTileElems, "gb_scan.cuh tile size out of date");
 
 // Exclusive block scan of one int per thread; returns the block total in *total.
 __device__ __forceinline__ int block_exclusive_scan(int v, int* s_warp, int* total)

@@ -11,8 +11,8 @@ where c_k is the normalised log-coefficient of the k-th cell adjacent to the nod
 positively homogeneous: N(s r) = s N(r) for s > 0, and no residual normalisation is needed).  The
 last layer starts at zero, so an untrained network is exactly the Jacobi-smoothed V-cycle.
 
-Inference: bf16 weights and activations, fp32 accumulation on the tensor cores
-(``gb_conv3_fwd_bf16``).  Training: fp32 forward / backward / Adam kernels (``gb_conv3_*_f32``,
+Inference: bf16 weights and activations, fp32 accumulation on the tcgen05 tensor cores
+(``gb_conv3_fwd_tc``).  Training: fp32 forward / backward / Adam kernels (``gb_conv3_*_f32``,
 ``gb_adam_step``), loss = ||e - V(r)||_A^2 / ||e||_A^2 over (residual, error) pairs with r = A e,
 back-propagated through the rest of the V-cycle with the cycle's own transposed pieces:
     z = (I - w D^-1 A)(I - P Vc R A) w + ...   =>   g_w = (I - A P Vc R)(I - w A D^-1) g_z
@@ -84,7 +84,7 @@ class ConvNet:
         net.step_count = int(d["steps"])
         return net
 
-    def bf16_weights(self, last_cout: int = 8) -> list[torch.Tensor]:
+    def bf16_weights(self, last_cout: int = 16) -> list[torch.Tensor]:
         """Inference layout Wt[t][co_pad][ci] bf16 (co padded to ``last_cout`` for the last layer)."""
         out = []
         for (ci, co, _), w in zip(LAYERS, self.W):
@@ -184,9 +184,8 @@ def padded_rows(dims, device) -> torch.Tensor:
 class LearnedSmoother:
     """The inference smoother plugged into ``MultigridPreconditioner.smoother``.
 
-    backend "tc": tcgen05 implicit-GEMM layers on the planar padded layout (features + 4 layers, the
-    last one fused with the Jacobi step: 5 launches); backend "mma": the legacy mma.sync layers on
-    the plain channels-last layout (features, 4 layers, combine: 6 launches)."""
+    tcgen05 implicit-GEMM layers on the planar padded layout (features + 4 layers, the last one fused
+    with the Jacobi step: 5 launches)."""
 
     def __init__(self, net: ConvNet, mg: multigrid.MultigridPreconditioner, coef, backend: str = "tc"):
         if getattr(mg, "bdim", 1) != 1:
@@ -194,8 +193,8 @@ class LearnedSmoother:
         lv = mg.levels[0]
         if len(lv.dims) != 3:
             raise ValueError("learned smoother: 3-D grids only")
-        if backend not in ("tc", "mma"):
-            raise ValueError(f"unknown backend {backend!r}")
+        if backend != "tc":
+            raise ValueError(f"unknown backend {backend!r} (the tcgen05 layers are the only inference path)")
         self.backend = backend
         self.mg = mg
         self.dims = lv.dims
@@ -205,39 +204,23 @@ class LearnedSmoother:
         self.status = mg.status
         coef_t = coef if isinstance(coef, torch.Tensor) else A.from_numpy(np.asarray(coef, np.float32).reshape(-1))
         self.chat = cell_features(self.dims, coef_t.reshape(-1).float().contiguous(), net.mean_log, net.inv_std)
-        if backend == "tc":
-            self.Wt = net.bf16_weights(last_cout=16)
-            rows = planar_rows(self.dims)
-            self.buf = [A.zeros(2 * rows * 8, torch.bfloat16), A.zeros(2 * rows * 8, torch.bfloat16)]
-            self.kernels_per_apply = 5
-        else:
-            self.Wt = net.bf16_weights(last_cout=8)
-            self.buf = [A.empty(self.n * CH, torch.bfloat16), A.empty(self.n * CH, torch.bfloat16)]
-            self.kernels_per_apply = 6
+        self.Wt = net.bf16_weights(last_cout=16)
+        rows = planar_rows(self.dims)
+        self.buf = [A.zeros(2 * rows * 8, torch.bfloat16), A.zeros(2 * rows * 8, torch.bfloat16)]
+        self.kernels_per_apply = 5
 
     def launch(self, stream, r: int, w: int) -> None:
         L = N.lib()
-        if self.backend == "tc":
-            N.check(L.gb_net_features_planar(*self.dims, r, A.ptr(self.dinv), A.ptr(self.chat), A.ptr(self.mask),
-                                             A.ptr(self.buf[0]), stream), "features")
-            src, dst = self.buf[0], self.buf[1]
-            for li, wt in enumerate(self.Wt):
-                last = li == len(self.Wt) - 1
-                N.check(L.gb_conv3_fwd_tc(*self.dims, int(last), A.ptr(src), A.ptr(wt), None if last else A.ptr(dst),
-                                          w if last else None, r if last else None, A.ptr(self.dinv) if last else None,
-                                          A.ptr(self.mask) if last else None, self.omega, A.ptr(self.status), stream),
-                        "conv tc")
-                src, dst = dst, src
-            return
-        N.check(L.gb_net_features(N.GB_BF16, self.n, r, A.ptr(self.dinv), A.ptr(self.chat), A.ptr(self.mask),
-                                  A.ptr(self.buf[0]), stream), "features")
+        N.check(L.gb_net_features_planar(*self.dims, r, A.ptr(self.dinv), A.ptr(self.chat), A.ptr(self.mask),
+                                         A.ptr(self.buf[0]), stream), "features")
         src, dst = self.buf[0], self.buf[1]
-        for (ci, co, relu), wt in zip(LAYERS, self.Wt):
-            cop = 16 if co == 16 else 8
-            N.check(L.gb_conv3_fwd_bf16(*self.dims, cop, int(relu), A.ptr(src), A.ptr(wt), A.ptr(dst), stream), "conv")
+        for li, wt in enumerate(self.Wt):
+            last = li == len(self.Wt) - 1
+            N.check(L.gb_conv3_fwd_tc(*self.dims, int(last), A.ptr(src), A.ptr(wt), None if last else A.ptr(dst),
+                                      w if last else None, r if last else None, A.ptr(self.dinv) if last else None,
+                                      A.ptr(self.mask) if last else None, self.omega, A.ptr(self.status), stream),
+                    "conv tc")
             src, dst = dst, src
-        N.check(L.gb_net_combine(N.GB_BF16, self.n, 8, A.ptr(src), A.ptr(self.mask), self.omega, A.ptr(self.dinv), r, w,
-                                 stream), "combine")
 
 
 class TrainingSmoother:

@@ -854,6 +854,35 @@ def bicgstab(A_, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, ch
 # -------------------------------------------------------------------------------------------
 # FP64 iterative refinement around the fused FP32 Krylov solver
 # -------------------------------------------------------------------------------------------
+class _DivergenceGuard:
+    """Decides when iterative refinement's corrections diverge, from the true residual norms.
+
+    ``step(rnorm)`` after each correction returns "ok", "save" (the residual grew: the caller keeps
+    the iterate before this correction), "undo" (stop; take this correction back) or "restore"
+    (stop; go back to the iterate saved at the previous "save").  Stops on a non-finite residual, a
+    residual over 100x the previous one or over 1e3 x max(||b||, initial residual), and on two
+    corrections in a row that each made the residual grow.
+    """
+
+    def __init__(self, r0: float, bnorm: float):
+        self.prev = r0
+        self.cap = 1e3 * max(bnorm, r0)
+        self.grew = False
+
+    def step(self, rnorm: float) -> str:
+        prev, self.prev = self.prev, rnorm
+        bad = not math.isfinite(rnorm) or rnorm > 100.0 * prev or rnorm > self.cap
+        if rnorm > prev or bad:
+            if self.grew:
+                return "restore"
+            if bad:
+                return "undo"
+            self.grew = True
+            return "save"
+        self.grew = False
+        return "ok"
+
+
 class RefinedSolver:
     """Mixed-precision solve: FP32 Jacobi-PCG (or BiCGSTAB) inner loop inside iterative refinement.
 
@@ -912,6 +941,7 @@ class RefinedSolver:
         self._norms = A.zeros(2, torch.float64)
         self._status = A.zeros(1, torch.int32)
         self._host = torch.zeros(2, dtype=torch.float64, pin_memory=True)
+        self._x_backup = None
         self.kernel_launches = 0
 
     def residual(self, x64: torch.Tensor, b: torch.Tensor, sync: bool = True):
@@ -955,6 +985,8 @@ class RefinedSolver:
         history.append(rnorm / bnorm if bnorm > 0 else 0.0)
         outer = 0
         Aop = self.inner._A
+        guard = _DivergenceGuard(rnorm, bnorm)
+        diverged = False
         while bnorm > 0 and rnorm > tol * bnorm and outer < max_outer:
             # ask the correction solve only for the reduction still missing (never below inner_tol)
             need = 0.25 * tol * bnorm / rnorm
@@ -978,20 +1010,36 @@ class RefinedSolver:
                     "update_solution")
             self.kernel_launches += 1
             inner_iters += it
-            prev = rnorm
             rnorm, _ = self.residual(x64, b)
             outer += 1
             history.append(rnorm / bnorm)
             if callback is not None:
                 callback(outer, it, rnorm / bnorm)
+            verdict = guard.step(rnorm)
+            if verdict == "save":
+                # this correction made the residual grow: keep the iterate before it, in case the
+                # next one grows too
+                if self._x_backup is None:
+                    self._x_backup = torch.empty_like(x64)
+                torch.sub(x64, self._d.to(torch.float64), out=self._x_backup)
+            elif verdict in ("undo", "restore"):
+                # the corrections diverge (e.g. reduced-precision inner values far from the true
+                # operator): return the last accepted iterate, not the one the bad correction made
+                if verdict == "undo":
+                    N.check(L.gb_update_solution(self.n, A.ptr(x64), A.ptr(self._x2), A.ptr(self._d), -1.0,
+                                                 A.stream()), "undo_solution")
+                else:
+                    x64.copy_(self._x_backup)
+                    N.check(L.gb_update_solution(self.n, A.ptr(x64), A.ptr(self._x2), None, 0.0, A.stream()),
+                            "restore_solution")
+                rnorm, _ = self.residual(x64, b)
+                history.append(rnorm / bnorm)
+                diverged = True
+                break
             if it == 0:
                 break
-            if not math.isfinite(rnorm) or rnorm > 100.0 * prev:
-                # the correction made the true residual 100x worse: the corrections diverge (e.g.
-                # reduced-precision inner values far from the true operator)
-                break
         return x64, dict(outer=outer, inner_iterations=inner_iters, rel_residual=history[-1], history=history,
-                         converged=bool(rnorm <= tol * bnorm))
+                         converged=bool(rnorm <= tol * bnorm), diverged=diverged)
 
 
 def solve_refined(A_: sparse.BsrMatrix, b, x64=None, tol: float = 1e-8, M=None, method: str = "cg",
