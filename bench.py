@@ -52,6 +52,16 @@ def _peaks():
         return 6800.0, "fallback"
 
 
+def _tensor_peak():
+    """Dense bf16 tensor peak (TFLOP/s) for a kernel timed alone: the measured burst figure."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["bf16_tflops"]), "measured (burst)"
+    except Exception:
+        return 1900.0, "fallback"
+
+
 class ClockSampler:
     """nvidia-smi clock/throttle sampling around the timed region.
 
@@ -264,6 +274,19 @@ def bench_assembly(args, system, hbm_peak):
                     "construction (no global sort); host-to-device copy of the coefficient field included"}
 
 
+def _oracle_residual_3x3(A, b, x):
+    """||b - A x|| / ||b|| in FP64 on the host (oracle BSR product of the fp32 3x3 blocks)."""
+    import numpy as np
+
+    import oracle
+
+    nnz = A.nnz_sync()
+    r = b.cpu().numpy().astype(np.float64) - oracle.bsr_mv_f64(
+        A.offsets.cpu().numpy(), A.columns[:nnz].cpu().numpy(), A.values[:nnz].cpu().numpy().reshape(-1),
+        x.cpu().numpy().astype(np.float64), block_shape=(3, 3))
+    return float(np.linalg.norm(r) / np.linalg.norm(b.cpu().numpy().astype(np.float64)))
+
+
 def bench_elasticity(args, hbm_peak):
     """64^3 Q1 vec3 elasticity (E lognormal sigma=1 i.i.d., nu=0.3, gravity, x=0 clamped): 3x3 bsr_mv
     bandwidth and the refined Jacobi-CG solve to 1e-8."""
@@ -282,10 +305,12 @@ def bench_elasticity(args, hbm_peak):
     mv_bytes = nnz * (36 + 4) + (A.nrow + 1) * 4 + 2 * n * 4
     solver = linear.RefinedSolver(A, M=linear.preconditioner(A, "diag"), inner_tol=args.inner_tol)
     solver.solve(s.b, tol=1e-8)
-    infos = []
+    infos, xs = [], []
 
     def step():
-        infos.append(solver.solve(s.b, tol=1e-8)[1])
+        x_, info_ = solver.solve(s.b, tol=1e-8)
+        infos.append(info_)
+        xs.append(x_)
 
     ms = _event_ms(step, 2, warmup=0)
     # bf16 storage of the matrix values for the FP32 inner loop (the FP64 residual keeps fp32 values)
@@ -300,7 +325,7 @@ def bench_elasticity(args, hbm_peak):
             "bsr_mv_us": mv_ms * 1e3, "bsr_mv_gbs": mv_bytes / (mv_ms * 1e-3) / 1e9,
             "bsr_mv_frac_of_hbm": mv_bytes / (mv_ms * 1e-3) / 1e9 / hbm_peak,
             "jacobi_cg_refined_ms": ms, "inner_iterations": infos[-1]["inner_iterations"],
-            "rel_residual": infos[-1]["rel_residual"]}
+            "rel_residual": infos[-1]["rel_residual"], "oracle_rel_residual": _oracle_residual_3x3(A, s.b, xs[-1])}
 
 
 def bench_elasticity_large(args, hbm_peak):
@@ -370,9 +395,16 @@ def bench_elasticity_large(args, hbm_peak):
            "mg_omega": [round(lv.omega, 4) for lv in mg.levels]}
     solver = linear.RefinedSolver(A, M=mg, method="fcg", inner_tol=args.inner_tol, inner_maxiter=5000)
     solver.solve(s.b, tol=1e-8, max_outer=10)
-    infos = []
-    ms = _event_ms(lambda: infos.append(solver.solve(s.b, tol=1e-8, max_outer=10)[1]), 2, warmup=0)
+    infos, xs = [], []
+
+    def solve_once():
+        x_, info_ = solver.solve(s.b, tol=1e-8, max_outer=10)
+        infos.append(info_)
+        xs.append(x_)
+
+    ms = _event_ms(solve_once, 2, warmup=0)
     out["mg_fcg_fp32_ms"] = ms
+    out["mg_fcg_fp32_oracle_rel_residual"] = _oracle_residual_3x3(A, s.b, xs[-1])
     out["mg_fcg_fp32_inner_iterations"] = infos[-1]["inner_iterations"]
     out["mg_fcg_fp32_outer_iterations"] = infos[-1]["outer"]
     out["mg_fcg_fp32_rel_residual"] = infos[-1]["rel_residual"]
@@ -390,18 +422,13 @@ def run_reference(args):
     if rank != 0:
         return 0
     import numpy as np
-    import torch
 
     import oracle
-    from warp_gb300 import problems
+    from oracle import fem_q1
 
-    system = problems.diffusion(args.res, sigma=1.5, corr_length=0.1, seed=args.seed)
-    A = system.A
-    nnz = A.nnz_sync()
-    off = A.offsets.cpu().numpy()
-    cols = A.columns[:nnz].cpu().numpy()
-    vals = A.values[:nnz].cpu().numpy()
-    b = system.b.cpu().numpy()
+    # the system is built on the host by the oracle (FP64 stencil assembly, Dirichlet projection):
+    # the same workload as the GPU arm's, without the product library
+    off, cols, vals, b = fem_q1.diffusion_system_3d(tuple(args.res), sigma=1.5, corr_length=0.1, seed=args.seed)
     dinv = oracle.inverse_diagonal_f32(off, cols, vals)
     threads = oracle.max_threads()
     # each step is one complete FP64 Jacobi-PCG solve to 1e-8 relative residual (about 0.5 s on 16
@@ -421,7 +448,9 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "ms", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": value, "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "parallelism": "replicas"},
+        "config": {"workload": WORKLOAD, "parallelism": "replicas",
+                   "input": "system built on the host by the oracle (FP64 stencil assembly + Dirichlet projection, "
+                            "oracle/fem_q1.py); the product library is not loaded"},
         "cpu_baseline": {"value": value, "unit": "ms", "cores": threads, "kind": "port",
                          "sample": f"one full FP64 Jacobi-PCG solve of the same 96^3 system per step on {threads} "
                                    f"threads ({iters[-1]} iterations, rel. residual {rels[-1]:.2e})"},
@@ -586,8 +615,9 @@ def main():
         launches0 = solver.kernel_launches
         w0 = datetime.datetime.now()
         e0.record(stream)
+        xlast = None
         for _ in range(steps):
-            _, info = solver.solve(b, tol=1e-8)
+            xlast, info = solver.solve(b, tol=1e-8)
             infos.append(info)
         e1.record(stream)
         torch.cuda.synchronize()
@@ -599,6 +629,7 @@ def main():
         if sampler:
             sampler.__exit__(None, None, None)
         ms_ = _barrier_max(e0.elapsed_time(e1) / steps, ws)
+        solver.last_x = xlast.cpu().numpy()  # outside the timed region: checked against the oracle below
         return ms_, infos, launches, (sampler.summary() if sampler else None)
 
     # ---- learned preconditioner: set-up (timed separately) and the headline solve -------------
@@ -674,6 +705,8 @@ def main():
     del mv_graph
     mv_bytes = nnz * (4 + 4) + (n + 1) * 4 + n * 4 + n * 4
     mv_gbs = mv_bytes / mv_s / 1e9
+    # fused Jacobi-PCG iteration: the SpMV (beta = 0) and 48 B of vector traffic per row
+    jit_bytes = mv_bytes + 48 * n
     # the same number of bytes moved by a plain device copy (read + write = mv_bytes): the bandwidth a
     # single launch of this size reaches (ramp-up and tail included), for context beside the peak
     cbuf = torch.empty(mv_bytes // 8, dtype=torch.float32, device="cuda")
@@ -747,6 +780,47 @@ def main():
     e2e_setup_ms = (time.perf_counter() - t0) * 1e3 / max(1, min(args.steps, 3))
     h2d_setup = off_h.numel() * 4 + col_h.numel() * 4 + val_h.numel() * 4 + coef_h.numel() * 4 + n * 4
 
+    # ---- one hidden tcgen05 conv layer alone (tensor-core roofline of the smoother's kernel) ------
+    import warp_gb300._native as N
+
+    dims = lmg.levels[0].dims
+    csrc = sm.buf[0]
+    cdst = torch.zeros_like(csrc)
+    cst = torch.zeros(1, dtype=torch.int32, device="cuda")
+
+    def conv_layer():
+        N.check(N.lib().gb_conv3_fwd_tc(*dims, 0, csrc.data_ptr(), sm.Wt[1].data_ptr(), cdst.data_ptr(), None, None,
+                                        None, None, 0.0, cst.data_ptr(), stream.cuda_stream), "conv layer")
+
+    conv_ms = _event_ms(conv_layer, 20, warmup=3)
+    conv_flop = 2.0 * 27 * 16 * 16 * n  # useful MACs x 2 of one 16 -> 16 layer over the node grid
+    conv_tflops = conv_flop / (conv_ms * 1e-3) / 1e12
+    tensor_peak, tensor_peak_kind = _tensor_peak()
+    assert int(cst.item()) == 0
+    del cdst
+
+    # ---- FP64 oracle checks of the solutions (outside every timed region) -----------------------
+    import oracle
+
+    off_np = A.offsets.cpu().numpy()
+    col_np = A.columns[:nnz].cpu().numpy()
+    val_np = A.values[:nnz].cpu().numpy()
+    b_np = system.b.cpu().numpy().astype(np.float64)
+    threads = oracle.max_threads()
+    t0 = time.perf_counter()
+    x_ref, ref_it, ref_rel = oracle.pcg_f64(off_np, col_np, val_np, b_np.astype(np.float32),
+                                            inv_diag=oracle.inverse_diagonal_f32(off_np, col_np, val_np), tol=1e-12,
+                                            maxiter=20000, nthreads=threads)
+    ref_s = time.perf_counter() - t0
+
+    def oracle_check(xs):
+        r = b_np - oracle.bsr_mv_f64(off_np, col_np, val_np, xs)
+        return {"oracle_rel_residual": float(np.linalg.norm(r) / np.linalg.norm(b_np)),
+                "oracle_rel_error": float(np.linalg.norm(xs - x_ref) / np.linalg.norm(x_ref))}
+
+    oracle_solve = {"method": "oracle FP64 Jacobi-PCG (oracle.pcg_f64) on the same fp32 matrix", "tol": 1e-12,
+                    "iterations": ref_it, "rel_residual": ref_rel, "seconds": ref_s, "threads": threads}
+
     inner_iters = [i["inner_iterations"] for i in linfos]
     outer = [i["outer"] for i in linfos]
     # counted by the solver: residuals, argument stores, FCG inits, solution updates, and per FCG
@@ -793,16 +867,25 @@ def main():
                            "d2h_bytes_per_step": d2h, "timing": "host wall clock, synchronised"},
         "gpu_launches": gpu_launches,
         "clocks": clocks,
+        "roofline_conv": {"bound": "tensor", "kernel": "k_conv3_tc<false> (one 16->16 hidden layer, 97^3 nodes)",
+                          "achieved": conv_tflops, "peak": tensor_peak, "unit": "TFLOP/s",
+                          "frac": conv_tflops / tensor_peak, "peak_kind": tensor_peak_kind,
+                          "algorithmic_flop": conv_flop, "launch_us": conv_ms * 1e3,
+                          "timing": "CUDA events on the launching stream around 20 launches after 3 warm-up"},
+        "oracle_solve": oracle_solve,
         "learned_fcg": {"ms": ms, "inner_iterations": statistics.median(inner_iters),
                         "outer_iterations": statistics.median(outer),
                         "rel_residual": max(i["rel_residual"] for i in linfos), "fallbacks": lsolver.fallbacks,
-                        "setup_ms": setup_ms, "speedup_vs_jacobi_cg": jms / ms},
+                        "setup_ms": setup_ms, "speedup_vs_jacobi_cg": jms / ms, **oracle_check(lsolver.last_x)},
         "jacobi_cg": {"ms": jms, "inner_iterations": statistics.median([i["inner_iterations"] for i in jinfos]),
                       "outer_iterations": statistics.median([i["outer"] for i in jinfos]),
-                      "rel_residual": max(i["rel_residual"] for i in jinfos), "clocks": jclocks},
+                      "rel_residual": max(i["rel_residual"] for i in jinfos), "clocks": jclocks,
+                      "iteration_frac_of_hbm": (jit_bytes * statistics.median([i["inner_iterations"] for i in jinfos])
+                                                / (jms * 1e-3) / 1e9 / hbm_peak),
+                      "iteration_bytes": jit_bytes, **oracle_check(jsolver.last_x)},
         "mg_fcg_no_net": {"ms": fcg_ms, "inner_iterations": statistics.median([f["inner_iterations"] for f in finfos]),
                           "rel_residual": max(f["rel_residual"] for f in finfos), "fallbacks": fsolver.fallbacks,
-                          "setup_ms": mg_setup_ms},
+                          "setup_ms": mg_setup_ms, **oracle_check(fsolver.last_x)},
         "conv_net": {"smoother_us": smoother_us, "launches": sm.kernels_per_apply, "useful_tflops": net_tflops,
                      "backend": "tcgen05 kind::f16 bf16 x bf16 -> fp32"},
         "bsr_mv_gbs": mv_gbs,

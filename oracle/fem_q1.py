@@ -196,3 +196,81 @@ def project_dense(Adense: np.ndarray, b: np.ndarray, mask: np.ndarray, fixed: np
     b2 = (I - P) @ (b - Adense @ (P @ f)) + P @ f
     A2 = (I - P) @ Adense @ (I - P) + P
     return A2, b2
+
+
+# ---------------------------------------------------------------------------------------------
+# Whole systems for the CPU baseline (the --impl reference arm of bench.py builds its input here,
+# without the product library)
+# ---------------------------------------------------------------------------------------------
+def gaussian_random_field(shape, corr_length: float, sigma: float, seed: int) -> np.ndarray:
+    """Input synthesis of the benchmark fields: a stationary Gaussian random field with a
+    squared-exponential covariance on cell centres, by spectral (FFT) synthesis on a periodic grid
+    twice the size, normalised to standard deviation ``sigma``.  Same method and seed convention as
+    the product's field generator (tests check that both give the same field)."""
+    shape = tuple(int(s) for s in shape)
+    rng = np.random.default_rng(seed)
+    ext = tuple(2 * s for s in shape)
+    h = tuple(1.0 / s for s in shape)
+    freqs = np.meshgrid(*[np.fft.fftfreq(n, d=hh) for n, hh in zip(ext, h)], indexing="ij")
+    k2 = sum(fq ** 2 for fq in freqs)
+    spec = np.exp(-2.0 * np.pi ** 2 * corr_length ** 2 * k2)
+    noise = rng.standard_normal(ext)
+    field = np.real(np.fft.ifftn(np.fft.fftn(noise) * np.sqrt(spec)))
+    field = field[tuple(slice(0, s) for s in shape)]
+    return (field - field.mean()) / (field.std() + 1e-300) * sigma
+
+
+def assemble_csr_stencil(res, coef) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """Q1 diffusion matrix on a unit Grid3D as a CSR with every node's full 27-neighbourhood
+    (the structure fem.integrate keeps on cubic cells), values summed in FP64 from the closed-form
+    element matrix and rounded to fp32 once.  Returns (offsets, columns, values)."""
+    res = tuple(int(r) for r in res)
+    assert len(res) == 3
+    nx, ny, nz = res
+    mx, my, mz = nx + 1, ny + 1, nz + 1
+    K = element_stiffness(3, [1.0 / r for r in res])
+    c = np.asarray(coef, np.float32).astype(np.float64).reshape(nx, ny, nz)
+    st = np.zeros((mx, my, mz, 3, 3, 3))  # st[node][dx+1][dy+1][dz+1]
+    for a in range(8):
+        ai, aj, ak = a >> 2, (a >> 1) & 1, a & 1
+        for b in range(8):
+            bi, bj, bk = b >> 2, (b >> 1) & 1, b & 1
+            st[ai:ai + nx, aj:aj + ny, ak:ak + nz, bi - ai + 1, bj - aj + 1, bk - ak + 1] += c * K[a, b]
+    node = np.arange(mx * my * mz).reshape(mx, my, mz)
+    cols_full = np.full((mx, my, mz, 3, 3, 3), -1, np.int64)
+    for dx in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dz in (-1, 0, 1):
+                sl_dst = (slice(max(0, -dx), mx - max(0, dx)), slice(max(0, -dy), my - max(0, dy)),
+                          slice(max(0, -dz), mz - max(0, dz)))
+                sl_src = (slice(max(0, dx), mx + min(0, dx)), slice(max(0, dy), my + min(0, dy)),
+                          slice(max(0, dz), mz + min(0, dz)))
+                cols_full[sl_dst + (dx + 1, dy + 1, dz + 1)] = node[sl_src]
+    valid = cols_full.reshape(-1, 27) >= 0
+    counts = valid.sum(1)
+    offsets = np.zeros(mx * my * mz + 1, np.int32)
+    np.cumsum(counts, out=offsets[1:])
+    columns = cols_full.reshape(-1, 27)[valid].astype(np.int32)
+    values = st.reshape(-1, 27)[valid].astype(np.float32)
+    return offsets, columns, values
+
+
+def diffusion_system_3d(res, sigma: float, corr_length: float, seed: int):
+    """The benchmark's 3-D diffusion system (-div(a grad u) = f, a = exp(GRF), f ~ U[-1, 1] per node,
+    u = 0 on the boundary by projection), restated on the host.  Returns (offsets, columns, values,
+    b) in fp32: the projection zeroes boundary rows and columns (structure kept) and sets their
+    diagonal to 1 (warp/_src/fem/dirichlet.py:69-124)."""
+    res = tuple(int(r) for r in res)
+    rng = np.random.default_rng(seed)
+    coef = np.exp(gaussian_random_field(res, corr_length, sigma, seed)).reshape(-1)
+    nn = int(np.prod([r + 1 for r in res]))
+    f = rng.uniform(-1.0, 1.0, nn).astype(np.float32)
+    off, cols, vals = assemble_csr_stencil(res, coef.astype(np.float32))
+    b = assemble_rhs(res, f_nodal=f)
+    mask = boundary_mask(res) > 0
+    rows = np.repeat(np.arange(nn), np.diff(off))
+    keep = ~(mask[rows] | mask[cols])
+    vals = np.where(keep, vals, np.float32(0.0)).astype(np.float32)
+    vals[(rows == cols) & mask[rows]] = 1.0
+    b = np.where(mask, 0.0, b).astype(np.float32)
+    return off, cols, vals, b

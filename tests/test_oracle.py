@@ -217,3 +217,57 @@ def test_krylov_restatements_converge_to_direct_solutions():
         x, it, res = krylov.gmres(N_, b, dinv=dinv, tol=1e-10, atol=0.0, restart=8, left=left)
         assert np.linalg.norm(N_ @ x - b) <= 1e-10 * np.linalg.norm(b) and it % 8 == 0
         assert np.allclose(x, xs, rtol=1e-7, atol=1e-9)
+
+
+def test_oracle_structure_matches_reference_routine_at_configs():
+    """The oracle's triplet->BSR of the configuration systems equals the reference's compiled routine
+    (tests/golden/config_structure_ref.npz), offsets, columns and run ends."""
+    import os
+
+    from oracle import fem_q1
+
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "config_structure_ref.npz"))
+    for name in ("cfg1", "q1_2d_irregular", "elasticity_6x5x4"):
+        meta = g[name + "_meta"]
+        dim = int(meta[0])
+        res = tuple(int(k) for k in meta[1:1 + dim])
+        ncomp = int(meta[4])
+        if name == "cfg1":
+            r, c, v = fem_q1.assemble_triplets(res, coef=1.0)
+        elif ncomp == 1:
+            r, c, v = fem_q1.assemble_triplets(res, coef=g[name + "_coef"])
+        else:
+            E = g[name + "_young"]
+            lam = E * 0.3 / (1.3 * 0.4)
+            mu = E / 2.6
+            r, c, v = fem_q1.assemble_triplets(res, ncomp=3, lame=(lam.astype(np.float32), mu.astype(np.float32)))
+        nn = int(np.prod([k + 1 for k in res]))
+        o = oracle.bsr_from_triplets(nn, nn, r, c, v.reshape(len(r), ncomp * ncomp), block_shape=(ncomp, ncomp))
+        assert o["nnz"] == int(meta[5]) == len(g[name + "_columns"])
+        np.testing.assert_array_equal(o["offsets"], g[name + "_offsets"])
+        np.testing.assert_array_equal(o["columns"], g[name + "_columns"])
+        np.testing.assert_array_equal(o["tpl_block_offsets"], g[name + "_runends"])
+
+
+def test_oracle_stencil_assembly_equals_triplet_assembly():
+    """The CPU baseline's stencil-form assembly (every node's 27-neighbourhood) gives the triplet
+    route's unpruned matrix: same structure, values equal up to FP64 summation order."""
+    from oracle import fem_q1
+
+    res = (6, 5, 4)
+    coef = np.exp(np.random.default_rng(0).standard_normal(120)).astype(np.float32)
+    off, cols, vals = fem_q1.assemble_csr_stencil(res, coef)
+    r, c, v = fem_q1.assemble_triplets(res, coef=coef)
+    nn = 7 * 6 * 5
+    o = oracle.bsr_from_triplets(nn, nn, r, c, v, prune_numerical_zeros=False)
+    np.testing.assert_array_equal(o["offsets"], off)
+    np.testing.assert_array_equal(o["columns"], cols)
+    assert np.abs(o["values"] - vals).max() <= 1e-6 * np.abs(vals).max()
+
+
+def test_oracle_random_field_equals_product_field_generator():
+    from oracle import fem_q1
+    from warp_gb300 import fem
+
+    np.testing.assert_array_equal(fem.gaussian_random_field((8, 9, 10), 0.1, 1.5, 3),
+                                  fem_q1.gaussian_random_field((8, 9, 10), 0.1, 1.5, 3))

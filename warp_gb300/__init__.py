@@ -10,6 +10,7 @@ C ABI (``include/warp_gb300.h``); PyTorch provides device memory and streams onl
 """
 
 from . import _native  # noqa: F401
+from ._arrays import ScopedStream  # noqa: F401
 from . import sparse  # noqa: F401
 from . import optim  # noqa: F401
 from . import fem  # noqa: F401

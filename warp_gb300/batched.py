@@ -104,6 +104,7 @@ class BatchedCG:
             A.ptr(self.status), stream), "batched_pcg")
         self.launches += 2  # queue reset + the persistent kernel
 
+    @A.on_caller_stream
     def solve(self, b, x) -> None:
         """x <- the batched solve of A x = b (x is the initial guess); stream-ordered, no host sync
         once tuned."""

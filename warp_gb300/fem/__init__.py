@@ -182,6 +182,7 @@ def _cell_array(v, ncells: int):
     return t, 0.0
 
 
+@A.on_caller_stream
 def integrate(integrand: Integrand, domain=None, quadrature=None, fields=None, values=None, accumulate_dtype=None,
               output_dtype=None, output=None, device=None, temporary_store=None, kernel_options=None, assembly=None,
               add=False, bsr_options=None):
@@ -312,6 +313,7 @@ def _diagonal_matrix(mask: torch.Tensor, ncomp: int) -> sparse.BsrMatrix:
     return P
 
 
+@A.on_caller_stream
 def project_linear_system(system_matrix: sparse.BsrMatrix, system_rhs, projector_matrix: sparse.BsrMatrix,
                           fixed_value=None, normalize_projector: bool = True) -> None:
     """``A <- (I-P) A (I-P) + P`` and ``b <- (I-P)(b - A P f) + P f`` in place, keeping A's structure.

@@ -236,6 +236,7 @@ class MultigridPreconditioner:
                                   A.ptr(Am.values), N.GB_F32, w, r, t, N.GB_F32, -1.0, 1.0, 0, 0, 0, -1,
                                   A.ptr(self.status), stream), "residual")
 
+    @A.on_caller_stream
     def apply(self, r: torch.Tensor, z: torch.Tensor | None = None) -> torch.Tensor:
         """Eager z = M r on the current stream (tests / diagnostics)."""
         z = torch.empty_like(r) if z is None else z

@@ -151,6 +151,7 @@ def aslinearoperator(Am, batch_offsets=None, max_batch_length=None) -> LinearOpe
     raise ValueError(f"Unable to create LinearOperator from {Am}")
 
 
+@A.on_caller_stream
 def preconditioner(Am, ptype: str = "diag") -> LinearOperator | None:
     """``"diag"`` (Jacobi), ``"diag_abs"`` or ``"id"`` (reference: ``linear.py:236-280``)."""
     if ptype == "id":
@@ -178,6 +179,7 @@ def preconditioner(Am, ptype: str = "diag") -> LinearOperator | None:
     raise ValueError("Unsupported source matrix type for building diagonal preconditioner")
 
 
+@A.on_caller_stream
 def refresh_preconditioner(M: LinearOperator, Am, ptype: str = "diag") -> None:
     """Recompute a Jacobi preconditioner in place after ``Am``'s values changed (same structure)."""
     inv = M._inv_diag
@@ -358,6 +360,7 @@ class LinearSolverState:
         return it, math.sqrt(rr), atol_v
 
     # -- public ---------------------------------------------------------------------------
+    @A.on_caller_stream
     def __call__(self, A_=None, b=None, x=None, M=None):
         Aop = aslinearoperator(A_) if A_ is not None else self._A
         Mop = aslinearoperator(M) if M is not None else self._M
@@ -799,6 +802,7 @@ class FCG(LinearSolverState):
         raise ValueError("FCG runs on the fused path only")
 
 
+@A.on_caller_stream
 def fcg(A_, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_every=10, use_cuda_graph=True,
         run=True, stagnation_window: int = 25, stagnation_factor: float = 0.9):
     """Flexible CG with a (possibly nonlinear) preconditioner object; see ``FCG``."""
@@ -810,6 +814,7 @@ def fcg(A_, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_e
     return state
 
 
+@A.on_caller_stream
 def cg(A_, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_every=10, use_cuda_graph=True,
        run=True, *, restart=None):
     """Preconditioned Conjugate Gradient (reference: ``linear.py:1035-1121``)."""
@@ -820,6 +825,7 @@ def cg(A_, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_ev
     return state
 
 
+@A.on_caller_stream
 def cr(A_, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_every=10, use_cuda_graph=True,
        run=True, *, restart=None):
     """Conjugate Residual (reference: ``linear.py:1288-1374``)."""
@@ -830,6 +836,7 @@ def cr(A_, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_ev
     return state
 
 
+@A.on_caller_stream
 def gmres(A_, b, x, tol=None, atol=None, restart=31, maxiter=0, M=None, callback=None, check_every=31,
           use_cuda_graph=True, is_left_preconditioner=False, run=True):
     """Restarted GMRES(k) (reference: ``linear.py:1918-2008``)."""
@@ -840,6 +847,7 @@ def gmres(A_, b, x, tol=None, atol=None, restart=31, maxiter=0, M=None, callback
     return state
 
 
+@A.on_caller_stream
 def bicgstab(A_, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_every=10, use_cuda_graph=True,
              is_left_preconditioner=False, run=True):
     """BiCGSTAB (reference: ``linear.py:1577-1650``)."""
@@ -967,6 +975,7 @@ class RefinedSolver:
         rr, bb = self._host.tolist()
         return math.sqrt(rr), math.sqrt(bb)
 
+    @A.on_caller_stream
     def solve(self, b, x64=None, tol: float = 1e-8, max_outer: int = 50, callback=None):
         b = A.as_tensor(b).reshape(-1)
         if b.dtype != torch.float32:
@@ -1042,6 +1051,7 @@ class RefinedSolver:
                          converged=bool(rnorm <= tol * bnorm), diverged=diverged)
 
 
+@A.on_caller_stream
 def solve_refined(A_: sparse.BsrMatrix, b, x64=None, tol: float = 1e-8, M=None, method: str = "cg",
                   inner_tol: float = 1e-5, max_outer: int = 50, residual: str = "df32"):
     """FP64-accurate solve of ``A x = b`` with an FP32 Krylov inner loop; returns ``(x64, info)``.

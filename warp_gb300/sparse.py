@@ -185,6 +185,7 @@ def bsr_zeros(rows_of_blocks: int, cols_of_blocks: int, block_type=torch.float32
     return BsrMatrix(rows_of_blocks, cols_of_blocks, shape, dt)
 
 
+@A.on_caller_stream
 def bsr_set_zero(bsr: BsrMatrix, rows_of_blocks: int | None = None, cols_of_blocks: int | None = None, **kwargs):
     if rows_of_blocks is not None:
         bsr.nrow = int(rows_of_blocks)
@@ -205,6 +206,7 @@ def _ensure_fits(bsr: BsrMatrix, nnz: int) -> None:
         bsr.values = A.empty(bsr._values_shape(nnz), bsr.values.dtype)
 
 
+@A.on_caller_stream
 def bsr_set_from_triplets(
     dest: BsrMatrix,
     rows,
@@ -302,6 +304,7 @@ def bsr_set_from_triplets(
     dest._last_temporaries = (ws, tbo, tbi, rows, columns, values)
 
 
+@A.on_caller_stream
 def bsr_compress(src: BsrMatrix, prune_numerical_zeros: bool = True, inplace: bool = False,
                  topology: str | None = None) -> BsrMatrix:
     """Sort and coalesce the active blocks of every row (reference: ``sparse.py:1571-1640``).
@@ -406,6 +409,7 @@ def _scatter_sub_structure(dest, sub_off, sub_cols, sub_vals):
     dest.values[pos] = sub_vals[:n_sub]
 
 
+@A.on_caller_stream
 def bsr_from_triplets(rows_of_blocks: int, cols_of_blocks: int, rows, columns, values,
                       prune_numerical_zeros: bool = True) -> BsrMatrix:
     """Constructs a BSR matrix from triplets (reference: ``sparse.py`` ``bsr_from_triplets``)."""
@@ -419,6 +423,7 @@ def bsr_from_triplets(rows_of_blocks: int, cols_of_blocks: int, rows, columns, v
     return Am
 
 
+@A.on_caller_stream
 def bsr_copy(A_: BsrMatrix, scalar_type=None) -> BsrMatrix:
     out = BsrMatrix(A_.nrow, A_.ncol, A_.block_shape, A_.scalar_type if scalar_type is None else _parse_scalar(scalar_type))
     nnz = A_.nnz_sync()
@@ -430,6 +435,7 @@ def bsr_copy(A_: BsrMatrix, scalar_type=None) -> BsrMatrix:
     return out
 
 
+@A.on_caller_stream
 def bsr_scale(x: BsrMatrix, alpha: float) -> BsrMatrix:
     x.values.mul_(alpha)
     return x
@@ -446,9 +452,12 @@ def _vec_view(v, n_scalars: int, dtype: torch.dtype, what: str) -> torch.Tensor:
     return t
 
 
+@A.on_caller_stream
 def bsr_mv(Am: BsrMatrix, x, y=None, alpha: float = 1.0, beta: float = 0.0, transpose: bool = False,
            work_buffer=None, tile_size: int = 0, _status: torch.Tensor | None = None):
-    """``y := alpha * A x + beta * y`` (reference: ``sparse.py:4792-4913``).  Returns ``y``.
+    """``y := alpha * A x + beta * y`` (reference: ``sparse.py:4792-4913``).  Returns ``y`` (the
+    caller's array when given; a new array of the caller's type -- ``wp.array`` for ``wp.array``
+    inputs -- otherwise).  Runs on the caller's stream (Warp's current stream under Warp).
 
     ``x`` and ``y`` may alias (a work buffer then holds a copy of x).  ``tile_size`` > 0 sets the
     number of lanes cooperating on one block row (power of two <= 32).  Vectors may be float32 or
@@ -462,7 +471,8 @@ def bsr_mv(Am: BsrMatrix, x, y=None, alpha: float = 1.0, beta: float = 0.0, tran
     vec_dtype = x_t.dtype
     if vec_dtype not in (torch.float32, torch.float64):
         raise TypeError(f"bsr_mv: unsupported vector dtype {vec_dtype}")
-    if y is None:
+    created = y is None
+    if created:
         y_shape = (nrow_out,) if br == 1 else (nrow_out, br)
         y = A.empty(y_shape, vec_dtype)
         beta = 0.0
@@ -490,9 +500,11 @@ def bsr_mv(Am: BsrMatrix, x, y=None, alpha: float = 1.0, beta: float = 0.0, tran
             A.ptr(y_t), A.ptr(y_t), A.gb_dtype(vec_dtype), float(alpha), float(beta), 1 if transpose else 0, 0,
             lanes, -1, A.ptr(status), A.stream()),
         "bsr_mv")
-    return y
+    # a new output comes back in the caller's array type (wp.array for wp.array inputs)
+    return A.like(x, y) if created else y
 
 
+@A.on_caller_stream
 def bsr_mv_into(Am: BsrMatrix, x, y, z, alpha: float = 1.0, beta: float = 0.0) -> None:
     """``z := alpha * A x + beta * y`` with distinct input ``y`` and output ``z`` (``y`` may be ``z``).
 
@@ -532,6 +544,7 @@ def clear_device_status() -> None:
     _status_word().zero_()
 
 
+@A.on_caller_stream
 def bsr_get_diag(Am: BsrMatrix, out=None) -> torch.Tensor:
     """Diagonal blocks (zero where absent) (reference: ``sparse.py:2887``)."""
     br, bc = Am.block_shape
@@ -543,6 +556,7 @@ def bsr_get_diag(Am: BsrMatrix, out=None) -> torch.Tensor:
     return out
 
 
+@A.on_caller_stream
 def bsr_mm(x: BsrMatrix, y: BsrMatrix, z: BsrMatrix | None = None, alpha: float = 1.0, beta: float = 0.0,
            masked: bool = False, work_arrays: Any = None, reuse_topology: bool = False, tile_size: int = 0,
            max_new_nnz: int | None = None, topology: Any = None) -> BsrMatrix:

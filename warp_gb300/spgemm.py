@@ -22,6 +22,7 @@ N.register("gb_spgemm_values", N._c_int, [N._c_int, N._c_int, N._vp, N._vp, N._v
                                           N._c_int, N._vp, N._vp, N._vp, N._c_dbl, N._c_dbl, N._vp, N._c_int, N._vp])
 
 
+@A.on_caller_stream
 def bsr_mm(x: sparse.BsrMatrix, y: sparse.BsrMatrix, z: sparse.BsrMatrix | None = None, alpha: float = 1.0,
            beta: float = 0.0, masked: bool = False) -> sparse.BsrMatrix:
     if x.ncol != y.nrow:
