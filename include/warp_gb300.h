@@ -170,9 +170,20 @@ int gb_spgemm_values(int dtype, int nrow, const int* out_offsets, const int* run
  * (integrate.py:1404-1625).  gb_grid_boundary_mask + gb_dirichlet_project: the nodal boundary
  * projector and project_linear_system (warp/_src/fem/dirichlet.py:69-124). */
 int64_t gb_q1_triplet_count(int dim, int nx, int ny, int nz);
-int gb_q1_assemble_triplets(int dim, int nx, int ny, int nz, int ncomp, const double* K0, const double* K1,
+int gb_q1_assemble_triplets(int dim, int nx, int ny, int nz, int ncomp, const float* K0, const float* K1,
                             const float* coef0, float coef0_const, const float* coef1, float coef1_const, int* rows,
                             int* cols, float* vals, gb_stream_t stream);
+/* Direct compact-BSR assembly of the same bilinear form (no counterpart entry point in the reference: it
+ * produces the matrix that bsr_set_from_triplets builds from the triplets above, bit for bit -- same
+ * pruning of all-zero triplets, same per-block summation order -- without writing or sorting them;
+ * warp/_src/fem/integrate.py:1627-1878 + warp/native/sparse.cu:1168-1325).  K0/K1 are fp32 tables;
+ * columns/values need gb_q1_bsr_nnz_max() blocks of capacity; bsr_nnz_host (optional) receives
+ * offsets[nodes] asynchronously. */
+int64_t gb_q1_bsr_nnz_max(int dim, int nx, int ny, int nz);
+size_t gb_q1_assemble_bsr_workspace_bytes(int dim, int nx, int ny, int nz);
+int gb_q1_assemble_bsr(int dim, int nx, int ny, int nz, int ncomp, const float* K0, const float* K1, const float* coef0,
+                       float coef0_const, const float* coef1, float coef1_const, int prune, int* offsets, int* columns,
+                       float* values, int* bsr_nnz_host, void* workspace, size_t workspace_bytes, gb_stream_t stream);
 int gb_q1_assemble_rhs(int dim, int nx, int ny, int nz, int ncomp, const double* M, const float* f, float f0, float f1,
                        float f2, float* out, gb_stream_t stream);
 int gb_grid_boundary_mask(int dim, int nx, int ny, int nz, int face_bits, int ncomp, int comp_mask, float* mask,
@@ -267,6 +278,19 @@ size_t gb_bsr_compact_workspace_bytes(int nrow);
 int gb_bsr_compact(int block_size, int dtype, int nrow, const int* old_offsets, int* counts, const int* columns_in,
                    const void* values_in, int* offsets_out, int* columns_out, void* values_out, void* workspace,
                    size_t workspace_bytes, gb_stream_t stream);
+
+/* ---- Padded topology of bsr_set_from_triplets --------------------------------------------------
+ * gb_bsr_scatter_padded replaces _bsr_set_from_triplets_padded_scatter_compact_topology
+ * (warp/_src/sparse.py:1173-1208): copy each row of a compact structure into the destination's row
+ * capacity [dest_offsets[r], dest_offsets[r+1]); rows that do not fit get dest_row_counts[r] = 0 and
+ * raise *status to 1 (BSR_STATUS_ROW_CAPACITY_EXCEEDED, atomic max); block_map (optional) receives,
+ * per padded slot, the compact block it holds or -1.
+ * gb_bsr_gather_blocks: dst[b] = src[block_map[b]] or 0 for -1 (the value pass of the padded
+ * topology, warp/_src/sparse.py:1211-1230, applied to the compact run sums). */
+int gb_bsr_scatter_padded(int nrow, const int* compact_offsets, const int* compact_columns, const int* dest_offsets,
+                          int* dest_row_counts, int* dest_columns, int* block_map, int* status, gb_stream_t stream);
+int gb_bsr_gather_blocks(int dtype, int block_size, int64_t nblocks, const int* block_map, const void* src, void* dst,
+                         gb_stream_t stream);
 
 /* ---- Batched solves --------------------------------------------------------------------------
  * gb_batched_pcg replaces the batched CG of warp/_src/optim/linear.py:893-1032 (LinearOperator with

@@ -78,14 +78,15 @@ def test_cfg1_poisson_64x64_end_to_end(cuda):
     bh = b.cpu().numpy().astype(np.float64)
     xh = x.cpu().numpy().astype(np.float64)
     rel = np.linalg.norm(bh - oracle.bsr_mv_f64(off, cols, vals, xh)) / np.linalg.norm(bh)
-    # the recursive fp32 residual stops at 1e-6; the true residual of the fp32 iterate stays within a
-    # small factor of it
-    assert rel <= 4e-6, rel
-    # iteration count: the oracle's restatement of CG._run on the same fp32 system
-    _, it_o, _, _ = oracle.pcg_f32(off, cols, vals, bh.astype(np.float32),
-                                   inv_diag=oracle.inverse_diagonal_f32(off, cols, vals), tol=1e-6, atol=0.0,
-                                   maxiter=2000)
+    # iteration count and true residual: the oracle's restatement of CG._run on the same fp32 system.
+    # The recursive fp32 residual stops at 1e-6 relative; the true residual of an fp32 iterate sits
+    # above it (rounding of x and of A x in fp32: measured ~6e-6 here, as for the oracle's iterate)
+    xo, it_o, _, _ = oracle.pcg_f32(off, cols, vals, bh.astype(np.float32),
+                                    inv_diag=oracle.inverse_diagonal_f32(off, cols, vals), tol=1e-6, atol=0.0,
+                                    maxiter=2000)
     assert abs(it - it_o) <= max(2, 0.02 * it_o), (it, it_o)
+    rel_o = np.linalg.norm(bh - oracle.bsr_mv_f64(off, cols, vals, xo.astype(np.float64))) / np.linalg.norm(bh)
+    assert rel <= 2.0 * rel_o + 1e-6 and rel <= 2e-5, (rel, rel_o)
     # FP64 direct solve of the same (projected) system
     Ah = sp.csr_matrix((vals.astype(np.float64), cols, off), shape=(nn, nn))
     xd = spl.spsolve(Ah.tocsc(), bh)

@@ -23,7 +23,7 @@ def test_diffusion_triplets_and_bsr(cuda, res):
     # raw triplets: rows/cols bit-exact, values within 1e-6 of the oracle (relative to the row max)
     space = fem.make_polynomial_space(geo, degree=1)
     K = fem.q1.stiffness(dim, geo.cell_size)
-    Kd = torch.from_numpy(K).cuda()
+    Kd = torch.from_numpy(K.astype(np.float32)).cuda()
     nud = torch.from_numpy(nu).cuda()
     L = N.lib()
     T = int(L.gb_q1_triplet_count(dim, *geo._dims()))
@@ -117,3 +117,39 @@ def test_rhs_and_projection(cuda, res, ncomp):
     np.testing.assert_allclose(b.cpu().numpy(), b2, rtol=1e-4, atol=1e-5 * np.abs(b2).max())
     # structure is preserved (explicit zeros kept)
     assert Am.nnz_sync() == (Am.offsets[-1].item())
+
+
+@pytest.mark.parametrize("res,ncomp,zero_cells", [((9, 7), 1, False), ((6, 5, 7), 1, False), ((6, 5, 7), 1, True),
+                                                  ((5, 4, 3), 3, False), ((5, 4, 3), 3, True), ((4, 6), 1, True)])
+@pytest.mark.parametrize("prune", [True, False])
+def test_direct_assembly_equals_triplet_construction(cuda, res, ncomp, zero_cells, prune):
+    """fem.integrate's default (direct compact-BSR assembly, no triplets) returns the triplet
+    construction's matrix bit for bit: offsets, columns, value bits -- including the pruning of
+    all-zero triplets (cells with a zero coefficient) and prune_numerical_zeros=False."""
+    from warp_gb300 import fem
+
+    dim = len(res)
+    geo = fem.Grid2D(res=res) if dim == 2 else fem.Grid3D(res=res)
+    rng = np.random.default_rng(5)
+    coef = np.exp(rng.standard_normal(geo.cell_count())).astype(np.float32)
+    if zero_cells:
+        coef[rng.random(coef.size) < 0.3] = 0.0
+        coef[0] = -0.0
+    if ncomp == 1:
+        space = fem.make_polynomial_space(geo, degree=1)
+        form, vals = fem.diffusion_form, {"nu": coef}
+    else:
+        space = fem.make_polynomial_space(geo, degree=1, dtype="vec3")
+        form, vals = fem.linear_elasticity_form, {"lame": (coef * 1.7, coef)}
+    fields = {"u": fem.make_trial(space), "v": fem.make_test(space)}
+    mats = {c: fem.integrate(form, fields=fields, values=vals,
+                             bsr_options={"construction": c, "prune_numerical_zeros": prune})
+            for c in ("auto", "triplets")}
+    d, t = mats["auto"], mats["triplets"]
+    nnz = d.nnz_sync()
+    assert nnz == t.nnz_sync()
+    np.testing.assert_array_equal(d.offsets.cpu().numpy(), t.offsets.cpu().numpy())
+    np.testing.assert_array_equal(d.columns[:nnz].cpu().numpy(), t.columns[:nnz].cpu().numpy())
+    np.testing.assert_array_equal(d.values[:nnz].cpu().numpy().view(np.uint32), t.values[:nnz].cpu().numpy().view(np.uint32))
+    if not prune:
+        assert nnz == int(np.prod([3 * (k + 1) - 2 for k in res]))

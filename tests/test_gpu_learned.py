@@ -82,10 +82,10 @@ def _bf16_round(a):
     return torch.from_numpy(np.ascontiguousarray(a, np.float32)).to(torch.bfloat16).float().numpy()
 
 
-# (64, 40, 40) and (300, 10, 10): more work items (columns x slabs) than CTAs, so CTAs walk several
-# x-slabs and cross column boundaries in their shared-memory ring of x-plane blocks; (160, 4, 300) and
-# (160, 3, 450): long z rows shrink the ring to 5 and to the minimum of 4 slots, and CTAs walk
-# several slabs through them
+# (1, 1, 1) and (2, 4, 16): one x-plane, runs of one plane (the MMAs of the first and last input planes
+# feed one output plane only); (64, 40, 40) and (300, 10, 10): more work items (columns x planes) than
+# CTAs, so CTAs walk runs of x-planes, cross column boundaries and wrap their TMEM chunk ring many
+# times; (160, 4, 300) and (160, 3, 450): long z rows shrink the shared-memory ring of x-plane blocks
 @pytest.mark.parametrize("dims", [(1, 1, 1), (2, 4, 16), (7, 9, 11), (9, 7, 35), (33, 17, 20), (20, 12, 97),
                                   (64, 40, 40), (300, 10, 10), (160, 4, 300), (160, 3, 450)])
 def test_conv3_tcgen05_layer_matches_oracle(cuda, dims):

@@ -267,3 +267,32 @@ def test_bsr_mm_diagonal_projector_keeps_structure(cuda):
     D = A.numpy_dense()
     PA = sparse.bsr_mm(P, A)
     np.testing.assert_allclose(PA.numpy_dense(), P.numpy_dense() @ D, atol=1e-5)
+
+
+@pytest.mark.parametrize("shapes", [((1, 1), (1, 1)), ((3, 3), (3, 3)), ((2, 3), (3, 1))])
+@pytest.mark.parametrize("beta", [0.0, 0.5])
+def test_bsr_mm_masked_keeps_z_topology(cuda, shapes, beta):
+    """topology="masked" (reference sparse.py:4200-4260): z keeps its blocks; on them
+    z = alpha x y + beta z, and product terms outside z's pattern are dropped."""
+    from warp_gb300 import sparse
+
+    (a, k), (k2, c) = shapes
+    X, ox = _random_bsr(60, 50, 400, (a, k), seed=11)
+    Y, oy = _random_bsr(50, 70, 500, (k2, c), seed=12)
+    Z, oz = _random_bsr(60, 70, 900, (a, c), seed=13)
+    Dx = oracle.bsr_to_dense(ox["offsets"], ox["columns"], ox["values"], 50, (a, k))
+    Dy = oracle.bsr_to_dense(oy["offsets"], oy["columns"], oy["values"], 70, (k2, c))
+    Dz = oracle.bsr_to_dense(oz["offsets"], oz["columns"], oz["values"], 70, (a, c))
+    off0, cols0 = Z.offsets.clone(), Z.columns[: Z.nnz_sync()].clone()
+    out = sparse.bsr_mm(X, Y, Z, alpha=1.5, beta=beta, topology="masked")
+    assert out is Z
+    np.testing.assert_array_equal(Z.offsets.cpu().numpy(), off0.cpu().numpy())
+    np.testing.assert_array_equal(Z.columns[: Z.nnz_sync()].cpu().numpy(), cols0.cpu().numpy())
+    mask = np.kron((oracle.bsr_to_dense(oz["offsets"], oz["columns"], np.ones_like(oz["values"]), 70, (a, c))
+                    .reshape(60, a, 70, c)[:, 0, :, 0] != 0).astype(float), np.ones((a, c)))
+    exp = (1.5 * Dx @ Dy + beta * Dz) * mask
+    np.testing.assert_allclose(Z.numpy_dense(), exp, rtol=1e-4, atol=1e-4 * np.abs(exp).max())
+    # the deprecated masked=True spelling is the same operation
+    Z2, _ = _random_bsr(60, 70, 900, (a, c), seed=13)
+    sparse.bsr_mm(X, Y, Z2, alpha=1.5, beta=beta, masked=True)
+    np.testing.assert_array_equal(Z2.values.cpu().numpy(), Z.values.cpu().numpy())

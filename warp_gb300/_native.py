@@ -109,6 +109,8 @@ _SIGNATURES = {
     "gb_multi_dot_workspace_bytes": (_c_sz, [_c_int]),
     "gb_multi_dot": (_c_int, [_c_int, _c_i64, _c_int, _vp, _c_i64, _vp, _vp, _vp, _c_sz, _vp]),
     "gb_multi_axpy": (_c_int, [_c_int, _c_i64, _c_int, _vp, _c_i64, _vp, _c_dbl, _c_dbl, _vp, _vp]),
+    "gb_bsr_scatter_padded": (_c_int, [_c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "gb_bsr_gather_blocks": (_c_int, [_c_int, _c_int, _c_i64, _vp, _vp, _vp, _vp]),
     "gb_bsr_rows_to_offsets": (_c_int, [_c_i64, _vp, _c_int, _vp, _vp, _vp]),
     "gb_bsr_compress_rows": (_c_int, [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_int, _c_u64, _vp, _vp]),
     "gb_bsr_compact_workspace_bytes": (_c_sz, [_c_int]),

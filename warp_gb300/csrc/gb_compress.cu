@@ -291,3 +291,87 @@ GB_API int gb_bsr_compact(int block_size, int dtype, int nrow, const int* old_of
     gb::set_error("bsr_compact: dtype must be f32 or f64");
     return GB_ERR_UNSUPPORTED;
 }
+
+// ---------------------------------------------------------------------------------------------
+// Padded topology of bsr_set_from_triplets (warp/_src/sparse.py:1173-1230, 1335-1420): a compact
+// triplet structure is written into the destination's existing row capacity.
+// ---------------------------------------------------------------------------------------------
+namespace gb {
+
+// One thread per row: rows whose compact block count exceeds their capacity get row_counts = 0 and
+// raise the status word (BSR_STATUS_ROW_CAPACITY_EXCEEDED = 1, atomic max); otherwise the compact
+// columns are copied to the front of the padded row.  block_map[b] = compact block of padded slot b,
+// or -1 for an unused slot (block_map may be null).
+__global__ void k_scatter_padded(int nrow, const int* __restrict__ c_off, const int* __restrict__ c_cols,
+                                 const int* __restrict__ d_off, int* __restrict__ d_counts, int* __restrict__ d_cols,
+                                 int* __restrict__ block_map, int* __restrict__ status)
+{
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= nrow) return;
+    const int cb = c_off[row];
+    int cnt = c_off[row + 1] - cb;
+    const int beg = d_off[row], cap_end = d_off[row + 1];
+    if (beg + cnt > cap_end) {
+        cnt = 0;
+        atomicMax(status, 1);
+    }
+    d_counts[row] = cnt;
+    for (int k = 0; k < cnt; ++k) {
+        d_cols[beg + k] = c_cols[cb + k];
+        if (block_map) block_map[beg + k] = cb + k;
+    }
+    if (block_map)
+        for (int b = beg + cnt; b < cap_end; ++b) block_map[b] = -1;
+}
+
+// dst[b] = block_map[b] >= 0 ? src[block_map[b]] : 0, block_size scalars per block
+template <typename T>
+__global__ void k_gather_blocks(int64_t nblocks, int block_size, const int* __restrict__ block_map,
+                                const T* __restrict__ src, T* __restrict__ dst)
+{
+    const int64_t total = nblocks * block_size;
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t b = t / block_size;
+        const int s = (int)(t - b * block_size);
+        const int m = block_map[b];
+        dst[t] = m >= 0 ? src[(size_t)m * block_size + s] : T(0);
+    }
+}
+
+}  // namespace gb
+
+GB_API int gb_bsr_scatter_padded(int nrow, const int* compact_offsets, const int* compact_columns,
+                                 const int* dest_offsets, int* dest_row_counts, int* dest_columns, int* block_map,
+                                 int* status, cudaStream_t stream)
+{
+    GB_REQUIRE(nrow >= 0, "bsr_scatter_padded: negative row count");
+    GB_REQUIRE(nrow == 0 || (compact_offsets && compact_columns && dest_offsets && dest_row_counts && dest_columns &&
+                             status), "bsr_scatter_padded: null argument");
+    if (nrow == 0) return GB_OK;
+    gb::k_scatter_padded<<<gb::ceil_div(nrow, 256), 256, 0, stream>>>(nrow, compact_offsets, compact_columns,
+                                                                      dest_offsets, dest_row_counts, dest_columns,
+                                                                      block_map, status);
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+GB_API int gb_bsr_gather_blocks(int dtype, int block_size, int64_t nblocks, const int* block_map, const void* src,
+                                void* dst, cudaStream_t stream)
+{
+    GB_REQUIRE(block_size >= 1 && nblocks >= 0, "bsr_gather_blocks: bad sizes");
+    if (nblocks == 0) return GB_OK;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(gb::ceil_div<int64_t>(nblocks * block_size, 256),
+                                                                 gb::kSmCount * 16));
+    if (dtype == GB_F32)
+        gb::k_gather_blocks<float><<<grid, 256, 0, stream>>>(nblocks, block_size, block_map,
+                                                             static_cast<const float*>(src), static_cast<float*>(dst));
+    else if (dtype == GB_F64)
+        gb::k_gather_blocks<double><<<grid, 256, 0, stream>>>(nblocks, block_size, block_map,
+                                                              static_cast<const double*>(src), static_cast<double*>(dst));
+    else {
+        gb::set_error("bsr_gather_blocks: float32 or float64 values");
+        return GB_ERR_UNSUPPORTED;
+    }
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}

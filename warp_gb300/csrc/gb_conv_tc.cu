@@ -10,22 +10,32 @@
 // the reads past the last tile.  The tap (dx, dy, dz) of output row p is input row
 // p + dx sx + dy sy + dz (sx = (ny+2)(nz+2), sy = nz+2).
 //
-// The dz taps are folded into the GEMM's N dimension: for 128 consecutive rows q,
-//     Z[q][dz][co] = sum_{dx,dy} sum_ci in[q + dx sx + dy sy][ci] W[dx,dy,dz][ci][co]
-// is 9 MMAs (one per (dx, dy); M = 128 rows, N = 48 = 3 dz x 16 co, K = 16 channels), each A
-// operand being 128 consecutive staged rows -- a K-major, non-swizzled UMMA operand (8-row core
-// matrices 128 B apart, the two 8-channel halves one plane apart) -- and then
-//     out[p] = Z[p-1][-1] + Z[p][0] + Z[p+1][+1]
+// The dx and dz taps are folded into the GEMM's N dimension.  For a window of 128 consecutive rows
+// q of input x-plane x_in and one dy,
+//     Z[q][dx][dz][co] = sum_ci in[x_in][q + dy sy][ci] W[dx,dy,dz][ci][co]
+// is one MMA (M = 128 rows, N = 144 = 3 dx x 3 dz x 16 co, K = 16 channels) whose A operand is 128
+// consecutive staged rows -- a K-major, non-swizzled UMMA operand (8-row core matrices 128 B apart,
+// the two 8-channel halves one plane apart).  Input plane x_in feeds output planes x_in + 1, x_in,
+// x_in - 1 (dx = -1, 0, +1), so the B operand orders its rows [dx = +1 | 0 | -1] and the MMA's 144
+// accumulator columns are three 48-column chunks of a per-window ring of output planes in TMEM:
+// the chunks of consecutive output planes are adjacent, and one MMA adds this input plane's
+// contribution to all three.  Over its three input planes an output plane's chunk receives its 27
+// taps: 3 dy MMAs per (window, input plane) instead of 9 when only dz was folded (the MMA issue
+// rate, not its N, bounds these K = 16 MMAs).  A chunk whose three planes wrap around the ring end
+// is split into two MMAs; at the ends of a CTA's run of x-planes only the chunks of planes in the
+// run are written (N = 48 or 96).  The epilogue then forms
+//     out[p] = Z[p-1][dz=-1] + Z[p][0] + Z[p+1][+1]
 // for the 126 rows whose neighbours lie in the same 128-row window (lane shuffles, plus one value
-// exchanged between neighbouring epilogue warps).
+// exchanged between neighbouring epilogue warps), and zeroes the chunk for its next plane.
 //
-// A stage covers TC_SUB = 4 such windows (504 output rows): for each dx, rows
-// [q0 + dx sx - sy, q0 + dx sx + sy + 126*3 + 128) of both planes are staged with 1-D bulk copies
-// (6 copies) into a 2-3 stage ring; one MMA thread issues the 36 MMAs (dx, dy)-major so the four
-// windows' accumulators (4 x 48 TMEM columns, two slots) form independent chains; four epilogue
-// warps read them with tcgen05.ld (each warp its 32-lane quarter), sum the dz taps, apply ReLU and
-// store bf16 rows of interior voxels -- or, for the last layer, write
-// w[v] = omega dinv[v] r[v] + (mask[v] ? 0 : out[v][0]) in fp32 (the Jacobi step fused).
+// A work item is one output x-plane of a column of TC_SUB = 2 windows (252 output rows); a CTA walks
+// x through a contiguous range of items, so each input x-plane block (both planes, rows
+// [q0 - sy, q0 + sy + 126 + 128)) is copied once with 1-D bulk copies into a ring of slots.  Warp
+// roles: a copy warp, one MMA-issuing warp per window (3 dy MMAs per input plane on the window's
+// chunk ring), and two groups of four epilogue warps per window (one warp per TMEM lane quarter;
+// the groups take alternate output planes) that read a finished chunk with tcgen05.ld, sum the dz taps, apply ReLU and store bf16 rows of
+// interior voxels -- or, for the last layer, write w[v] = omega dinv[v] r[v] + (mask[v] ? 0 :
+// out[v][0]) in fp32 (the Jacobi step fused) -- then zero the chunk with tcgen05.st.
 // Every wait is bounded (globaltimer); a timeout sets GB_DEV_WAIT_TIMEOUT, the CTA drains its own
 // copies and MMAs (bounded) and frees its TMEM before returning.
 #include "gb_bulk.cuh"
@@ -36,21 +46,27 @@ namespace gb {
 
 constexpr int TC_M = 128;                  // rows of one window (UMMA M)
 constexpr int TC_OUT = TC_M - 2;           // output rows per window
-constexpr int TC_SUB = 4;                  // windows per work item (504 output rows of one x-slab)
-constexpr int TC_N = 48;                   // 3 dz taps x 16 output channels (UMMA N)
+constexpr int TC_SUB = 2;                  // windows per work item (252 output rows of one x-plane)
+constexpr int TC_CHUNK = 48;               // TMEM columns of one (window, output plane): 3 dz x 16 co
+constexpr int TC_RING = 5;                 // output planes in flight per window (chunk ring)
+constexpr int TC_N = 3 * TC_CHUNK;         // 144 = 3 dx x 3 dz x 16 co (UMMA N of a full MMA)
 constexpr int TC_ISSUERS = TC_SUB;         // one MMA-issuing warp per window
-constexpr int TC_EPI_GROUPS = 2;           // epilogue groups of 4 warps (one per TMEM lane quarter)
-constexpr int TC_EPI_WARP0 = 1 + TC_ISSUERS;  // warp 0 copies, warps 1..4 issue MMAs, then the epilogue
+constexpr int TC_EPI_PAR = 2;              // epilogue groups per window: items drained alternately
+constexpr int TC_EPI_GROUPS = TC_SUB * TC_EPI_PAR;  // groups of 4 warps (one per TMEM lane quarter)
+constexpr int TC_EPI_WARP0 = 1 + TC_ISSUERS;  // warp 0 copies, warps 1..TC_ISSUERS issue MMAs, then the epilogue
 constexpr int TC_THREADS = 32 * TC_EPI_WARP0 + TC_EPI_GROUPS * 128;
-constexpr uint32_t TC_TMEM_COLS = 512;     // 2 slots x 4 windows x 48 columns = 384, rounded up
-constexpr int TC_W_BYTES = 9 * 1536;       // per (dx, dy): [k-half][dz 3 x co 16][8 ci] bf16
-constexpr int TC_WPG = TC_SUB / TC_EPI_GROUPS;  // windows per epilogue group per item (drained together)
-constexpr int TC_XCHG_BYTES = TC_EPI_GROUPS * 2 * TC_WPG * 4 * 2 * 16 * 4;  // [group][parity][window][quarter][lo/hi][16]
+constexpr uint32_t TC_TMEM_COLS = 512;     // TC_SUB x TC_RING x TC_CHUNK = 480, rounded up
+constexpr uint32_t TC_WIN_COLS = TC_RING * TC_CHUNK;  // 240 columns per window
+constexpr int TC_WB_KHALF = TC_N * 16;     // B operand of one dy: [k-half][n 144][8 ci] bf16
+constexpr int TC_WB_DY = 2 * TC_WB_KHALF;  // 4608 bytes
+constexpr int TC_W_BYTES = 3 * TC_WB_DY;   // 13824 bytes for the 3 dy
+constexpr int TC_XCHG_BYTES = TC_EPI_GROUPS * 2 * 4 * 2 * 16 * 4;  // [group][parity][quarter][lo/hi][16]
 constexpr int TC_MAX_SLOTS = 8;            // x-plane blocks in the shared-memory ring
-constexpr int TC_MIN_SLOTS = 4;            // three in use (x-1, x, x+1) plus one in flight
-constexpr size_t TC_SMEM_LIMIT = 220 * 1024;
-constexpr int TC_BAR_PROLOGUE = 2 + TC_EPI_GROUPS;  // named barriers: 0 CTA, 1..groups epilogue groups,
-                                                    // 1 + groups all epilogue warps, then the prologue
+constexpr int TC_MIN_SLOTS = 3;            // one being read, one landing, one in flight
+constexpr size_t TC_SMEM_LIMIT = 200 * 1024;
+constexpr int TC_BAR_PROLOGUE = 1 + TC_EPI_GROUPS;  // named barriers: 0 CTA, 1..groups epilogue groups,
+                                                    // then the prologue
+static_assert(TC_SUB * TC_WIN_COLS <= TC_TMEM_COLS, "chunk rings exceed the TMEM allocation");
 
 // Division by a loop-invariant divisor with a multiply and shifts (Granlund and Montgomery, "Division
 // by invariant integers using multiplication", PLDI 1994, figure 4.1): exact for every 32-bit n.
@@ -103,8 +119,10 @@ __device__ __forceinline__ uint64_t umma_desc(uint32_t addr, uint32_t lbo, uint3
 }
 
 // kind::f16 instruction descriptor: D fp32, A and B bf16, both K-major, N >> 3, M >> 4.
-constexpr uint32_t kTcIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_N >> 3) << 17) |
-                              ((uint32_t)(TC_M >> 4) << 24);
+__host__ __device__ constexpr uint32_t tc_idesc(int n)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+}
 
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
@@ -143,6 +161,17 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16])
     for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
 }
 
+// zero 16 consecutive accumulator columns of this warp's lane quarter
+__device__ __forceinline__ void tc_st16_zero(uint32_t taddr)
+{
+    const uint32_t z = 0u;
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, "
+        "%1, %1};" ::"r"(taddr),
+        "r"(z)
+        : "memory");
+}
+
 __device__ __forceinline__ float tc_ld1(uint32_t taddr)
 {
     uint32_t r;
@@ -163,14 +192,10 @@ __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity, volatile
 }
 
 // named barriers (non-aligned form: lanes may arrive after divergent code): id 1 + group for the four
-// warps of one epilogue group, id 1 + TC_EPI_GROUPS for all epilogue warps
+// warps of one epilogue group
 __device__ __forceinline__ void epi_group_barrier(int group)
 {
     asm volatile("barrier.sync %0, 128;" ::"r"(1 + group) : "memory");
-}
-__device__ __forceinline__ void epi_all_barrier()
-{
-    asm volatile("barrier.sync %0, %1;" ::"r"(1 + TC_EPI_GROUPS), "r"(TC_EPI_GROUPS * 128) : "memory");
 }
 
 template <bool LAST>
@@ -180,20 +205,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
     pdl_enter();
     unsigned char* ring = smem;
     unsigned char* wsm = smem + (size_t)c.slots * c.block_bytes;
-    float* xchg = reinterpret_cast<float*>(wsm + TC_W_BYTES);  // [group][parity][window][quarter][lo/hi][16]
+    float* xchg = reinterpret_cast<float*>(wsm + TC_W_BYTES);  // [group][parity][quarter][lo/hi][16]
     uint64_t* full = reinterpret_cast<uint64_t*>(wsm + TC_W_BYTES + TC_XCHG_BYTES);
     uint64_t* empty = full + TC_MAX_SLOTS;
-    uint64_t* accfull = empty + TC_MAX_SLOTS;
-    uint64_t* accempty = accfull + 2;
-    uint64_t* done = accempty + 2;  // every issuer's last commit: all MMAs of the CTA completed
+    uint64_t* accfull = empty + TC_MAX_SLOTS;  // [TC_RING]: an output plane's chunks are complete
+    uint64_t* accempty = accfull + TC_RING;    // [TC_RING]: a chunk was drained and zeroed
+    uint64_t* done = accempty + TC_RING;       // every issuer's last commit: all MMAs of the CTA completed
     uint32_t* s_tmem = reinterpret_cast<uint32_t*>(done + 1);
     volatile int* s_abort = reinterpret_cast<volatile int*>(s_tmem + 1);
     volatile int* s_issued = s_abort + 1;      // x-plane blocks whose copies were issued
-    volatile int* s_epi_abort = s_issued + 1;  // written by epilogue warps only, read after their barrier
     const int NS = c.slots;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // contiguous range of work items; consecutive items of one column differ by one x-slab, so the
-    // blocks x and x+1 of an item are the blocks x-1 and x of the next one
+    volatile int* s_gabort = s_issued + 1;  // [TC_EPI_GROUPS] per epilogue group, read after its barrier
+    // contiguous range of work items (output planes); consecutive items of one column are consecutive
+    // x-planes, so every input plane of a run is staged once
     const int64_t k_begin = (int64_t)blockIdx.x * c.nitems / gridDim.x;
     const int64_t k_end = (int64_t)(blockIdx.x + 1) * c.nitems / gridDim.x;
 
@@ -202,14 +227,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], TC_ISSUERS);
         }
-        for (int a = 0; a < 2; ++a) {
+        for (int a = 0; a < TC_RING; ++a) {
             mbar_init(&accfull[a], TC_ISSUERS);
-            mbar_init(&accempty[a], 4 * TC_EPI_GROUPS);
+            mbar_init(&accempty[a], 4 * TC_SUB);  // the 4 warps of each window's group draining the plane
         }
         mbar_init(done, TC_ISSUERS);
         *s_abort = 0;
         *s_issued = 0;
-        *s_epi_abort = 0;
+        for (int gq = 0; gq < TC_EPI_GROUPS; ++gq) s_gabort[gq] = 0;
         fence_mbar_init();
     }
     uint32_t tmem = 0;
@@ -220,12 +245,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
         __threadfence_block();  // the barrier words and flags written by thread 0 before the arrival
         asm volatile("bar.arrive %0, %1;" ::"r"(TC_BAR_PROLOGUE), "r"(TC_THREADS) : "memory");
     } else {
-        // weights -> B operands: (dx, dy) pair g, k-half kc, row n = 16 dz_idx + co at g*1536 + kc*768 + n*16
+        // weights -> B operands: dy index g, k-half kc, row n = 48 (1 - dx) + 16 (dz + 1) + co at
+        // g * TC_WB_DY + kc * TC_WB_KHALF + n * 16 (rows ordered by the output plane they feed)
         for (int i = threadIdx.x - 32; i < 27 * 16 * 2; i += blockDim.x - 32) {
             const int t = i >> 5, co = (i >> 1) & 15, kc = i & 1;
-            const int g = t / 3, dzi = t % 3;
+            const int dx = t / 9 - 1, g = (t / 3) % 3, dz = t % 3 - 1;
             const uint4 v = reinterpret_cast<const uint4*>(c.Wt)[(t * 16 + co) * 2 + kc];
-            *reinterpret_cast<uint4*>(wsm + g * 1536 + kc * 768 + (dzi * 16 + co) * 16) = v;
+            const int n = TC_CHUNK * (1 - dx) + 16 * (dz + 1) + co;
+            *reinterpret_cast<uint4*>(wsm + g * TC_WB_DY + kc * TC_WB_KHALF + n * 16) = v;
         }
         fence_proxy_async_shared();  // make the generic-proxy stores visible to the tensor cores
         if (warp == 1) {
@@ -274,195 +301,189 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
             }
         }
     } else if (warp <= TC_ISSUERS) {
-        // ------------- MMA warps: warp 1 + j issues the 9 (dx, dy) MMAs of window j --------------------
+        // ---------- MMA warps: warp 1 + j issues window j's 3 dy MMAs for every input plane -----------
         if (lane == 0) {
             const int j = warp - 1;
             const uint32_t wbase = smem_u32(wsm);
             const uint32_t rbase = smem_u32(ring);
-            int it = 0;  // items of this CTA so far (TMEM slot it & 1)
-            int q0 = 0;  // sequence number of the current run's first block (x0 - 1)
+            const uint32_t dwin = tmem + (uint32_t)j * TC_WIN_COLS;
+            int it0 = 0;  // item number (CTA order) of the current run's first output plane
+            int q0 = 0;   // block sequence number of the run's first input plane (x0 - 1)
             bool ok = true;
             for (int64_t k = k_begin; k < k_end && ok;) {
                 const int o = (int)(k / c.nx);
+                const int x0 = (int)(k % c.nx) + 1;
                 const int64_t run_end = min(k_end, (int64_t)(o + 1) * c.nx);
-                const int run = (int)(run_end - k);
-                for (int t = 0; t < run; ++t, ++it) {
-                    const int a = it & 1;
-                    // blocks q0+t (x-1), q0+t+1 (x), q0+t+2 (x+1); the earlier item of the run waited for the first two
-                    for (int d = (t == 0 ? 0 : 2); d < 3 && ok; ++d) {
-                        const int q = q0 + t + d;
-                        ok = tc_wait(&full[q % NS], (q / NS) & 1, s_abort);
+                const int x1 = (int)((run_end - 1) % c.nx) + 1;
+                for (int xi = x0 - 1; xi <= x1 + 1; ++xi) {
+                    const int q = q0 + (xi - x0 + 1);
+                    // output planes this input feeds inside the run, and whether the last of them is
+                    // touched for the first time (its chunk must have been drained and zeroed)
+                    const int lo = max(x0, xi - 1), hi = min(x1, xi + 1);
+                    const bool fresh = (hi == xi + 1) || (xi == x0 - 1);
+                    ok = tc_wait(&full[q % NS], (q / NS) & 1, s_abort);
+                    if (ok && fresh) {
+                        const int sh = it0 + (hi - x0);
+                        ok = tc_wait(&accempty[sh % TC_RING], (sh / TC_RING) & 1, s_abort);
                     }
-                    if (ok && it >= 2) ok = tc_wait(&accempty[a], ((it >> 1) & 1) ^ 1, s_abort);
                     if (!ok) {
                         *s_abort = 1;
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t dcol = tmem + (uint32_t)((a * TC_SUB + j) * TC_N);
+                    const int np = hi - lo + 1;                 // planes fed (1..3)
+                    const int clo = (it0 + (lo - x0)) % TC_RING;  // chunk of plane lo
+                    const int n1 = min(np, TC_RING - clo);      // planes before the ring wraps
+                    const uint32_t boff = (uint32_t)((lo - (xi - 1)) * TC_CHUNK * 16);  // B rows of plane lo
+                    const uint32_t arow0 = rbase + (uint32_t)(q % NS) * c.block_bytes + (uint32_t)(j * TC_OUT) * 16u;
 #pragma unroll
-                    for (int g = 0; g < 9; ++g) {
-                        const int b = g / 3, dyi = g % 3;
-                        const uint32_t arow = rbase + (uint32_t)((q0 + t + b) % NS) * c.block_bytes +
-                                              (uint32_t)(dyi * c.sy + j * TC_OUT) * 16u;
-                        tc_mma(dcol, umma_desc(arow, c.rows_bytes, 128), umma_desc(wbase + g * 1536, 768, 128),
-                               kTcIdesc, g > 0 ? 1u : 0u);
+                    for (int g = 0; g < 3; ++g) {
+                        const uint64_t adesc = umma_desc(arow0 + (uint32_t)(g * c.sy) * 16u, c.rows_bytes, 128);
+                        const uint32_t b0 = wbase + (uint32_t)(g * TC_WB_DY) + boff;
+                        tc_mma(dwin + (uint32_t)(clo * TC_CHUNK), adesc, umma_desc(b0, TC_WB_KHALF, 128),
+                               tc_idesc(n1 * TC_CHUNK), 1u);
+                        if (n1 < np)
+                            tc_mma(dwin, adesc, umma_desc(b0 + (uint32_t)(n1 * TC_CHUNK * 16), TC_WB_KHALF, 128),
+                                   tc_idesc((np - n1) * TC_CHUNK), 1u);
                     }
-                    // x-1 is not read again in this run; after the run's last item neither are x and x+1
-                    tc_commit(&empty[(q0 + t) % NS]);
-                    if (t == run - 1) {
-                        tc_commit(&empty[(q0 + t + 1) % NS]);
-                        tc_commit(&empty[(q0 + t + 2) % NS]);
-                    }
-                    tc_commit(&accfull[a]);
+                    tc_commit(&empty[q % NS]);  // the block is not read again
+                    if (xi - 1 >= x0) tc_commit(&accfull[(it0 + (xi - 1 - x0)) % TC_RING]);  // plane xi - 1 done
                 }
-                q0 += run + 2;
+                it0 += (int)(run_end - k);
+                q0 += (int)(run_end - k) + 2;
                 k = run_end;
             }
             tc_commit(done);  // arrives once every MMA this thread issued has completed
         }
     } else {
         // --------------------------------- epilogue warps --------------------------------------------
-        const int quarter = warp & 3;                   // TMEM lanes 32*quarter .. +31 belong to this warp
-        const int group = (warp - TC_EPI_WARP0) >> 2;   // windows group, group + TC_EPI_GROUPS, ...
-        const int i = quarter * 32 + lane;              // row of the 128-row window
+        // group = par * TC_SUB + window: the groups of parity `par` drain the items it with
+        // it % TC_EPI_PAR == par, so the TMEM loads, exchange and stores of consecutive items overlap
+        const int quarter = warp & 3;                  // TMEM lanes 32*quarter .. +31 belong to this warp
+        const int group = (warp - TC_EPI_WARP0) >> 2;
+        const int win = group % TC_SUB, par = group / TC_SUB;
+        const int i = quarter * 32 + lane;             // row of the 128-row window
         const uint32_t usx = (uint32_t)c.sx, usy = (uint32_t)c.sy;
-        float* xg = xchg + group * (2 * TC_WPG * 4 * 2 * 16);
-        int it = 0;
+        const uint32_t tq = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)win * TC_WIN_COLS;
+        float* xg = xchg + group * (2 * 4 * 2 * 16);
+        // the accumulator chunks start at zero (every MMA accumulates); the parity-0 groups clear them
+        // and give the first "drained" arrival of every chunk
+        if (par == 0) {
+            for (int a = 0; a < TC_RING; ++a) {
+#pragma unroll
+                for (int h = 0; h < 3; ++h) tc_st16_zero(tq + (uint32_t)(a * TC_CHUNK + 16 * h));
+            }
+            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0)
+                for (int a = 0; a < TC_RING; ++a) mbar_arrive1(&accempty[a]);
+        }
         int xp = 0;  // exchange buffer parity
-        for (int64_t k = k_begin; k < k_end; ++k, ++it) {
-            const int a = it & 1;
+        for (int64_t k = k_begin + par; k < k_end; k += TC_EPI_PAR) {
+            const int it = (int)(k - k_begin);
+            const int a = it % TC_RING;
             const uint32_t xk = (uint32_t)(k % c.nx) + 1u;
             // row of lane 0 of window 0: one row before the item's first output row
             const uint32_t q0 = xk * usx + usy + (uint32_t)(k / c.nx) * (uint32_t)(TC_SUB * TC_OUT);
             int ok = 1;
-            if (lane == 0) ok = tc_wait(&accfull[a], (it >> 1) & 1, s_abort) ? 1 : 0;
+            if (lane == 0) ok = tc_wait(&accfull[a], (it / TC_RING) & 1, s_abort) ? 1 : 0;
             ok = __shfl_sync(0xffffffffu, ok, 0);
-            if (!ok && lane == 0) *s_epi_abort = 1;
-            // all epilogue warps decide together: the flag only changes before this barrier
-            epi_all_barrier();
-            if (*s_epi_abort) {
+            if (!ok && lane == 0) s_gabort[group] = 1;
+            // the group's four warps decide together: the flag only changes before this barrier
+            epi_group_barrier(group);
+            if (s_gabort[group]) {
                 if (lane == 0) *s_abort = 1;
                 break;
             }
             tc_fence_after();
             __syncwarp();
-            // this group's windows j = group + w * TC_EPI_GROUPS are drained together: all TMEM loads,
-            // one exchange of the quarter-boundary rows, one barrier, then the outputs
-            float* xb = xg + xp * (TC_WPG * 4 * 2 * 16);
-            uint32_t taddr[TC_WPG];
-            bool valid[TC_WPG];
-            uint32_t prow[TC_WPG];
-            int64_t vox[TC_WPG];
-#pragma unroll
-            for (int w = 0; w < TC_WPG; ++w) {
-                const int j = group + w * TC_EPI_GROUPS;
-                taddr[w] = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)((a * TC_SUB + j) * TC_N);
-                // voxel of row p (rows < 2^31: checked on the host); rows of the next x-slab belong to
-                // the next item of the column
-                const uint32_t up = q0 + (uint32_t)(j * TC_OUT + i);
-                const uint32_t xq = fastdiv(up, c.div_sx);
-                const uint32_t rem = up - xq * usx;
-                const uint32_t yq = fastdiv(rem, c.div_sy);
-                const uint32_t zq = rem - yq * usy;
-                prow[w] = up;
-                valid[w] = i >= 1 && i <= TC_OUT && xq == xk && yq - 1u < (uint32_t)c.ny && zq - 1u < (uint32_t)c.nz;
-                vox[w] = ((int64_t)(xq - 1) * c.ny + (yq - 1)) * (int64_t)c.nz + (zq - 1);
-            }
+            float* xb = xg + xp * (4 * 2 * 16);
+            const uint32_t taddr = tq + (uint32_t)(a * TC_CHUNK);
+            // voxel of row p (rows < 2^31: checked on the host); rows of the next x-plane belong to the
+            // next item of the column
+            const uint32_t up = q0 + (uint32_t)(win * TC_OUT + i);
+            const uint32_t xq = fastdiv(up, c.div_sx);
+            const uint32_t rem = up - xq * usx;
+            const uint32_t yq = fastdiv(rem, c.div_sy);
+            const uint32_t zq = rem - yq * usy;
+            const bool valid = i >= 1 && i <= TC_OUT && xq == xk && yq - 1u < (uint32_t)c.ny && zq - 1u < (uint32_t)c.nz;
+            const int64_t vox = ((int64_t)(xq - 1) * c.ny + (yq - 1)) * (int64_t)c.nz + (zq - 1);
             if (LAST) {
-                float zm[TC_WPG], z0[TC_WPG], zp[TC_WPG];
-#pragma unroll
-                for (int w = 0; w < TC_WPG; ++w) {
-                    zm[w] = tc_ld1(taddr[w]);
-                    z0[w] = tc_ld1(taddr[w] + 16);
-                    zp[w] = tc_ld1(taddr[w] + 32);
-                }
+                const float zm = tc_ld1(taddr);
+                const float z0 = tc_ld1(taddr + 16);
+                const float zp = tc_ld1(taddr + 32);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-                for (int w = 0; w < TC_WPG; ++w) {
-                    if (lane == 31) xb[((w * 4 + quarter) * 2 + 0) * 16] = zm[w];
-                    if (lane == 0) xb[((w * 4 + quarter) * 2 + 1) * 16] = zp[w];
-                }
+                if (lane == 31) xb[(quarter * 2 + 0) * 16] = zm;
+                if (lane == 0) xb[(quarter * 2 + 1) * 16] = zp;
                 epi_group_barrier(group);
-#pragma unroll
-                for (int w = 0; w < TC_WPG; ++w) {
-                    float lo = __shfl_up_sync(0xffffffffu, zm[w], 1);
-                    float hi = __shfl_down_sync(0xffffffffu, zp[w], 1);
-                    if (lane == 0 && quarter > 0) lo = xb[((w * 4 + quarter - 1) * 2 + 0) * 16];
-                    if (lane == 31 && quarter < 3) hi = xb[((w * 4 + quarter + 1) * 2 + 1) * 16];
-                    if (valid[w]) {
-                        const int64_t v = vox[w];
-                        float o = lo + z0[w] + hi;
-                        if (c.mask && c.mask[v] != 0.f) o = 0.f;
-                        if (c.dinv) o += c.omega * c.dinv[v] * c.r[v];
-                        c.w[v] = o;
-                    }
+                float lo = __shfl_up_sync(0xffffffffu, zm, 1);
+                float hi = __shfl_down_sync(0xffffffffu, zp, 1);
+                if (lane == 0 && quarter > 0) lo = xb[((quarter - 1) * 2 + 0) * 16];
+                if (lane == 31 && quarter < 3) hi = xb[((quarter + 1) * 2 + 1) * 16];
+                if (valid) {
+                    float o = lo + z0 + hi;
+                    if (c.mask && c.mask[vox] != 0.f) o = 0.f;
+                    if (c.dinv) o += c.omega * c.dinv[vox] * c.r[vox];
+                    c.w[vox] = o;
                 }
             } else {
-                float zm[TC_WPG][16], z0[TC_WPG][16], zp[TC_WPG][16];
-#pragma unroll
-                for (int w = 0; w < TC_WPG; ++w) {
-                    tc_ld16(taddr[w], zm[w]);
-                    tc_ld16(taddr[w] + 16, z0[w]);
-                    tc_ld16(taddr[w] + 32, zp[w]);
-                }
+                float zm[16], z0[16], zp[16];
+                tc_ld16(taddr, zm);
+                tc_ld16(taddr + 16, z0);
+                tc_ld16(taddr + 32, zp);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                float4* lo_dst = reinterpret_cast<float4*>(xb + (quarter * 2 + 0) * 16);
+                float4* hi_dst = reinterpret_cast<float4*>(xb + (quarter * 2 + 1) * 16);
+                if (lane == 31) {
 #pragma unroll
-                for (int w = 0; w < TC_WPG; ++w) {
-                    float4* lo_dst = reinterpret_cast<float4*>(xb + ((w * 4 + quarter) * 2 + 0) * 16);
-                    float4* hi_dst = reinterpret_cast<float4*>(xb + ((w * 4 + quarter) * 2 + 1) * 16);
-                    if (lane == 31) {
+                    for (int u = 0; u < 4; ++u) lo_dst[u] = make_float4(zm[4 * u], zm[4 * u + 1], zm[4 * u + 2], zm[4 * u + 3]);
+                }
+                if (lane == 0) {
 #pragma unroll
-                        for (int q = 0; q < 4; ++q)
-                            lo_dst[q] = make_float4(zm[w][4 * q], zm[w][4 * q + 1], zm[w][4 * q + 2], zm[w][4 * q + 3]);
-                    }
-                    if (lane == 0) {
-#pragma unroll
-                        for (int q = 0; q < 4; ++q)
-                            hi_dst[q] = make_float4(zp[w][4 * q], zp[w][4 * q + 1], zp[w][4 * q + 2], zp[w][4 * q + 3]);
-                    }
+                    for (int u = 0; u < 4; ++u) hi_dst[u] = make_float4(zp[4 * u], zp[4 * u + 1], zp[4 * u + 2], zp[4 * u + 3]);
                 }
                 epi_group_barrier(group);
+                float lo[16], hi[16];
 #pragma unroll
-                for (int w = 0; w < TC_WPG; ++w) {
-                    float lo[16], hi[16];
+                for (int u = 0; u < 16; ++u) {
+                    lo[u] = __shfl_up_sync(0xffffffffu, zm[u], 1);
+                    hi[u] = __shfl_down_sync(0xffffffffu, zp[u], 1);
+                }
+                if (lane == 0 && quarter > 0) {
+                    const float4* src = reinterpret_cast<const float4*>(xb + ((quarter - 1) * 2 + 0) * 16);
 #pragma unroll
-                    for (int q = 0; q < 16; ++q) {
-                        lo[q] = __shfl_up_sync(0xffffffffu, zm[w][q], 1);
-                        hi[q] = __shfl_down_sync(0xffffffffu, zp[w][q], 1);
-                    }
-                    if (lane == 0 && quarter > 0) {
-                        const float4* src = reinterpret_cast<const float4*>(xb + ((w * 4 + quarter - 1) * 2 + 0) * 16);
-#pragma unroll
-                        for (int q = 0; q < 4; ++q) {
-                            const float4 v = src[q];
-                            lo[4 * q] = v.x; lo[4 * q + 1] = v.y; lo[4 * q + 2] = v.z; lo[4 * q + 3] = v.w;
-                        }
-                    }
-                    if (lane == 31 && quarter < 3) {
-                        const float4* src = reinterpret_cast<const float4*>(xb + ((w * 4 + quarter + 1) * 2 + 1) * 16);
-#pragma unroll
-                        for (int q = 0; q < 4; ++q) {
-                            const float4 v = src[q];
-                            hi[4 * q] = v.x; hi[4 * q + 1] = v.y; hi[4 * q + 2] = v.z; hi[4 * q + 3] = v.w;
-                        }
-                    }
-                    if (valid[w]) {
-                        uint32_t pk[8];
-#pragma unroll
-                        for (int q = 0; q < 8; ++q) {
-                            const __nv_bfloat162 h2 =
-                                __floats2bfloat162_rn(fmaxf(lo[2 * q] + z0[w][2 * q] + hi[2 * q], 0.f),
-                                                      fmaxf(lo[2 * q + 1] + z0[w][2 * q + 1] + hi[2 * q + 1], 0.f));
-                            pk[q] = *reinterpret_cast<const uint32_t*>(&h2);
-                        }
-                        const int64_t p = prow[w];
-                        *reinterpret_cast<uint4*>(c.out + p * 16) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-                        *reinterpret_cast<uint4*>(c.out + (c.plane_rows + p) * 16) =
-                            make_uint4(pk[4], pk[5], pk[6], pk[7]);
+                    for (int u = 0; u < 4; ++u) {
+                        const float4 v = src[u];
+                        lo[4 * u] = v.x; lo[4 * u + 1] = v.y; lo[4 * u + 2] = v.z; lo[4 * u + 3] = v.w;
                     }
                 }
+                if (lane == 31 && quarter < 3) {
+                    const float4* src = reinterpret_cast<const float4*>(xb + ((quarter + 1) * 2 + 1) * 16);
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const float4 v = src[u];
+                        hi[4 * u] = v.x; hi[4 * u + 1] = v.y; hi[4 * u + 2] = v.z; hi[4 * u + 3] = v.w;
+                    }
+                }
+                if (valid) {
+                    uint32_t pk[8];
+#pragma unroll
+                    for (int u = 0; u < 8; ++u) {
+                        const __nv_bfloat162 h2 =
+                            __floats2bfloat162_rn(fmaxf(lo[2 * u] + z0[2 * u] + hi[2 * u], 0.f),
+                                                  fmaxf(lo[2 * u + 1] + z0[2 * u + 1] + hi[2 * u + 1], 0.f));
+                        pk[u] = *reinterpret_cast<const uint32_t*>(&h2);
+                    }
+                    const int64_t pr = up;
+                    *reinterpret_cast<uint4*>(c.out + pr * 16) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                    *reinterpret_cast<uint4*>(c.out + (c.plane_rows + pr) * 16) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+                }
             }
+            // the chunk starts the plane TC_RING items later at zero
+#pragma unroll
+            for (int h = 0; h < 3; ++h) tc_st16_zero(taddr + (uint32_t)(16 * h));
+            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
             xp ^= 1;
             tc_fence_before();
             __syncwarp();
@@ -575,7 +596,7 @@ GB_API int gb_conv3_fwd_tc(int nx, int ny, int nz, int last, const void* in, con
                "conv3_fwd_tc: planar padding too small");
     c.rows_bytes = (uint32_t)(rows * 16);
     c.block_bytes = 2 * c.rows_bytes;
-    const size_t fixed = TC_W_BYTES + TC_XCHG_BYTES + 256;
+    const size_t fixed = TC_W_BYTES + TC_XCHG_BYTES + 512;
     c.slots = (int)std::min<size_t>(TC_MAX_SLOTS, (TC_SMEM_LIMIT - fixed) / c.block_bytes);
     if (c.slots < TC_MIN_SLOTS) {
         gb::set_error("conv3_fwd_tc: grid too long in z (nz = %d) for the staged x-plane blocks", nz);

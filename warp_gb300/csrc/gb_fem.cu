@@ -18,6 +18,7 @@
 // 2 points per axis, exact for Q1 products) and scaled here by the per-cell coefficient; values
 // are rounded to fp32 once, like the reference's fp64-accumulated dispatch kernel.
 #include "gb_common.cuh"
+#include "gb_scan.cuh"
 
 namespace gb {
 
@@ -99,8 +100,19 @@ __device__ __forceinline__ void local_node(const Grid& g, int a, int& i, int& j,
 // One thread per (node, adjacent-cell slot): writes that pair's NPE triplets (trial nodes).
 // ncomp = 1: scalar diffusion, value = coef[cell] * K[a][b] (K: NPE x NPE)
 // ncomp = 3: linear elasticity, block(i,j) = lam[cell] * KL[(a,i),(b,j)] + mu[cell] * KM[(a,i),(b,j)]
+// Value of scalar (i, j) of the triplet (test node a, trial node b) of a cell: the fp32 element
+// tables (rounded once from the FP64 integrals) scaled by the cell's coefficients in fp32, with a
+// fixed operation order so every assembly route produces the same bits.
 template <int NCOMP>
-__global__ void k_q1_triplets(Grid g, const double* __restrict__ K0, const double* __restrict__ K1,
+__device__ __forceinline__ float q1_entry(const float* __restrict__ K0, const float* __restrict__ K1, int nd, int r,
+                                          int c, float c0, float c1)
+{
+    const float v = __fmul_rn(c0, K0[r * nd + c]);
+    return NCOMP == 3 ? __fmaf_rn(c1, K1[r * nd + c], v) : v;
+}
+
+template <int NCOMP>
+__global__ void k_q1_triplets(Grid g, const float* __restrict__ K0, const float* __restrict__ K1,
                               const float* __restrict__ coef0, float coef0_const, const float* __restrict__ coef1,
                               float coef1_const, int* __restrict__ rows, int* __restrict__ cols,
                               float* __restrict__ vals)
@@ -128,8 +140,8 @@ __global__ void k_q1_triplets(Grid g, const double* __restrict__ K0, const doubl
     const int64_t pair = pair_start(g, x, y, z) + s;
     const int cell = cell_index(g, cx, cy, cz);
     const int a = (g.dim == 2) ? ((x - cx) * 2 + (y - cy)) : ((x - cx) * 4 + (y - cy) * 2 + (z - cz));
-    const double c0 = coef0 ? (double)coef0[cell] : (double)coef0_const;
-    const double c1 = coef1 ? (double)coef1[cell] : (double)coef1_const;
+    const float c0 = coef0 ? coef0[cell] : coef0_const;
+    const float c1 = coef1 ? coef1[cell] : coef1_const;
     const int nd = npe * NCOMP;  // element matrix dimension
     for (int b = 0; b < npe; ++b) {
         int bi, bj, bk;
@@ -140,13 +152,169 @@ __global__ void k_q1_triplets(Grid g, const double* __restrict__ K0, const doubl
 #pragma unroll
         for (int i = 0; i < NCOMP; ++i) {
 #pragma unroll
+            for (int j = 0; j < NCOMP; ++j)
+                vals[tri * NCOMP * NCOMP + i * NCOMP + j] =
+                    q1_entry<NCOMP>(K0, K1, nd, a * NCOMP + i, b * NCOMP + j, c0, c1);
+        }
+    }
+}
+
+// Direct assembly of the Q1 bilinear form into compact BSR (no triplets, no sort).  Produces exactly
+// what k_q1_triplets + bsr_set_from_triplets + the run sums produce: row = test node; its candidate
+// blocks are generated in triplet order (adjacent cells in ascending cell index, then trial nodes in
+// element-local order), a triplet whose scalars are all zero is dropped when pruning (bits & 0x7FFFFFFF),
+// each block is the fp32 sum of its remaining triplets in that order (starting from the first one),
+// and blocks are stored in ascending column (node) order.  Thread layout: NCOMP = 1, one thread per
+// row; NCOMP = 3, a group of 4 lanes per block row (lanes 0..2 hold component rows i = 0..2, lane 3
+// mirrors lane 0 and writes nothing) that agree on each triplet's zero test with two shuffles.
+// Cells are visited by their offset (ox, oy, oz) in {-1, 0}^3 from the node, so every index is a
+// compile-time constant and the 27 (9 in 2-D) block accumulators live in registers.
+// FILL = false: counts[row] = number of blocks; FILL = true: write columns / values at offsets[row].
+constexpr int Q1_BSR_THREADS = 128;
+
+template <int DIM, int NCOMP, bool FILL>
+__device__ __forceinline__ void q1_bsr_row(Grid g, const float* __restrict__ K0, const float* __restrict__ K1,
+                                           const float* __restrict__ coef0, float coef0_const,
+                                           const float* __restrict__ coef1, float coef1_const, int prune,
+                                           int* __restrict__ counts, const int* __restrict__ offsets, int* s_cols,
+                                           float* s_vals)
+{
+    constexpr int NPE = DIM == 3 ? 8 : 4;
+    constexpr int ND = NPE * NCOMP;
+    constexpr int NNB = DIM == 3 ? 27 : 9;
+    constexpr int LPR = NCOMP == 3 ? 4 : 1;  // lanes per block row
+    const int64_t nnodes = (int64_t)(g.nx + 1) * (g.ny + 1) * (DIM == 3 ? g.nz + 1 : 1);
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int64_t node = t / LPR;
+    const int comp = (int)(t % LPR);
+    if (node >= nnodes) return;  // whole 4-lane groups leave together
+    const int ci = comp < NCOMP ? comp : 0;
+    const unsigned gmask = NCOMP == 3 ? (0xFu << (threadIdx.x & 28)) : 0u;
+    int x, y, z = 0;
+    if (DIM == 2) {
+        x = (int)(node / (g.ny + 1));
+        y = (int)(node % (g.ny + 1));
+    } else {
+        const int64_t pitch_x = (int64_t)(g.ny + 1) * (g.nz + 1);
+        x = (int)(node / pitch_x);
+        const int64_t rem = node - x * pitch_x;
+        y = (int)(rem / (g.nz + 1));
+        z = (int)(rem % (g.nz + 1));
+    }
+    float acc[NNB][NCOMP];
+    uint32_t has = 0;
+#pragma unroll
+    for (int k = 0; k < NNB; ++k)
+#pragma unroll
+        for (int j = 0; j < NCOMP; ++j) acc[k][j] = 0.f;
+#pragma unroll
+    for (int oc = 0; oc < (1 << DIM); ++oc) {
+        // cell offset from the node, ascending cell index: ox outermost, each -1 before 0
+        const int ox = (oc >> (DIM - 1)) - 1;
+        const int oy = DIM == 3 ? ((oc >> 1) & 1) - 1 : (oc & 1) - 1;
+        const int oz = DIM == 3 ? (oc & 1) - 1 : 0;
+        const int cx = x + ox, cy = y + oy, cz = z + oz;
+        const bool inside = cx >= 0 && cx < g.nx && cy >= 0 && cy < g.ny && (DIM == 2 || (cz >= 0 && cz < g.nz));
+        if (!inside) continue;  // uniform inside a lane group (same node)
+        const int cell = DIM == 2 ? cx * g.ny + cy : (cx * g.ny + cy) * g.nz + cz;
+        const float c0 = coef0 ? coef0[cell] : coef0_const;
+        const float c1 = coef1 ? coef1[cell] : coef1_const;
+        const int a = DIM == 2 ? (-ox) * 2 + (-oy) : (-ox) * 4 + (-oy) * 2 + (-oz);
+#pragma unroll
+        for (int b = 0; b < NPE; ++b) {
+            const int bi = DIM == 2 ? (b >> 1) : (b >> 2);
+            const int bj = DIM == 2 ? (b & 1) : ((b >> 1) & 1);
+            const int bk = DIM == 2 ? 0 : (b & 1);
+            const int k = DIM == 2 ? 3 * (ox + bi + 1) + (oy + bj + 1)
+                                   : 9 * (ox + bi + 1) + 3 * (oy + bj + 1) + (oz + bk + 1);
+            float v[NCOMP];
+            uint32_t nzbits = 0;
+#pragma unroll
             for (int j = 0; j < NCOMP; ++j) {
-                const int r = a * NCOMP + i, c = b * NCOMP + j;
-                double v = c0 * K0[r * nd + c];
-                if (NCOMP == 3) v += c1 * K1[r * nd + c];
-                vals[tri * NCOMP * NCOMP + i * NCOMP + j] = (float)v;
+                v[j] = q1_entry<NCOMP>(K0, K1, ND, a * NCOMP + ci, b * NCOMP + j, c0, c1);
+                nzbits |= __float_as_uint(v[j]) & 0x7FFFFFFFu;
+            }
+            if (NCOMP == 3) {
+                nzbits = comp < NCOMP ? nzbits : 0u;
+                nzbits |= __shfl_xor_sync(gmask, nzbits, 1);
+                nzbits |= __shfl_xor_sync(gmask, nzbits, 2);
+            }
+            if (!prune || nzbits != 0u) {
+                const bool first = !(has & (1u << k));
+#pragma unroll
+                for (int j = 0; j < NCOMP; ++j) acc[k][j] = first ? v[j] : acc[k][j] + v[j];
+                has |= 1u << k;
             }
         }
+    }
+    if (!FILL) {
+        if (comp == 0) counts[node] = __popc(has);
+        return;
+    }
+    // the CTA's rows are one contiguous range of blocks: stage them in shared memory (the kernel then
+    // copies the range out with coalesced stores)
+    const int base = offsets[(int64_t)blockIdx.x * (blockDim.x / LPR)];
+    int pos = offsets[node] - base;
+    const int64_t sy = DIM == 3 ? (g.nz + 1) : 1;
+    const int64_t sx = DIM == 3 ? (int64_t)(g.ny + 1) * (g.nz + 1) : (g.ny + 1);
+#pragma unroll
+    for (int k = 0; k < NNB; ++k) {
+        if (has & (1u << k)) {
+            const int dx = DIM == 3 ? k / 9 - 1 : k / 3 - 1;
+            const int dy = DIM == 3 ? (k / 3) % 3 - 1 : k % 3 - 1;
+            const int dz = DIM == 3 ? k % 3 - 1 : 0;
+            if (comp == 0) s_cols[pos] = (int)(node + dx * sx + dy * sy + dz);
+            if (comp < NCOMP) {
+#pragma unroll
+                for (int j = 0; j < NCOMP; ++j) s_vals[(pos * NCOMP + ci) * NCOMP + j] = acc[k][j];
+            }
+            ++pos;
+        }
+    }
+}
+
+// Coalesced copy of a CTA's staged blocks (see k_q1_bsr): called after the CTA's barrier.
+template <int NCOMP>
+__device__ __forceinline__ void q1_bsr_flush(int nblocks, int base, const int* s_cols, const float* s_vals,
+                                             int* __restrict__ columns, float* __restrict__ values)
+{
+    for (int t = threadIdx.x; t < nblocks; t += blockDim.x) columns[base + t] = s_cols[t];
+    for (int t = threadIdx.x; t < nblocks * NCOMP * NCOMP; t += blockDim.x)
+        values[(size_t)base * NCOMP * NCOMP + t] = s_vals[t];
+}
+
+template <int DIM, int NCOMP, bool FILL>
+__global__ void __launch_bounds__(Q1_BSR_THREADS) k_q1_bsr(Grid g, const float* __restrict__ K0g,
+                                                           const float* __restrict__ K1g,
+                                                           const float* __restrict__ coef0, float coef0_const,
+                                                           const float* __restrict__ coef1, float coef1_const,
+                                                           int prune, int* __restrict__ counts,
+                                                           const int* __restrict__ offsets, int* __restrict__ columns,
+                                                           float* __restrict__ values)
+{
+    constexpr int NPE = DIM == 3 ? 8 : 4;
+    constexpr int ND = NPE * NCOMP;
+    constexpr int NNB = DIM == 3 ? 27 : 9;
+    constexpr int LPR = NCOMP == 3 ? 4 : 1;
+    constexpr int ROWS = Q1_BSR_THREADS / LPR;
+    __shared__ float K0[ND * ND];
+    __shared__ float K1[NCOMP == 3 ? ND * ND : 1];
+    __shared__ int s_cols[FILL ? ROWS * NNB : 1];
+    __shared__ float s_vals[FILL ? ROWS * NNB * NCOMP * NCOMP : 1];
+    for (int t = threadIdx.x; t < ND * ND; t += blockDim.x) {
+        K0[t] = K0g[t];
+        if (NCOMP == 3) K1[t] = K1g[t];
+    }
+    __syncthreads();
+    q1_bsr_row<DIM, NCOMP, FILL>(g, K0, K1, coef0, coef0_const, coef1, coef1_const, prune, counts, offsets, s_cols,
+                                 s_vals);
+    if (FILL) {
+        const int64_t nnodes = (int64_t)(g.nx + 1) * (g.ny + 1) * (DIM == 3 ? g.nz + 1 : 1);
+        const int64_t row0 = (int64_t)blockIdx.x * ROWS;
+        const int64_t row1 = min(row0 + (int64_t)ROWS, nnodes);
+        __syncthreads();
+        const int base = offsets[row0];
+        q1_bsr_flush<NCOMP>(offsets[row1] - base, base, s_cols, s_vals, columns, values);
     }
 }
 
@@ -284,9 +452,9 @@ GB_API int64_t gb_q1_triplet_count(int dim, int nx, int ny, int nz)
     return cells * npe * npe;
 }
 
-// Q1 bilinear-form triplets.  ncomp = 1: K0 = unit-coefficient stiffness (NPE x NPE), coefficient
-// per cell (coef0) or constant.  ncomp = 3: K0 = lambda part, K1 = mu part (3NPE x 3NPE).
-GB_API int gb_q1_assemble_triplets(int dim, int nx, int ny, int nz, int ncomp, const double* K0, const double* K1,
+// Q1 bilinear-form triplets.  ncomp = 1: K0 = unit-coefficient stiffness (NPE x NPE, fp32), coefficient
+// per cell (coef0) or constant.  ncomp = 3: K0 = lambda part, K1 = mu part (3NPE x 3NPE, fp32).
+GB_API int gb_q1_assemble_triplets(int dim, int nx, int ny, int nz, int ncomp, const float* K0, const float* K1,
                                    const float* coef0, float coef0_const, const float* coef1, float coef1_const,
                                    int* rows, int* cols, float* vals, cudaStream_t stream)
 {
@@ -303,6 +471,60 @@ GB_API int gb_q1_assemble_triplets(int dim, int nx, int ny, int nz, int ncomp, c
     else
         k_q1_triplets<3><<<grid, 256, 0, stream>>>(g, K0, K1, coef0, coef0_const, coef1, coef1_const, rows, cols, vals);
     GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+// Upper bound (exact when nothing is pruned) of the blocks of the direct assembly: prod (3 m_d - 2).
+GB_API int64_t gb_q1_bsr_nnz_max(int dim, int nx, int ny, int nz)
+{
+    int64_t n = (int64_t)(3 * (nx + 1) - 2) * (3 * (ny + 1) - 2);
+    return dim == 3 ? n * (3 * (nz + 1) - 2) : n;
+}
+
+GB_API size_t gb_q1_assemble_bsr_workspace_bytes(int dim, int nx, int ny, int nz)
+{
+    return scan_workspace_bytes(grid_nodes(dim, nx, ny, nz) + 1);
+}
+
+// Direct compact-BSR assembly of the Q1 bilinear form (same tables and coefficients as
+// gb_q1_assemble_triplets): the matrix bsr_set_from_triplets builds from those triplets, bit for bit,
+// without writing or sorting them.  offsets: [nodes + 1]; columns / values: capacity
+// gb_q1_bsr_nnz_max(); bsr_nnz_host (optional) receives offsets[nodes] asynchronously.
+GB_API int gb_q1_assemble_bsr(int dim, int nx, int ny, int nz, int ncomp, const float* K0, const float* K1,
+                              const float* coef0, float coef0_const, const float* coef1, float coef1_const, int prune,
+                              int* offsets, int* columns, float* values, int* bsr_nnz_host, void* workspace,
+                              size_t workspace_bytes, cudaStream_t stream)
+{
+    GB_REQUIRE(dim == 2 || dim == 3, "q1_assemble_bsr: dim must be 2 or 3");
+    GB_REQUIRE(ncomp == 1 || ncomp == 3, "q1_assemble_bsr: ncomp must be 1 or 3");
+    GB_REQUIRE(nx > 0 && ny > 0 && (dim == 2 || nz > 0), "q1_assemble_bsr: empty grid");
+    GB_REQUIRE(K0 && offsets && columns && values && (ncomp == 1 || K1), "q1_assemble_bsr: null argument");
+    GB_REQUIRE(workspace_bytes >= gb_q1_assemble_bsr_workspace_bytes(dim, nx, ny, nz),
+               "q1_assemble_bsr: workspace too small");
+    Grid g{dim, nx, ny, dim == 3 ? nz : 0};
+    const int64_t nn = grid_nodes(dim, nx, ny, nz);
+    const int lpr = ncomp == 3 ? 4 : 1;
+    const int grid = (int)ceil_div<int64_t>(nn * lpr, Q1_BSR_THREADS);
+#define GB_Q1_BSR(D, C, F) \
+    k_q1_bsr<D, C, F><<<grid, Q1_BSR_THREADS, 0, stream>>>(g, K0, K1, coef0, coef0_const, coef1, coef1_const, prune, offsets + 1, \
+                                                offsets, columns, values)
+    // pass 1: blocks per row (into offsets[1..]); exclusive scan; pass 2: write the rows
+    GB_CHECK_CUDA(cudaMemsetAsync(offsets, 0, sizeof(int), stream));
+    if (dim == 3 && ncomp == 1) GB_Q1_BSR(3, 1, false);
+    else if (dim == 3) GB_Q1_BSR(3, 3, false);
+    else if (ncomp == 1) GB_Q1_BSR(2, 1, false);
+    else GB_Q1_BSR(2, 3, false);
+    GB_CHECK_CUDA(cudaGetLastError());
+    int rc = scan_i32(offsets + 1, offsets + 1, nn, true, workspace, stream);
+    if (rc) return rc;
+    if (dim == 3 && ncomp == 1) GB_Q1_BSR(3, 1, true);
+    else if (dim == 3) GB_Q1_BSR(3, 3, true);
+    else if (ncomp == 1) GB_Q1_BSR(2, 1, true);
+    else GB_Q1_BSR(2, 3, true);
+#undef GB_Q1_BSR
+    GB_CHECK_CUDA(cudaGetLastError());
+    if (bsr_nnz_host)
+        GB_CHECK_CUDA(cudaMemcpyAsync(bsr_nnz_host, offsets + nn, sizeof(int), cudaMemcpyDeviceToHost, stream));
     return GB_OK;
 }
 

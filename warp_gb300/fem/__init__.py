@@ -54,6 +54,11 @@ N.register("gb_q1_assemble_rhs", N._c_int,
            [N._c_int, N._c_int, N._c_int, N._c_int, N._c_int, N._vp, N._vp, _f32, _f32, _f32, N._vp, N._vp])
 N.register("gb_grid_boundary_mask", N._c_int,
            [N._c_int, N._c_int, N._c_int, N._c_int, N._c_int, N._c_int, N._c_int, N._vp, N._vp])
+N.register("gb_q1_bsr_nnz_max", N._c_i64, [N._c_int] * 4)
+N.register("gb_q1_assemble_bsr_workspace_bytes", N._c_sz, [N._c_int] * 4)
+N.register("gb_q1_assemble_bsr", N._c_int,
+           [N._c_int, N._c_int, N._c_int, N._c_int, N._c_int, N._vp, N._vp, N._vp, _f32, N._vp, _f32, N._c_int, N._vp,
+            N._vp, N._vp, N._vp, N._vp, N._c_sz, N._vp])
 N.register("gb_dirichlet_project", N._c_int,
            [N._c_int, N._c_int, N._vp, N._vp, N._vp, N._vp, N._vp, N._vp, N._vp, N._c_int, N._vp])
 
@@ -243,14 +248,14 @@ def integrate(integrand: Integrand, domain=None, quadrature=None, fields=None, v
     if integrand.name == "diffusion":
         if ncomp != 1:
             raise NotImplementedError("diffusion form on scalar spaces")
-        K0 = A.from_numpy(q1.stiffness(dim, h))
+        K0 = A.from_numpy(q1.stiffness(dim, h).astype(np.float32))
         K1 = None
         c0, c0c = _cell_array(values.get("nu", 1.0), ncells)
         c1, c1c = None, 0.0
     elif integrand.name == "mass":
         if ncomp != 1:
             raise NotImplementedError("mass form on scalar spaces")
-        K0 = A.from_numpy(q1.mass(dim, h))
+        K0 = A.from_numpy(q1.mass(dim, h).astype(np.float32))
         K1 = None
         c0, c0c = _cell_array(values.get("rho", 1.0), ncells)
         c1, c1c = None, 0.0
@@ -258,28 +263,51 @@ def integrate(integrand: Integrand, domain=None, quadrature=None, fields=None, v
         if ncomp != 3 or dim != 3:
             raise NotImplementedError("elasticity form on 3-D vector spaces")
         KL, KM = q1.elasticity(dim, h)
-        K0, K1 = A.from_numpy(KL), A.from_numpy(KM)
+        K0, K1 = A.from_numpy(KL.astype(np.float32)), A.from_numpy(KM.astype(np.float32))
         lam, mu = values.get("lame", (1.0, 1.0))
         c0, c0c = _cell_array(lam, ncells)
         c1, c1c = _cell_array(mu, ncells)
     else:
         raise NotImplementedError(integrand.name)
 
+    nnode = geo.node_count()
+    block_type = torch.float32 if ncomp == 1 else ((3, 3), torch.float32)
+    opts = dict(bsr_options or {})
+    construction = opts.pop("construction", "auto")
+    if construction not in ("triplets", "row_compress", "auto"):
+        raise ValueError(f"Unsupported BSR construction policy: {construction}")
+    prune = bool(opts.pop("prune_numerical_zeros", True))
+    if add and output is not None:
+        raise NotImplementedError("add=True is not supported")
+    if construction == "auto":
+        # the structure of a Q1 grid is known from the element: assemble the compact BSR directly (the
+        # matrix the triplet construction gives, bit for bit, without writing or sorting triplets)
+        mat = output if output is not None else sparse.bsr_zeros(nnode, nnode, block_type)
+        cap = int(L.gb_q1_bsr_nnz_max(dim, nx, ny, nz))
+        mat.offsets = A.empty(nnode + 1, torch.int32)
+        mat.columns = A.empty(cap, torch.int32)
+        mat.values = A.empty((cap,) if ncomp == 1 else (cap, ncomp, ncomp), torch.float32)
+        mat.row_counts = None
+        ws = A.workspace(int(L.gb_q1_assemble_bsr_workspace_bytes(dim, nx, ny, nz)))
+        if mat._nnz_host is None:
+            mat._nnz_host = torch.zeros(1, dtype=torch.int32, pin_memory=True)
+        N.check(L.gb_q1_assemble_bsr(dim, nx, ny, nz, ncomp, A.ptr(K0), A.ptr(K1), A.ptr(c0), c0c, A.ptr(c1), c1c,
+                                     int(prune), A.ptr(mat.offsets), A.ptr(mat.columns), A.ptr(mat.values),
+                                     mat._nnz_host.data_ptr(), ws.data_ptr(), ws.numel(), stream), "q1_assemble_bsr")
+        event = torch.cuda.Event()
+        event.record()
+        mat._nnz_event, mat._nnz_exact, mat.nnz = event, False, cap
+        mat._topology_version += 1
+        mat._keep_assembly = (K0, K1, c0, c1, ws)
+        return mat
     T = int(L.gb_q1_triplet_count(dim, nx, ny, nz))
     rows = A.empty(T, torch.int32)
     cols = A.empty(T, torch.int32)
     vals = A.empty((T,) if ncomp == 1 else (T, ncomp, ncomp), torch.float32)
     N.check(L.gb_q1_assemble_triplets(dim, nx, ny, nz, ncomp, A.ptr(K0), A.ptr(K1), A.ptr(c0), c0c, A.ptr(c1), c1c,
                                       A.ptr(rows), A.ptr(cols), A.ptr(vals), stream), "q1_assemble")
-    nnode = geo.node_count()
-    block_type = torch.float32 if ncomp == 1 else ((3, 3), torch.float32)
     mat = output if (output is not None and not add) else sparse.bsr_zeros(nnode, nnode, block_type)
-    opts = dict(bsr_options or {})
-    construction = opts.pop("construction", "triplets")
-    if construction not in ("triplets", "row_compress", "auto"):
-        raise ValueError(f"Unsupported BSR construction policy: {construction}")
-    prune = bool(opts.pop("prune_numerical_zeros", True))
-    if construction in ("row_compress", "auto"):
+    if construction == "row_compress":
         # the candidates come out row by row (test node, ascending element, trial node): they already
         # are the padded row layout of integrate.py:1664-1712, so only a row-local compression remains
         status = A.zeros(1, torch.int32)
@@ -293,8 +321,6 @@ def integrate(integrand: Integrand, domain=None, quadrature=None, fields=None, v
     else:
         sparse.bsr_set_from_triplets(mat, rows, cols, vals, prune_numerical_zeros=prune)
     mat._keep_assembly = (K0, K1, c0, c1)
-    if add and output is not None:
-        raise NotImplementedError("add=True is not supported")
     return mat
 
 

@@ -109,7 +109,7 @@ class MultigridPreconditioner:
             if self.bdim == 1:
                 space = fem.make_polynomial_space(cgeo, degree=1)
                 cA = fem.integrate(fem.diffusion_form, fields={"u": fem.make_trial(space), "v": fem.make_test(space)},
-                                   values={"nu": ccoef}, bsr_options={"construction": "row_compress"})
+                                   values={"nu": ccoef})
             else:
                 space = fem.make_polynomial_space(cgeo, degree=1, dtype="vec3")
                 nu = self.poisson
@@ -117,7 +117,7 @@ class MultigridPreconditioner:
                 mu = (ccoef * (1.0 / (2.0 * (1.0 + nu)))).contiguous()
                 cA = fem.integrate(fem.linear_elasticity_form,
                                    fields={"u": fem.make_trial(space), "v": fem.make_test(space)},
-                                   values={"lame": (lam, mu)}, bsr_options={"construction": "row_compress"})
+                                   values={"lame": (lam, mu)})
             rhs = A.zeros(cgeo.node_count() * self.bdim, torch.float32)
             bd = fem.BoundarySides(cgeo, self.faces)
             P = fem.integrate(fem.boundary_projector_form,

@@ -69,6 +69,12 @@ def block_type_repr(dt) -> str:
     return getattr(dt, "__name__", repr(dt))
 
 
+BSR_STATUS_SUCCESS = 0
+"""Sparse operation status code for success (reference ``sparse.py:82``)."""
+BSR_STATUS_ROW_CAPACITY_EXCEEDED = 1
+"""Sparse operation status code for insufficient padded row capacity (reference ``sparse.py:85``)."""
+
+
 class BsrMatrix:
     """BSR matrix with the reference's attributes (``warp/_src/sparse.py:103-463``).
 
@@ -76,7 +82,8 @@ class BsrMatrix:
         nrow, ncol: rows / columns of blocks.
         nnz: host-side upper bound of stored blocks (``nnz_sync()`` makes it exact).
         offsets: int32 tensor ``[nrow + 1]``.
-        row_counts: ``None`` (compact topology).
+        row_counts: ``None`` (compact topology) or int32 ``[nrow]`` active blocks per row (padded
+            topology: row r owns ``[offsets[r], offsets[r + 1])`` and uses its first ``row_counts[r]``).
         columns: int32 tensor (capacity >= nnz).
         values: tensor ``[capacity]`` for 1x1 blocks or ``[capacity, br, bc]``.
     """
@@ -95,6 +102,25 @@ class BsrMatrix:
         self._nnz_event = None
         self._nnz_exact = True
         self._topology_version = 0
+        self._status = None
+
+    def _ensure_status(self) -> torch.Tensor:
+        if self._status is None:
+            self._status = A.zeros(1, torch.int32)
+        return self._status
+
+    def status_sync(self) -> int:
+        """Sticky status of the sparse operations on this matrix (``BSR_STATUS_*``; reference
+        ``sparse.py:265``): a padded construction that ran out of row capacity sets it."""
+        if self._status is None:
+            return BSR_STATUS_SUCCESS
+        if torch.cuda.is_current_stream_capturing():
+            raise RuntimeError("BsrMatrix.status_sync() cannot read the status during a CUDA graph capture")
+        return int(self._status.item())
+
+    def clear_status(self) -> None:
+        if self._status is not None:
+            self._status.zero_()
 
     def _values_shape(self, cap):
         return (cap,) if self._block_shape == (1, 1) else (cap, *self._block_shape)
@@ -179,24 +205,84 @@ class BsrMatrix:
         return D
 
 
-def bsr_zeros(rows_of_blocks: int, cols_of_blocks: int, block_type=torch.float32, device=None) -> BsrMatrix:
-    """Empty BSR matrix (reference: ``sparse.py:639``)."""
+def bsr_zeros(rows_of_blocks: int, cols_of_blocks: int, block_type=torch.float32, device=None, *,
+              topology: str | None = None, row_capacity=None, nnz_capacity: int | None = None) -> BsrMatrix:
+    """Empty BSR matrix (reference: ``sparse.py:639-690``).  ``row_capacity`` (an int, or an int32
+    array of per-row capacities) gives the padded topology: every row owns that many block slots."""
+    if topology is None:
+        topology = "padded" if row_capacity is not None else "compact"
+    elif topology not in ("compact", "padded"):
+        raise ValueError(f"Unsupported topology policy: {topology}")
     shape, dt = _parse_block_type(block_type)
-    return BsrMatrix(rows_of_blocks, cols_of_blocks, shape, dt)
+    bsr = BsrMatrix(rows_of_blocks, cols_of_blocks, shape, dt)
+    _set_zero_topology(bsr, topology, row_capacity, nnz_capacity, preserve_row_capacity=False)
+    return bsr
+
+
+def _set_zero_topology(bsr: BsrMatrix, topology: str, row_capacity, nnz_capacity, preserve_row_capacity: bool):
+    """Reference: ``_bsr_set_zero_topology`` (``sparse.py:574-636``)."""
+    if nnz_capacity is not None and int(nnz_capacity) < 0:
+        raise ValueError("nnz_capacity must be nonnegative")
+    if row_capacity is not None and topology != "padded":
+        raise ValueError("row_capacity requires topology='padded'")
+    if topology == "padded":
+        if row_capacity is not None:
+            if isinstance(row_capacity, (int, np.integer)):
+                rc = int(row_capacity)
+                if rc < 0:
+                    raise ValueError("row_capacity must be nonnegative")
+                bsr.offsets = torch.arange(0, (bsr.nrow + 1) * rc, max(rc, 1), dtype=torch.int32,
+                                           device=A.device())[: bsr.nrow + 1] if rc > 0 else A.zeros(bsr.nrow + 1,
+                                                                                                   torch.int32)
+                cap = bsr.nrow * rc
+            else:
+                caps = A.as_tensor(row_capacity)
+                if caps.dim() != 1 or caps.shape[0] != bsr.nrow:
+                    raise ValueError(f"row_capacity array must have shape ({bsr.nrow},), got {tuple(caps.shape)}")
+                if caps.dtype != torch.int32:
+                    raise TypeError("row_capacity array must have dtype int32")
+                off = A.zeros(bsr.nrow + 1, torch.int32)
+                torch.cumsum(caps, 0, out=off[1:])
+                bsr.offsets = off
+                cap = int(nnz_capacity) if nnz_capacity is not None else int(off[-1].item())
+        elif preserve_row_capacity and bsr.row_counts is not None:
+            cap = bsr.capacity
+        else:
+            bsr.offsets = A.zeros(bsr.nrow + 1, torch.int32)
+            cap = 0
+        cap = max(cap, int(nnz_capacity or 0))
+        _ensure_fits(bsr, cap)
+        bsr.row_counts = A.zeros(bsr.nrow, torch.int32)
+        bsr._ensure_status()
+        bsr.nnz = cap if row_capacity is not None or preserve_row_capacity else 0
+    else:
+        bsr.offsets = A.zeros(bsr.nrow + 1, torch.int32)
+        bsr.row_counts = None
+        bsr.nnz = 0
+        if nnz_capacity:
+            _ensure_fits(bsr, int(nnz_capacity))
+    bsr._nnz_event = None
+    bsr._nnz_exact = True
+    bsr._topology_version += 1
 
 
 @A.on_caller_stream
-def bsr_set_zero(bsr: BsrMatrix, rows_of_blocks: int | None = None, cols_of_blocks: int | None = None, **kwargs):
+def bsr_set_zero(bsr: BsrMatrix, rows_of_blocks: int | None = None, cols_of_blocks: int | None = None, *,
+                 topology: str = "compact", row_capacity=None, nnz_capacity: int | None = None):
+    """Remove every block (reference: ``sparse.py:770-812``); ``topology="padded"`` keeps (or, with
+    ``row_capacity``, sets) the row capacity and empties every row."""
+    if topology not in ("compact", "padded", "masked"):
+        raise ValueError(f"Unsupported topology policy: {topology}")
+    if topology == "masked":
+        bsr.values.zero_()
+        return
+    resized = rows_of_blocks is not None and int(rows_of_blocks) != bsr.nrow
     if rows_of_blocks is not None:
         bsr.nrow = int(rows_of_blocks)
     if cols_of_blocks is not None:
         bsr.ncol = int(cols_of_blocks)
-    bsr.offsets = A.zeros(bsr.nrow + 1, torch.int32)
-    bsr.row_counts = None
-    bsr.nnz = 0
-    bsr._nnz_event = None
-    bsr._nnz_exact = True
-    bsr._topology_version += 1
+    _set_zero_topology(bsr, topology, row_capacity, nnz_capacity,
+                       preserve_row_capacity=(topology == "padded" and row_capacity is None and not resized))
 
 
 def _ensure_fits(bsr: BsrMatrix, nnz: int) -> None:
@@ -229,8 +315,6 @@ def bsr_set_from_triplets(
         raise ValueError(f"Unsupported topology policy: {topology}")
     elif masked and topology != "masked":
         raise ValueError("Cannot pass masked=True with a non-masked topology policy")
-    if topology == "padded":
-        raise NotImplementedError("padded BSR topology is not supported by this implementation")
     masked = topology == "masked"
 
     rows = A.as_tensor(rows)
@@ -263,7 +347,10 @@ def bsr_set_from_triplets(
         if masked:
             dest.values.zero_()
             return
-        bsr_set_zero(dest)
+        bsr_set_zero(dest, topology="padded" if topology == "padded" else "compact")
+        return
+    if topology == "padded":
+        _set_from_triplets_padded(dest, rows, columns, values, count, prune_numerical_zeros)
         return
 
     stream = A.stream()
@@ -359,6 +446,31 @@ def bsr_compress(src: BsrMatrix, prune_numerical_zeros: bool = True, inplace: bo
     return src
 
 
+def _set_from_triplets_padded(dest, rows, columns, values, count, prune_numerical_zeros):
+    """padded topology (reference ``sparse.py:1335-1420``): build the compact structure of the triplets,
+    write each row into dest's existing row capacity (rows that do not fit are left empty and raise
+    ``BSR_STATUS_ROW_CAPACITY_EXCEEDED``), then the block sums."""
+    if dest.row_counts is None:
+        # a compact matrix's rows become padded rows of their current extent
+        dest.row_counts = A.zeros(dest.nrow, torch.int32)
+    status = dest._ensure_status()
+    tmp = BsrMatrix(dest.nrow, dest.ncol, dest.block_shape, dest.scalar_type)
+    bsr_set_from_triplets(tmp, rows, columns, values, count, prune_numerical_zeros)
+    L = N.lib()
+    stream = A.stream()
+    cap = dest.capacity
+    block_map = A.empty(max(cap, 1), torch.int32) if values is not None else None
+    N.check(L.gb_bsr_scatter_padded(dest.nrow, A.ptr(tmp.offsets), A.ptr(tmp.columns), A.ptr(dest.offsets),
+                                    A.ptr(dest.row_counts), A.ptr(dest.columns), A.ptr(block_map), A.ptr(status),
+                                    stream), "bsr_scatter_padded")
+    if values is not None and cap > 0:
+        total = int(dest.offsets[dest.nrow].item()) if not torch.cuda.is_current_stream_capturing() else cap
+        N.check(L.gb_bsr_gather_blocks(A.gb_dtype(dest.scalar_type), dest.block_size, min(total, cap), A.ptr(block_map),
+                                       A.ptr(tmp.values), A.ptr(dest.values), stream), "bsr_gather_blocks")
+    dest._padded_temporaries = (tmp, block_map)
+    dest._topology_version += 1
+
+
 def _set_from_triplets_masked(dest, rows, columns, values, count, prune_numerical_zeros):
     """masked topology: keep dest's structure and sum only triplets that hit existing blocks."""
     nnz = int(rows.shape[0])
@@ -395,8 +507,9 @@ def _set_from_triplets_masked(dest, rows, columns, values, count, prune_numerica
     _scatter_sub_structure(dest, sub_off, mcols, sub_vals)
 
 
-def _scatter_sub_structure(dest, sub_off, sub_cols, sub_vals):
-    """dest.values[block(r, c)] = sub_vals[k] for every block k = (r, c) of the sub-structure."""
+def _scatter_sub_structure(dest, sub_off, sub_cols, sub_vals, add: bool = False):
+    """dest.values[block(r, c)] = sub_vals[k] (``add``: += ) for every block k = (r, c) of the
+    sub-structure."""
     n_sub = int(sub_off[dest.nrow].item())
     if n_sub == 0:
         return
@@ -406,7 +519,10 @@ def _scatter_sub_structure(dest, sub_off, sub_cols, sub_vals):
     keys_dest = dest.uncompress_rows().long() * dest.ncol + dest.columns[: int(dest.offsets[dest.nrow].item())].long()
     keys_sub = sub_rows * dest.ncol + sub_cols[:n_sub].long()
     pos = torch.searchsorted(keys_dest, keys_sub)
-    dest.values[pos] = sub_vals[:n_sub]
+    if add:
+        dest.values[pos] += sub_vals[:n_sub]
+    else:
+        dest.values[pos] = sub_vals[:n_sub]
 
 
 @A.on_caller_stream
@@ -568,4 +684,4 @@ def bsr_mm(x: BsrMatrix, y: BsrMatrix, z: BsrMatrix | None = None, alpha: float 
     """
     from .spgemm import bsr_mm as _mm
 
-    return _mm(x, y, z, alpha=alpha, beta=beta, masked=masked)
+    return _mm(x, y, z, alpha=alpha, beta=beta, masked=masked, topology=topology)
