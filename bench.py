@@ -432,10 +432,27 @@ def bench_elasticity_large(args, hbm_peak):
     out["mg_fcg_fp32_rel_residual"] = infos[-1]["rel_residual"]
     out["mg_fcg_fp32_converged"] = infos[-1]["converged"]
     out["mg_fcg_fp32_fallbacks"] = solver.fallbacks
+    # bf16 matrix values inside the V-cycle (fine level), fp32 values in the flexible solver's product
+    del mg, solver
+    torch.cuda.empty_cache()
+    mg16 = multigrid.MultigridPreconditioner(A, s.geo, s.coef, faces=("x-",), fine_values=torch.bfloat16)
+    solver16 = linear.RefinedSolver(A, M=mg16, method="fcg", inner_tol=args.inner_tol, inner_maxiter=5000)
+    solver16.solve(s.b, tol=1e-8, max_outer=10)
+    infos16, xs16 = [], []
+
+    def solve16():
+        x_, info_ = solver16.solve(s.b, tol=1e-8, max_outer=10)
+        infos16.append(info_)
+        xs16.append(x_)
+
+    out["mg_fcg_bf16_vcycle_ms"] = _event_ms(solve16, 2, warmup=0)
+    out["mg_fcg_bf16_vcycle_inner_iterations"] = infos16[-1]["inner_iterations"]
+    out["mg_fcg_bf16_vcycle_converged"] = infos16[-1]["converged"]
+    out["mg_fcg_bf16_vcycle_oracle_rel_residual"] = _oracle_residual_3x3(A, s.b, xs16[-1])
     out["note"] = ("flexible CG with the vec3 geometric V-cycle (point-Jacobi smoothing, damping 4/(3 rho) per "
-                   "level), FP32 values; bf16 values are measured for the SpMV only -- as the inner operator of "
-                   "the refined solve they diverge on this field (sigma 1.5); the 3-channel conv-net smoother "
-                   "for this configuration is not built")
+                   "level); fp32 values, and bf16 fine-level values inside the V-cycle with fp32 values in the "
+                   "flexible solver's product (bf16 values as the refinement's inner operator diverge on this "
+                   "field, sigma 1.5); the 3-channel conv-net smoother for this configuration is not built")
     return out
 
 

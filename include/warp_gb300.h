@@ -199,10 +199,11 @@ int gb_dirichlet_project(int bdim, int nrow, const int* offsets, const int* colu
  * r.z <= 0) stops the loop with GB_DEV_STAGNATION so the caller can fall back to Jacobi-CG. */
 typedef int (*gb_precond_fn)(void* user, gb_stream_t stream, const float* r, float* z);
 int gb_krylov_set_precond(void* handle, gb_precond_fn fn, void* user, int stag_window, double stag_factor);
-/* z_out = z + omega * dinv * (r - A z) (fused Jacobi smoothing step; z_out may not alias z). */
+/* z_out = z + omega * dinv * (r - A z) (fused Jacobi smoothing step; z_out may not alias z; fp32 or bf16
+ * values). */
 int gb_bsr_jacobi_smooth(int bdim, int nrow, int64_t nnz, int64_t ncap, const int* offsets, const int* columns,
-                         const float* values, const float* r, const float* z, const float* dinv, float omega,
-                         float* z_out, int* status, gb_stream_t stream);
+                         const void* values, int val_dtype, const float* r, const float* z, const float* dinv,
+                         float omega, float* z_out, int* status, gb_stream_t stream);
 /* Vertex-centred 2:1 transfers on Q1 node grids (nodes per axis; masks 1 = Dirichlet, may be NULL). */
 int gb_mg_restrict(int fnx, int fny, int fnz, int cnx, int cny, int cnz, const float* r, const float* fmask,
                    const float* cmask, float* rc, gb_stream_t stream);
@@ -239,18 +240,22 @@ int gb_conv3_bwd_weight_f32(int nx, int ny, int nz, int cin, int cout, const flo
 int gb_relu_bwd(int64_t n, const float* out, float* g, gb_stream_t stream);
 int gb_adam_step(int n, float* w, const float* g, float* m, float* v, float lr, float b1, float b2, float eps, int step,
                  void* w_bf16, gb_stream_t stream);
-int gb_net_features(int dtype, int64_t n, const float* r, const float* dinv, const float* chat, const float* mask,
-                    void* out, gb_stream_t stream);
+int gb_net_features(int dtype, int ncomp, int64_t n, const float* r, const float* dinv, const float* chat,
+                    const float* mask, void* out, gb_stream_t stream);
 int gb_net_cell_features(int nx, int ny, int nz, const float* cell_coef, float mean_log, float inv_std, float* chat,
                          gb_stream_t stream);
-int gb_net_combine(int dtype, int64_t n, int stride, const void* act, const float* mask, float omega, const float* dinv,
-                   const float* r, float* out, gb_stream_t stream);
+int gb_net_combine(int dtype, int ncomp, int64_t n, int stride, const void* act, const float* mask, float omega,
+                   const float* dinv, const float* r, float* out, gb_stream_t stream);
 /* tcgen05 implicit-GEMM layers on the planar padded layout: the grid padded by one zero voxel per side,
  * row p = ((x+1)(ny+2) + (y+1))(nz+2) + (z+1), channels 0-7 in plane 0 and 8-15 in plane 1 (16 B per row),
  * planes gb_conv3_planar_rows() rows apart, border rows zero.  last = 0: ReLU layer, planar bf16 out;
- * last = 1: w = omega dinv r + (mask ? 0 : channel 0) in fp32.  Wt: [27][16][16] bf16. */
+ * last = 1: w = omega dinv r + (mask ? 0 : channel 0) in fp32; last = 3 (vec3 fields, 3 interleaved dofs per
+ * node): w[3v+c] = omega dinv[3v+c] r[3v+c] + (mask[v] ? 0 : channel c).  Wt: [27][16][16] bf16.
+ * Features (gb_net_features*): ncomp = 1 scalar fields (x = dinv r and x times the 8 adjacent cells'
+ * normalised log-coefficients), ncomp = 3 vec3 fields (x_c and x_c times the mean and x/y/z contrasts of
+ * those 8 values).  gb_net_combine: out[dof] = omega dinv r + (mask[node] ? 0 : act[node][c]). */
 int64_t gb_conv3_planar_rows(int nx, int ny, int nz);
-int gb_net_features_planar(int nx, int ny, int nz, const float* r, const float* dinv, const float* chat,
+int gb_net_features_planar(int ncomp, int nx, int ny, int nz, const float* r, const float* dinv, const float* chat,
                            const float* mask, void* out, gb_stream_t stream);
 int gb_conv3_fwd_tc(int nx, int ny, int nz, int last, const void* in, const void* Wt, void* out, float* w,
                     const float* r, const float* dinv, const float* mask, float omega, int* status, gb_stream_t stream);
@@ -315,6 +320,16 @@ int gb_batched_pcg2(int nbatch, const int* batch_offsets, const int* order, int6
                     double atol, int maxiter, int x_is_zero, int threads, int lanes_per_row, int small_rows,
                     int smem_rows, int grid, int* iters, float* rr, float* atol_sq, void* workspace,
                     size_t workspace_bytes, int* status, gb_stream_t stream);
+/* gb_batched_bicgstab replaces BiCGSTAB with batch_offsets (warp/_src/optim/linear.py:1377-1574; per-subproblem
+ * tolerances :2063-2083): the same persistent queue of subproblems, one CTA per subproblem running its
+ * BiCGSTAB (right preconditioning, left with left_precond; Jacobi dinv or none) to its own tolerance.
+ * Workspace: gb_batched_bicgstab_workspace_bytes(n) (8 work vectors). */
+size_t gb_batched_bicgstab_workspace_bytes(int64_t n);
+int gb_batched_bicgstab(int nbatch, const int* batch_offsets, const int* order, int64_t n, const int* offsets,
+                        const int* columns, const float* values, const float* dinv, const float* b, float* x,
+                        double rtol, double atol, int maxiter, int x_is_zero, int left_precond, int threads,
+                        int lanes_per_row, int grid, int* iters, float* rr, float* atol_sq, void* workspace,
+                        size_t workspace_bytes, int* status, gb_stream_t stream);
 int gb_q1_batched_assemble_2d(int nbatch, const int* ncell, const int* row_off, const int* nnz_off,
                               const int* cell_off, const float* coef, const float* f, int total_rows, int* offsets,
                               int* columns, float* values, float* rhs, gb_stream_t stream);

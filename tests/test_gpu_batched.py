@@ -231,3 +231,75 @@ def test_batched_shared_vectors_are_bit_identical(cuda, lanes):
     for sv in (600, 16896):
         assert torch.equal(out[sv][0], out[0][0]) and torch.equal(out[sv][1], out[0][1])
         assert torch.equal(out[sv][2], out[0][2])
+
+
+@pytest.mark.parametrize("left", [False, True])
+def test_batched_bicgstab_each_subproblem_converges(cuda, left):
+    """Batched BiCGSTAB (reference: BiCGSTAB with batch_offsets, linear.py:1377-1574): one launch,
+    every subproblem meets its own tolerance; with right preconditioning the iteration counts follow
+    the oracle's restatement of the same BiCGSTAB run per subproblem."""
+    from warp_gb300 import batched
+    from warp_gb300.optim import linear
+
+    ncells = [16, 3, 40, 8, 25, 12, 2, 33, 20, 6]
+    Am, b, offs = batched.q1_batch_2d(ncells, seed=5)
+    offs_h = offs.cpu().numpy()
+    M = linear.preconditioner(Am, "diag")
+    x = torch.zeros_like(b)
+    op = linear.aslinearoperator(Am, batch_offsets=offs, max_batch_length=int(np.diff(offs_h).max()))
+    state = linear.bicgstab(op, b, x, tol=1e-6, atol=0.0, maxiter=2000, M=M, check_every=0,
+                            is_left_preconditioner=left, run=False)
+    it, rr, atol_sq = state()
+    bat = state._batched.iters.cpu().numpy()
+    assert rr.shape == (len(ncells),)
+    assert bool((rr <= atol_sq).all()), (rr, atol_sq)
+    assert int(torch.as_tensor(it).max()) < 2000
+    nnz = Am.nnz_sync()
+    off = Am.offsets.cpu().numpy()
+    col = Am.columns[:nnz].cpu().numpy()
+    val = Am.values[:nnz].cpu().numpy()
+    bh = b.cpu().numpy()
+    xh = x.cpu().numpy().astype(np.float64)
+    for i in range(len(ncells)):
+        r0, r1 = int(offs_h[i]), int(offs_h[i + 1])
+        k0, k1 = off[r0], off[r1]
+        o = off[r0:r1 + 1] - k0
+        c = col[k0:k1] - r0
+        v = val[k0:k1]
+        res = np.linalg.norm(oracle.bsr_mv_f64(o, c, v, xh[r0:r1]) - bh[r0:r1])
+        assert res <= 32 * 1e-6 * np.linalg.norm(bh[r0:r1]) + 1e-12, (i, res)
+        if not left:
+            _, it_ref, _, _ = oracle.bicgstab_f32(o, c, v, bh[r0:r1], inv_diag=oracle.inverse_diagonal_f32(o, c, v),
+                                                  tol=1e-6, atol=0.0, maxiter=2000)
+            assert abs(int(bat[i]) - it_ref) <= max(3, 0.1 * it_ref), (i, bat[i], it_ref)
+
+
+def test_batched_bicgstab_nonsymmetric_dense_blocks_and_inactive_tail(cuda):
+    """Nonsymmetric diagonally dominant dense blocks (BiCGSTAB's domain), per-batch residuals, and rows
+    past batch_offsets[-1] left untouched."""
+    from warp_gb300.optim import linear
+
+    rng = np.random.default_rng(3)
+    sizes = [8, 15, 10, 12]
+    n = sum(sizes) + 3
+    Ad = np.zeros((n, n), np.float32)
+    bd = rng.standard_normal(n).astype(np.float32)
+    o = 0
+    for s in sizes:
+        Ad[o:o + s, o:o + s] = (rng.standard_normal((s, s)) + 2.0 * s * np.eye(s)).astype(np.float32)
+        o += s
+    offs = torch.tensor(np.concatenate([[0], np.cumsum(sizes)]), dtype=torch.int32, device="cuda")
+    op = linear.aslinearoperator(torch.from_numpy(Ad).cuda(), batch_offsets=offs, max_batch_length=max(sizes))
+    b = torch.from_numpy(bd).cuda()
+    x = torch.zeros_like(b)
+    x[-3:] = torch.tensor([7.0, 8.0, 9.0], device="cuda")
+    niter, err, atol = linear.bicgstab(op, b, x, tol=1e-5, atol=0.0, maxiter=500, check_every=1)
+    assert err <= atol
+    xh = x.cpu().numpy().astype(np.float64)
+    o = 0
+    for s in sizes:
+        sl = slice(o, o + s)
+        res = np.linalg.norm(Ad[sl, sl].astype(np.float64) @ xh[sl] - bd[sl])
+        assert res <= 32 * 1e-5 * np.linalg.norm(bd[sl])
+        o += s
+    np.testing.assert_array_equal(x.cpu().numpy()[-3:], [7.0, 8.0, 9.0])

@@ -131,3 +131,30 @@ def test_refined_solver_stops_when_reduced_precision_corrections_diverge(cuda):
     assert not infow["converged"] and infow["outer"] < 10, infow["history"]
     assert infow["rel_residual"] <= infow["history"][0] * (1 + 1e-6) or infow["rel_residual"] <= 1e-8, \
         infow["history"]
+
+
+def test_bf16_values_inside_the_vcycle_converge_on_the_rough_field(cuda):
+    """bf16 matrix values inside the V-cycle only (the flexible solver's product keeps fp32): on the
+    rough field where bf16 inner operators make the refinement diverge, the solve still reaches the
+    FP64 target, checked on the host, with close to the fp32 cycle's iteration count."""
+    from warp_gb300 import multigrid, problems
+    from warp_gb300.optim import linear
+
+    s = problems.elasticity((32,) * 3, sigma=1.5, corr_length=0.05, seed=0)
+    A = s.A
+    nnz = A.nnz_sync()
+    mg32 = multigrid.MultigridPreconditioner(A, s.geo, s.coef, faces=FACES)
+    mg16 = multigrid.MultigridPreconditioner(A, s.geo, s.coef, faces=FACES, fine_values=torch.bfloat16)
+    assert mg16.levels[0].vals.dtype == torch.bfloat16 and mg16.levels[1].vals.dtype == torch.float32
+    x32, i32 = linear.RefinedSolver(A, M=mg32, method="fcg", inner_maxiter=3000).solve(s.b, tol=1e-8)
+    x16, i16 = linear.RefinedSolver(A, M=mg16, method="fcg", inner_maxiter=3000).solve(s.b, tol=1e-8)
+    assert i32["converged"] and i16["converged"], (i32, i16)
+    assert i16["inner_iterations"] <= 1.5 * i32["inner_iterations"] + 5, (i16, i32)
+    sp = pytest.importorskip("scipy.sparse")
+    n = A.nrow * 3
+    Ah = sp.bsr_matrix((A.values[:nnz].cpu().numpy().astype(np.float64).reshape(-1, 3, 3),
+                        A.columns[:nnz].cpu().numpy(), A.offsets.cpu().numpy()), shape=(n, n))
+    bd = s.b.cpu().numpy().astype(np.float64)
+    res = np.linalg.norm(bd - Ah @ x16.cpu().numpy()) / np.linalg.norm(bd)
+    assert res <= 2e-8, res
+    assert int(mg16.status.item()) == 0

@@ -156,17 +156,17 @@ def test_features_and_combine_match_oracle(cuda):
     mask = (rng.uniform(size=n) < 0.2).astype(np.float32)
     rd, dd, md = _dev(r), _dev(dinv), _dev(mask)
     f = torch.empty(n * 16, device="cuda")
-    N.check(L.gb_net_features(N.GB_F32, n, rd.data_ptr(), dd.data_ptr(), chat.data_ptr(), md.data_ptr(), f.data_ptr(),
+    N.check(L.gb_net_features(N.GB_F32, 1, n, rd.data_ptr(), dd.data_ptr(), chat.data_ptr(), md.data_ptr(), f.data_ptr(),
                               STREAM()))
     ref_f = C.features(r, dinv, ref_chat, mask)
     np.testing.assert_allclose(f.cpu().numpy().reshape(n, 16), ref_f, rtol=1e-5, atol=1e-6)
     fb = torch.empty(n * 16, dtype=torch.bfloat16, device="cuda")
-    N.check(L.gb_net_features(N.GB_BF16, n, rd.data_ptr(), dd.data_ptr(), chat.data_ptr(), md.data_ptr(),
+    N.check(L.gb_net_features(N.GB_BF16, 1, n, rd.data_ptr(), dd.data_ptr(), chat.data_ptr(), md.data_ptr(),
                               fb.data_ptr(), STREAM()))
     np.testing.assert_allclose(fb.float().cpu().numpy().reshape(n, 16), ref_f, rtol=8e-3, atol=1e-6)
     act = rng.standard_normal(n).astype(np.float32)
     out = torch.empty(n, device="cuda")
-    N.check(L.gb_net_combine(N.GB_F32, n, 1, _dev(act).data_ptr(), md.data_ptr(), 0.6, dd.data_ptr(), rd.data_ptr(),
+    N.check(L.gb_net_combine(N.GB_F32, 1, n, 1, _dev(act).data_ptr(), md.data_ptr(), 0.6, dd.data_ptr(), rd.data_ptr(),
                              out.data_ptr(), STREAM()))
     np.testing.assert_allclose(out.cpu().numpy(), C.combine(act, mask, 0.6, dinv, r), rtol=1e-5, atol=1e-6)
 

@@ -53,7 +53,7 @@ def test_padded_rows_hold_the_compact_rows(cuda, bdim):
     y = sparse.bsr_mv(P, x)
     exp = oracle.bsr_mv_f64(o["offsets"], o["columns"], ov.reshape(-1), x.cpu().numpy().astype(np.float64),
                             block_shape=(bdim, bdim))
-    np.testing.assert_allclose(y.cpu().numpy(), exp, rtol=1e-5, atol=1e-5 * np.abs(exp).max())
+    np.testing.assert_allclose(y.cpu().numpy().reshape(-1), exp, rtol=1e-5, atol=1e-5 * np.abs(exp).max())
 
 
 def test_rows_over_capacity_are_emptied_and_raise_the_status(cuda):

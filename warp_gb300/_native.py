@@ -70,8 +70,8 @@ _SIGNATURES = {
                                 _vp, _vp, _c_sz, _vp, _vp]),
     "gb_update_solution": (_c_int, [_c_i64, _vp, _vp, _vp, _c_dbl, _vp]),
     "gb_krylov_set_precond": (_c_int, [_vp, _vp, _vp, _c_int, _c_dbl]),
-    "gb_bsr_jacobi_smooth": (_c_int, [_c_int, _c_int, _c_i64, _c_i64, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_float,
-                                      _vp, _vp, _vp]),
+    "gb_bsr_jacobi_smooth": (_c_int, [_c_int, _c_int, _c_i64, _c_i64, _vp, _vp, _vp, _c_int, _vp, _vp, _vp,
+                                      ctypes.c_float, _vp, _vp, _vp]),
     "gb_mg_restrict": (_c_int, [_c_int] * 6 + [_vp, _vp, _vp, _vp, _vp]),
     "gb_mg_restrict_c": (_c_int, [_c_int] * 7 + [_vp, _vp, _vp, _vp, _vp]),
     "gb_mg_prolong_add_c": (_c_int, [_c_int] * 7 + [_vp, _vp, ctypes.c_float, _vp, _vp]),
@@ -95,15 +95,18 @@ _SIGNATURES = {
     "gb_relu_bwd": (_c_int, [_c_i64, _vp, _vp, _vp]),
     "gb_adam_step": (_c_int, [_c_int, _vp, _vp, _vp, _vp, ctypes.c_float, ctypes.c_float, ctypes.c_float,
                               ctypes.c_float, _c_int, _vp, _vp]),
-    "gb_net_features": (_c_int, [_c_int, _c_i64, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "gb_net_features": (_c_int, [_c_int, _c_int, _c_i64, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gb_net_cell_features": (_c_int, [_c_int, _c_int, _c_int, _vp, ctypes.c_float, ctypes.c_float, _vp, _vp]),
-    "gb_net_combine": (_c_int, [_c_int, _c_i64, _c_int, _vp, _vp, ctypes.c_float, _vp, _vp, _vp, _vp]),
+    "gb_net_combine": (_c_int, [_c_int, _c_int, _c_i64, _c_int, _vp, _vp, ctypes.c_float, _vp, _vp, _vp, _vp]),
     "gb_conv3_planar_rows": (_c_i64, [_c_int] * 3),
-    "gb_net_features_planar": (_c_int, [_c_int] * 3 + [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "gb_net_features_planar": (_c_int, [_c_int] * 4 + [_vp, _vp, _vp, _vp, _vp, _vp]),
     "gb_conv3_fwd_tc": (_c_int, [_c_int] * 4 + [_vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_float, _vp, _vp]),
     "gb_batched_pcg_workspace_bytes": (_c_sz, [_c_i64]),
     "gb_batched_pcg": (_c_int, [_c_int, _vp, _vp, _c_i64, _vp, _vp, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _c_int, _c_int,
                                 _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_sz, _vp, _vp]),
+    "gb_batched_bicgstab_workspace_bytes": (_c_sz, [_c_i64]),
+    "gb_batched_bicgstab": (_c_int, [_c_int, _vp, _vp, _c_i64, _vp, _vp, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _c_int,
+                                     _c_int, _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_sz, _vp, _vp]),
     "gb_batched_pcg2": (_c_int, [_c_int, _vp, _vp, _c_i64, _vp, _vp, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _c_int,
                                  _c_int, _c_int, _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_sz, _vp, _vp]),
     "gb_multi_dot_workspace_bytes": (_c_sz, [_c_int]),

@@ -52,6 +52,8 @@ class BatchedCG:
         use_cuda_graph: capture the launch into a CUDA graph on the first solve and replay it.
     """
 
+    method = "cg"
+
     def __init__(self, Am: sparse.BsrMatrix, batch_offsets, inv_diag=None, rtol: float = 1e-6, atol: float = 0.0,
                  maxiter: int = 0, config=None, use_cuda_graph: bool = True):
         if Am.block_shape != (1, 1) or Am.scalar_type != torch.float32 or Am.row_counts is not None:
@@ -83,7 +85,7 @@ class BatchedCG:
             self._autotune_pending = False
         self.use_cuda_graph = bool(use_cuda_graph)
         L = N.lib()
-        self._ws = A.zeros(int(L.gb_batched_pcg_workspace_bytes(self.n)), torch.uint8)
+        self._ws = A.zeros(int(self._workspace_bytes(L)), torch.uint8)
         B = max(self.nbatch, 1)
         self.iters = A.zeros(B, torch.int32)
         self.rr = A.zeros(B, torch.float32)
@@ -92,6 +94,9 @@ class BatchedCG:
         self._graph = None
         self._graph_key = None
         self.launches = 0
+
+    def _workspace_bytes(self, L) -> int:
+        return L.gb_batched_pcg_workspace_bytes(self.n)
 
     def _launch(self, b: torch.Tensor, x: torch.Tensor, cfg, stream) -> None:
         Am = self.A
@@ -135,6 +140,35 @@ class BatchedCG:
     def results(self):
         """(max iterations over subproblems [1], r.r [B], atol^2 [B]) as device tensors."""
         return self.iters.max().reshape(1), self.rr, self.atol_sq
+
+
+class BatchedBiCGSTAB(BatchedCG):
+    """Persistent batched BiCGSTAB (Jacobi or no preconditioner, right or left preconditioning) on the
+    same block-diagonal layout: one CTA per subproblem, each to its own tolerance (reference: BiCGSTAB
+    with ``batch_offsets``, ``warp/_src/optim/linear.py:1377-1574``).  ``config``: threads and lanes per
+    row (the autotuner's CG table does not apply; default 256 threads, 1 lane per row)."""
+
+    method = "bicgstab"
+
+    def __init__(self, Am: sparse.BsrMatrix, batch_offsets, inv_diag=None, rtol: float = 1e-6, atol: float = 0.0,
+                 maxiter: int = 0, left_precond: bool = False, config=None, use_cuda_graph: bool = True):
+        self.left_precond = bool(left_precond)
+        super().__init__(Am, batch_offsets, inv_diag, rtol, atol, maxiter,
+                         config=dict(config) if isinstance(config, dict) else dict(DEFAULT_CONFIG),
+                         use_cuda_graph=use_cuda_graph)
+
+    def _workspace_bytes(self, L) -> int:
+        return L.gb_batched_bicgstab_workspace_bytes(self.n)
+
+    def _launch(self, b: torch.Tensor, x: torch.Tensor, cfg, stream) -> None:
+        Am = self.A
+        N.check(N.lib().gb_batched_bicgstab(
+            self.nbatch, A.ptr(self.batch_offsets), A.ptr(self.order), self.n, A.ptr(Am.offsets), A.ptr(Am.columns),
+            A.ptr(Am.values), A.ptr(self.inv_diag), A.ptr(b), A.ptr(x), self.rtol, self.atol, self.maxiter, 0,
+            int(self.left_precond), int(cfg["threads"]), int(cfg["lanes_per_row"]), int(cfg.get("grid", 0)),
+            A.ptr(self.iters), A.ptr(self.rr), A.ptr(self.atol_sq), A.ptr(self._ws), self._ws.numel(),
+            A.ptr(self.status), stream), "batched_bicgstab")
+        self.launches += 2
 
 
 def autotune(solver: BatchedCG, b: torch.Tensor, x: torch.Tensor, candidates=None, repeats: int = 1, log=None):

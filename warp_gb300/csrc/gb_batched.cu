@@ -34,6 +34,8 @@ struct BatchArgs {
     float* r;
     float* p;
     float* Ap;
+    float *r0, *v, *t, *y, *z;  // BiCGSTAB only
+    int left_precond;           // BiCGSTAB: left (1) or right (0) preconditioning
     float rtol, atol;
     int maxiter;
     int x_is_zero;
@@ -245,6 +247,172 @@ __device__ void solve_one(const BatchArgs& a, int pid, int tid, int nthr, double
     sync();
 }
 
+// out[row] = (A v)[row] for the rows [r0, r1) of one subproblem by a CTA (LPR lanes per row).
+template <int LPR>
+__device__ void batch_spmv(const BatchArgs& a, int r0, int r1, const float* __restrict__ v, float* __restrict__ out)
+{
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const int gid = tid / LPR, sub = tid % LPR;
+    const int rows_per_pass = nthr / LPR;
+    constexpr int U = LPR == 1 ? 9 : (LPR == 2 ? 5 : (LPR == 4 ? 3 : 2));
+    for (int base = r0; base < r1; base += rows_per_pass) {
+        const int row = base + gid;
+        const bool valid = row < r1;
+        int kb = valid ? a.offsets[row] + sub : 0;
+        const int k1 = valid ? a.offsets[row + 1] : 0;
+        float s = 0.f;
+        while (kb < k1) {
+            int cc[U];
+            float vv[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int k = kb + u * LPR;
+                const bool in = k < k1;
+                cc[u] = in ? a.columns[k] : -1;
+                vv[u] = in ? a.values[k] : 0.f;
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) s += vv[u] * (cc[u] >= 0 ? v[cc[u]] : 0.f);
+            kb += U * LPR;
+        }
+        s = group_sum<LPR>(s);
+        if (valid && sub == 0) out[row] = s;
+    }
+}
+
+// BiCGSTAB of subproblem pid by the whole CTA, the same iteration as the fused single-system solver
+// (right preconditioning by default: y = M p, z = M r, omega = (r.t)/(t.t); left: omega from M t),
+// with M = D^-1 or the identity; stops on the subproblem's own tolerance.
+template <int LPR>
+__device__ void solve_one_bicgstab(const BatchArgs& a, int pid, double* red)
+{
+    const int r0 = a.batch_offsets[pid], r1 = a.batch_offsets[pid + 1];
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    auto M = [&](int i, float u) { return a.dinv ? a.dinv[i] * u : u; };
+    // ---- init: r = b - A x (or b), r0 = p = r, y = M p ----------------------------------------
+    if (a.x_is_zero) {
+        for (int i = r0 + tid; i < r1; i += nthr) a.x[i] = 0.f;
+    } else {
+        batch_spmv<LPR>(a, r0, r1, a.x, a.t);
+        __syncthreads();
+    }
+    float part2[2] = {0.f, 0.f};
+    for (int i = r0 + tid; i < r1; i += nthr) {
+        const float bi = a.b[i];
+        const float ri = a.x_is_zero ? bi : bi - a.t[i];
+        a.r[i] = ri;
+        a.r0[i] = ri;
+        a.p[i] = ri;
+        a.y[i] = M(i, ri);
+        part2[0] += bi * bi;
+        part2[1] += ri * ri;
+    }
+    double tot2[2];
+    cta_allreduce<2>(part2, tot2, red);
+    const double an = fmax((double)a.rtol * sqrt(tot2[0]), (double)a.atol);
+    const double atol_sq = an * an;
+    double rr = tot2[1], rho = tot2[1];
+    int it = 0;
+    bool broke = false;
+    while (it < a.maxiter && rr > atol_sq) {
+        // ---- v = A y, alpha = rho / (r0.v) ------------------------------------------------------
+        batch_spmv<LPR>(a, r0, r1, a.y, a.v);
+        __syncthreads();
+        float p1[1] = {0.f};
+        for (int i = r0 + tid; i < r1; i += nthr) p1[0] += a.r0[i] * a.v[i];
+        double r0v[1];
+        cta_allreduce<1>(p1, r0v, red);
+        const double alpha_d = rho / r0v[0];
+        if (!isfinite(alpha_d)) {
+            broke = true;
+            break;
+        }
+        const float alpha = (float)alpha_d;
+        // ---- x += alpha y, r -= alpha v, z = M r ----------------------------------------------
+        for (int i = r0 + tid; i < r1; i += nthr) {
+            a.x[i] += alpha * a.y[i];
+            const float ri = a.r[i] - alpha * a.v[i];
+            a.r[i] = ri;
+            a.z[i] = M(i, ri);
+        }
+        __syncthreads();
+        // ---- t = A z, omega = st / tt -------------------------------------------------------------
+        batch_spmv<LPR>(a, r0, r1, a.z, a.t);
+        __syncthreads();
+        float p2[2] = {0.f, 0.f};
+        for (int i = r0 + tid; i < r1; i += nthr) {
+            const float ti = a.t[i];
+            if (a.left_precond) {
+                const float mt = M(i, ti);
+                p2[0] += a.z[i] * mt;
+                p2[1] += mt * mt;
+            } else {
+                p2[0] += a.r[i] * ti;
+                p2[1] += ti * ti;
+            }
+        }
+        double stt[2];
+        cta_allreduce<2>(p2, stt, red);
+        const double omega_d = stt[0] / stt[1];
+        if (!isfinite(omega_d)) {
+            broke = true;
+            break;
+        }
+        const float omega = (float)omega_d;
+        // ---- x += omega z, r -= omega t, rr, rho = r0.r -------------------------------------------
+        float p3[2] = {0.f, 0.f};
+        for (int i = r0 + tid; i < r1; i += nthr) {
+            a.x[i] += omega * a.z[i];
+            const float ri = a.r[i] - omega * a.t[i];
+            a.r[i] = ri;
+            p3[0] += ri * ri;
+            p3[1] += a.r0[i] * ri;
+        }
+        double t3[2];
+        cta_allreduce<2>(p3, t3, red);
+        rr = t3[0];
+        ++it;
+        if (!(rr > atol_sq)) break;
+        const double beta_d = t3[1] * stt[1] / (r0v[0] * stt[0]);
+        const double bo_d = t3[1] / r0v[0];
+        if (!isfinite(beta_d) || !isfinite(bo_d)) {
+            broke = true;
+            break;
+        }
+        rho = t3[1];
+        const float beta = (float)beta_d, bo = (float)bo_d;
+        // ---- p = r + beta p - beta_omega v, y = M p ---------------------------------------------
+        for (int i = r0 + tid; i < r1; i += nthr) {
+            const float pi = a.r[i] + beta * a.p[i] - bo * a.v[i];
+            a.p[i] = pi;
+            a.y[i] = M(i, pi);
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        a.iters[pid] = it;
+        a.rr_out[pid] = (float)rr;
+        a.atol_sq_out[pid] = (float)atol_sq;
+        if (broke) atomicOr(a.status, GB_DEV_BREAKDOWN);
+    }
+    __syncthreads();
+}
+
+template <int LPR>
+__global__ void __launch_bounds__(512) k_batched_bicgstab(const BatchArgs a)
+{
+    __shared__ double red[32 * 3];
+    __shared__ int s_item;
+    for (;;) {
+        if (threadIdx.x == 0) s_item = atomicAdd(a.queue, 1);
+        __syncthreads();
+        const int item = s_item;
+        __syncthreads();
+        if (item >= a.nbatch) return;
+        solve_one_bicgstab<LPR>(a, a.order[item], red);
+    }
+}
+
 template <int LPR>
 __global__ void __launch_bounds__(512) k_batched_pcg(const BatchArgs a)
 {
@@ -433,6 +601,75 @@ GB_API int gb_batched_pcg(int nbatch, const int* batch_offsets, const int* order
     return gb_batched_pcg2(nbatch, batch_offsets, order, n, offsets, columns, values, dinv, b, x, rtol, atol, maxiter,
                            x_is_zero, threads, lanes_per_row, small_rows, 0, grid, iters, rr, atol_sq, workspace,
                            workspace_bytes, status, stream);
+}
+
+GB_API size_t gb_batched_bicgstab_workspace_bytes(int64_t n) { return 8 * sizeof(float) * (size_t)n + 256; }
+
+// Persistent batched BiCGSTAB with the Jacobi (dinv) or no preconditioner: each CTA takes subproblems
+// from the queue (order: largest first) and runs one subproblem's BiCGSTAB to its own tolerance
+// (reference: BiCGSTAB with batch_offsets, warp/_src/optim/linear.py:1377-1574, per-subproblem
+// tolerances :2063-2083).  left_precond selects left preconditioning; threads 128/256/512;
+// lanes_per_row 1/2/4/8.
+GB_API int gb_batched_bicgstab(int nbatch, const int* batch_offsets, const int* order, int64_t n, const int* offsets,
+                               const int* columns, const float* values, const float* dinv, const float* b, float* x,
+                               double rtol, double atol, int maxiter, int x_is_zero, int left_precond, int threads,
+                               int lanes_per_row, int grid, int* iters, float* rr, float* atol_sq, void* workspace,
+                               size_t workspace_bytes, int* status, cudaStream_t stream)
+{
+    GB_REQUIRE(nbatch >= 0 && n >= 0, "batched_bicgstab: negative sizes");
+    GB_REQUIRE(threads == 128 || threads == 256 || threads == 512, "batched_bicgstab: threads must be 128, 256 or 512");
+    GB_REQUIRE(workspace_bytes >= gb_batched_bicgstab_workspace_bytes(n), "batched_bicgstab: workspace too small");
+    GB_REQUIRE(status != nullptr && iters != nullptr && rr != nullptr && atol_sq != nullptr,
+               "batched_bicgstab: status and per-subproblem result arrays are required");
+    if (nbatch == 0) return GB_OK;
+    unsigned char* ws = static_cast<unsigned char*>(workspace);
+    BatchArgs a{};
+    a.nbatch = nbatch;
+    a.batch_offsets = batch_offsets;
+    a.order = order;
+    a.offsets = offsets;
+    a.columns = columns;
+    a.values = values;
+    a.dinv = dinv;
+    a.b = b;
+    a.x = x;
+    a.queue = reinterpret_cast<int*>(ws);
+    a.r = reinterpret_cast<float*>(ws + 256);
+    a.p = a.r + n;
+    a.r0 = a.p + n;
+    a.v = a.r0 + n;
+    a.t = a.v + n;
+    a.y = a.t + n;
+    a.z = a.y + n;
+    a.left_precond = left_precond;
+    a.rtol = (float)rtol;
+    a.atol = (float)atol;
+    a.maxiter = maxiter;
+    a.x_is_zero = x_is_zero;
+    a.iters = iters;
+    a.rr_out = rr;
+    a.atol_sq_out = atol_sq;
+    a.status = status;
+    void (*kern)(const BatchArgs) = nullptr;
+    switch (lanes_per_row) {
+    case 1: kern = k_batched_bicgstab<1>; break;
+    case 2: kern = k_batched_bicgstab<2>; break;
+    case 4: kern = k_batched_bicgstab<4>; break;
+    case 8: kern = k_batched_bicgstab<8>; break;
+    default: gb::set_error("batched_bicgstab: lanes_per_row must be 1, 2, 4 or 8"); return GB_ERR_INVALID;
+    }
+    if (grid <= 0) {
+        int dev = 0, sms = kSmCount, per_sm = 1;
+        GB_CHECK_CUDA(cudaGetDevice(&dev));
+        GB_CHECK_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        GB_CHECK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, 0));
+        grid = sms * std::max(1, std::min(per_sm, 2048 / threads));
+    }
+    grid = std::min(grid, nbatch);
+    GB_CHECK_CUDA(cudaMemsetAsync(a.queue, 0, sizeof(int), stream));
+    kern<<<grid, threads, 0, stream>>>(a);
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
 }
 
 // Batched 2-D Q1 assembly (see k_q1_batched_2d): ncell[B] cells per side, row_off / nnz_off / cell_off

@@ -40,6 +40,7 @@
 // copies and MMAs (bounded) and frees its TMEM before returning.
 #include "gb_bulk.cuh"
 #include "gb_common.cuh"
+#include "gb_net_features.cuh"
 #include "gb_spmv.cuh"  // sm_count()
 
 namespace gb {
@@ -198,7 +199,7 @@ __device__ __forceinline__ void epi_group_barrier(int group)
     asm volatile("barrier.sync %0, 128;" ::"r"(1 + group) : "memory");
 }
 
-template <bool LAST>
+template <int NOUT>
 __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
@@ -409,23 +410,35 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
             const uint32_t zq = rem - yq * usy;
             const bool valid = i >= 1 && i <= TC_OUT && xq == xk && yq - 1u < (uint32_t)c.ny && zq - 1u < (uint32_t)c.nz;
             const int64_t vox = ((int64_t)(xq - 1) * c.ny + (yq - 1)) * (int64_t)c.nz + (zq - 1);
-            if (LAST) {
-                const float zm = tc_ld1(taddr);
-                const float z0 = tc_ld1(taddr + 16);
-                const float zp = tc_ld1(taddr + 32);
+            if constexpr (NOUT > 0) {
+                // last layer: output channels 0..NOUT-1 of the node's NOUT interleaved dofs
+                float zm[NOUT], z0[NOUT], zp[NOUT];
+#pragma unroll
+                for (int q = 0; q < NOUT; ++q) {
+                    zm[q] = tc_ld1(taddr + q);
+                    z0[q] = tc_ld1(taddr + 16 + q);
+                    zp[q] = tc_ld1(taddr + 32 + q);
+                }
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                if (lane == 31) xb[(quarter * 2 + 0) * 16] = zm;
-                if (lane == 0) xb[(quarter * 2 + 1) * 16] = zp;
+#pragma unroll
+                for (int q = 0; q < NOUT; ++q) {
+                    if (lane == 31) xb[(quarter * 2 + 0) * 16 + q] = zm[q];
+                    if (lane == 0) xb[(quarter * 2 + 1) * 16 + q] = zp[q];
+                }
                 epi_group_barrier(group);
-                float lo = __shfl_up_sync(0xffffffffu, zm, 1);
-                float hi = __shfl_down_sync(0xffffffffu, zp, 1);
-                if (lane == 0 && quarter > 0) lo = xb[((quarter - 1) * 2 + 0) * 16];
-                if (lane == 31 && quarter < 3) hi = xb[((quarter + 1) * 2 + 1) * 16];
-                if (valid) {
-                    float o = lo + z0 + hi;
-                    if (c.mask && c.mask[vox] != 0.f) o = 0.f;
-                    if (c.dinv) o += c.omega * c.dinv[vox] * c.r[vox];
-                    c.w[vox] = o;
+#pragma unroll
+                for (int q = 0; q < NOUT; ++q) {
+                    float lo = __shfl_up_sync(0xffffffffu, zm[q], 1);
+                    float hi = __shfl_down_sync(0xffffffffu, zp[q], 1);
+                    if (lane == 0 && quarter > 0) lo = xb[((quarter - 1) * 2 + 0) * 16 + q];
+                    if (lane == 31 && quarter < 3) hi = xb[((quarter + 1) * 2 + 1) * 16 + q];
+                    if (valid) {
+                        const int64_t d = vox * NOUT + q;
+                        float o = lo + z0[q] + hi;
+                        if (c.mask && c.mask[vox] != 0.f) o = 0.f;
+                        if (c.dinv) o += c.omega * c.dinv[d] * c.r[d];
+                        c.w[d] = o;
+                    }
                 }
             } else {
                 float zm[16], z0[16], zp[16];
@@ -508,8 +521,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_TMEM_COLS) : "memory");
 }
 
-// features in the planar padded bf16 layout (interior rows only)
-__global__ void k_features_planar(int nx, int ny, int nz, int64_t plane_rows, const float* __restrict__ r,
+// features in the planar padded bf16 layout (interior rows only); ncomp = 1 or 3 (see node_features in
+// gb_convnet.cu: the same channels)
+__global__ void k_features_planar(int ncomp, int nx, int ny, int nz, int64_t plane_rows, const float* __restrict__ r,
                                   const float* __restrict__ dinv, const float* __restrict__ chat,
                                   const float* __restrict__ mask, unsigned char* __restrict__ out)
 {
@@ -521,13 +535,8 @@ __global__ void k_features_planar(int nx, int ny, int nz, int64_t plane_rows, co
         const int y = (int)((v / nz) % ny);
         const int z = (int)(v % nz);
         const int64_t p = (x + 1) * sx + (y + 1) * sy + (z + 1);
-        const float xm = (mask && mask[v] != 0.f) ? 0.f : dinv[v] * r[v];
         float f[16];
-        f[0] = xm;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) f[1 + k] = xm * chat[v * 8 + k];
-#pragma unroll
-        for (int k = 9; k < 16; ++k) f[k] = 0.f;
+        net_node_features(ncomp, v, r, dinv, chat, mask, f);
         uint32_t pk[8];
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
@@ -551,20 +560,22 @@ using namespace gb;
 
 GB_API int64_t gb_conv3_planar_rows(int nx, int ny, int nz) { return planar_rows(nx, ny, nz); }
 
-GB_API int gb_net_features_planar(int nx, int ny, int nz, const float* r, const float* dinv, const float* chat,
-                                  const float* mask, void* out, cudaStream_t stream)
+GB_API int gb_net_features_planar(int ncomp, int nx, int ny, int nz, const float* r, const float* dinv,
+                                  const float* chat, const float* mask, void* out, cudaStream_t stream)
 {
     const int64_t n = (int64_t)nx * ny * nz;
+    GB_REQUIRE(ncomp == 1 || ncomp == 3, "net_features_planar: ncomp must be 1 or 3");
     if (n <= 0) return GB_OK;
     GB_REQUIRE((uintptr_t)out % 16 == 0, "net_features_planar: output must be 16-byte aligned");
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(n, 256), kSmCount * 16));
-    GB_CHECK_CUDA(launch_pdl(k_features_planar, grid, 256, 0, stream, nx, ny, nz, planar_rows(nx, ny, nz), r, dinv,
-                             chat, mask, static_cast<unsigned char*>(out)));
+    GB_CHECK_CUDA(launch_pdl(k_features_planar, grid, 256, 0, stream, ncomp, nx, ny, nz, planar_rows(nx, ny, nz), r,
+                             dinv, chat, mask, static_cast<unsigned char*>(out)));
     return GB_OK;
 }
 
 // One 16 -> 16 layer (last = 0: ReLU, planar bf16 output) or the last layer (last = 1: output channel 0
-// only, w = omega dinv r + (mask ? 0 : out) in fp32).  in/out: planar padded bf16 buffers of
+// only, w = omega dinv r + (mask ? 0 : out) in fp32; last = 3: channels 0..2 into the 3 interleaved dofs
+// of each node, w[3v + c] = omega dinv[3v + c] r[3v + c] + (mask[v] ? 0 : out[v][c])).  in/out: planar padded bf16 buffers of
 // 2 * gb_conv3_planar_rows() rows of 16 bytes whose border rows are zero; Wt: [27][16][16] bf16.
 GB_API int gb_conv3_fwd_tc(int nx, int ny, int nz, int last, const void* in, const void* Wt, void* out, float* w,
                            const float* r, const float* dinv, const float* mask, float omega, int* status,
@@ -572,6 +583,7 @@ GB_API int gb_conv3_fwd_tc(int nx, int ny, int nz, int last, const void* in, con
 {
     GB_REQUIRE(nx >= 1 && ny >= 1 && nz >= 1, "conv3_fwd_tc: empty grid");
     GB_REQUIRE((uintptr_t)in % 16 == 0 && (uintptr_t)Wt % 16 == 0, "conv3_fwd_tc: in/Wt must be 16-byte aligned");
+    GB_REQUIRE(last == 0 || last == 1 || last == 3, "conv3_fwd_tc: last must be 0, 1 or 3");
     GB_REQUIRE(last ? (w != nullptr && (dinv == nullptr || r != nullptr)) : (out != nullptr && (uintptr_t)out % 16 == 0),
                "conv3_fwd_tc: missing output");
     GB_REQUIRE(status != nullptr, "conv3_fwd_tc: status word required");
@@ -612,20 +624,21 @@ GB_API int gb_conv3_fwd_tc(int nx, int ny, int nz, int last, const void* in, con
     c.mask = mask;
     c.omega = omega;
     c.status = status;
-    // one-time per process: the largest dynamic shared memory either variant may use
+    // one-time per process: the largest dynamic shared memory any variant may use
     static bool attr_set = false;
     if (!attr_set) {
-        GB_CHECK_CUDA(cudaFuncSetAttribute(k_conv3_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)TC_SMEM_LIMIT));
-        GB_CHECK_CUDA(cudaFuncSetAttribute(k_conv3_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)TC_SMEM_LIMIT));
+        GB_CHECK_CUDA(cudaFuncSetAttribute(k_conv3_tc<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_LIMIT));
+        GB_CHECK_CUDA(cudaFuncSetAttribute(k_conv3_tc<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_LIMIT));
+        GB_CHECK_CUDA(cudaFuncSetAttribute(k_conv3_tc<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_LIMIT));
         attr_set = true;
     }
     // one CTA per SM: it holds all 512 TMEM columns
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(c.nitems, (int64_t)sm_count()));
-    if (last)
-        GB_CHECK_CUDA(launch_pdl(k_conv3_tc<true>, grid, TC_THREADS, smem, stream, c));
+    if (last == 3)
+        GB_CHECK_CUDA(launch_pdl(k_conv3_tc<3>, grid, TC_THREADS, smem, stream, c));
+    else if (last)
+        GB_CHECK_CUDA(launch_pdl(k_conv3_tc<1>, grid, TC_THREADS, smem, stream, c));
     else
-        GB_CHECK_CUDA(launch_pdl(k_conv3_tc<false>, grid, TC_THREADS, smem, stream, c));
+        GB_CHECK_CUDA(launch_pdl(k_conv3_tc<0>, grid, TC_THREADS, smem, stream, c));
     return GB_OK;
 }

@@ -12,6 +12,7 @@
 // reduced in a fixed order: deterministic), ReLU backward and Adam.  Inference runs on the tcgen05
 // tensor cores (gb_conv_tc.cu).
 #include "gb_common.cuh"
+#include "gb_net_features.cuh"
 
 namespace gb {
 
@@ -194,18 +195,14 @@ __global__ void k_adam(int n, float* __restrict__ w, const float* __restrict__ g
 // Input features: ch0 = x = dinv * r; ch1..8 = x * chat[v][k] (normalised log-coefficient of the
 // k-th adjacent cell, 0 outside the grid); ch9..15 = 0; masked (Dirichlet) nodes are all zero.
 // fp32 (training) or bf16 (inference) output.
+// fp32 (training) or bf16 (inference) output, channels-last [n][16].
 template <typename OT>
-__global__ void k_features(int64_t n, const float* __restrict__ r, const float* __restrict__ dinv,
+__global__ void k_features(int ncomp, int64_t n, const float* __restrict__ r, const float* __restrict__ dinv,
                            const float* __restrict__ chat, const float* __restrict__ mask, OT* __restrict__ out)
 {
     for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-        const float xm = (mask && mask[v] != 0.f) ? 0.f : dinv[v] * r[v];
         float f[CN];
-        f[0] = xm;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) f[1 + k] = xm * chat[v * 8 + k];
-#pragma unroll
-        for (int k = 9; k < CN; ++k) f[k] = 0.f;
+        net_node_features(ncomp, v, r, dinv, chat, mask, f);
         if constexpr (sizeof(OT) == 2) {
             __nv_bfloat162* o = reinterpret_cast<__nv_bfloat162*>(out + v * CN);
 #pragma unroll
@@ -236,19 +233,21 @@ __global__ void k_cell_features(Grid3 g, const float* __restrict__ cell_coef, fl
     }
 }
 
-// out[v] = omega * dinv[v] * r[v] + (mask[v] ? 0 : act[v][0]): the Jacobi step plus the network's
-// single output channel (dinv may be null: network only).
+// out[i] = omega * dinv[i] * r[i] + (mask[node] ? 0 : act[node][c]) for dof i = node * ncomp + c: the Jacobi
+// step plus the network's output channel c (dinv may be null: network only).
 template <typename T>
-__global__ void k_net_combine(int64_t n, int stride, const T* __restrict__ act, const float* __restrict__ mask,
-                              float omega, const float* __restrict__ dinv, const float* __restrict__ r,
-                              float* __restrict__ out)
+__global__ void k_net_combine(int ncomp, int64_t n, int stride, const T* __restrict__ act,
+                              const float* __restrict__ mask, float omega, const float* __restrict__ dinv,
+                              const float* __restrict__ r, float* __restrict__ out)
 {
-    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t v = i / ncomp;
+        const int c = (int)(i - v * ncomp);
         float a;
-        if constexpr (sizeof(T) == 2) a = __bfloat162float(act[v * stride]); else a = act[v * stride];
+        if constexpr (sizeof(T) == 2) a = __bfloat162float(act[v * stride + c]); else a = act[v * stride + c];
         if (mask && mask[v] != 0.f) a = 0.f;
-        if (dinv) a += omega * dinv[v] * r[v];
-        out[v] = a;
+        if (dinv) a += omega * dinv[i] * r[i];
+        out[i] = a;
     }
 }
 
@@ -325,15 +324,17 @@ GB_API int gb_adam_step(int n, float* w, const float* g, float* m, float* v, flo
     return GB_OK;
 }
 
-// features: dtype GB_F32 -> fp32 [n][16], GB_BF16 -> bf16 [n][16]
-GB_API int gb_net_features(int dtype, int64_t n, const float* r, const float* dinv, const float* chat,
+// features: dtype GB_F32 -> fp32 [n][16], GB_BF16 -> bf16 [n][16]; n nodes of ncomp components
+GB_API int gb_net_features(int dtype, int ncomp, int64_t n, const float* r, const float* dinv, const float* chat,
                            const float* mask, void* out, cudaStream_t stream)
 {
+    GB_REQUIRE(ncomp == 1 || ncomp == 3, "net_features: ncomp must be 1 or 3");
     if (n <= 0) return GB_OK;
     if (dtype == GB_F32)
-        k_features<float><<<g1(n), 256, 0, stream>>>(n, r, dinv, chat, mask, static_cast<float*>(out));
+        k_features<float><<<g1(n), 256, 0, stream>>>(ncomp, n, r, dinv, chat, mask, static_cast<float*>(out));
     else if (dtype == GB_BF16)
-        k_features<__nv_bfloat16><<<g1(n), 256, 0, stream>>>(n, r, dinv, chat, mask, static_cast<__nv_bfloat16*>(out));
+        k_features<__nv_bfloat16><<<g1(n), 256, 0, stream>>>(ncomp, n, r, dinv, chat, mask,
+                                                             static_cast<__nv_bfloat16*>(out));
     else {
         gb::set_error("net_features: dtype must be f32 or bf16");
         return GB_ERR_UNSUPPORTED;
@@ -352,16 +353,19 @@ GB_API int gb_net_cell_features(int nx, int ny, int nz, const float* cell_coef, 
     return GB_OK;
 }
 
-GB_API int gb_net_combine(int dtype, int64_t n, int stride, const void* act, const float* mask, float omega,
+GB_API int gb_net_combine(int dtype, int ncomp, int64_t n, int stride, const void* act, const float* mask, float omega,
                           const float* dinv, const float* r, float* out, cudaStream_t stream)
 {
+    GB_REQUIRE(ncomp >= 1 && ncomp <= stride, "net_combine: 1 <= ncomp <= stride");
     if (n <= 0) return GB_OK;
+    const int64_t nd = n * ncomp;
     if (dtype == GB_F32)
-        k_net_combine<float><<<g1(n), 256, 0, stream>>>(n, stride, static_cast<const float*>(act), mask, omega, dinv, r,
-                                                        out);
+        k_net_combine<float><<<g1(nd), 256, 0, stream>>>(ncomp, nd, stride, static_cast<const float*>(act), mask, omega,
+                                                         dinv, r, out);
     else
-        k_net_combine<__nv_bfloat16><<<g1(n), 256, 0, stream>>>(n, stride, static_cast<const __nv_bfloat16*>(act), mask,
-                                                                omega, dinv, r, out);
+        k_net_combine<__nv_bfloat16><<<g1(nd), 256, 0, stream>>>(ncomp, nd, stride,
+                                                                 static_cast<const __nv_bfloat16*>(act), mask, omega,
+                                                                 dinv, r, out);
     GB_CHECK_CUDA(cudaGetLastError());
     return GB_OK;
 }

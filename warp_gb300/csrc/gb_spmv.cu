@@ -327,37 +327,44 @@ int gb_bsr_mv_internal(int bdim, int nrow, const int* offsets, const int* column
 
 // One damped Jacobi step fused with its residual product: z_out = z + omega * D^-1 (r - A z)
 // (no reference counterpart; the multigrid smoother of the flexible-CG preconditioner).
-// z_out must not alias z.  fp32 values/vectors, 1x1 or 3x3 blocks.
-GB_API int gb_bsr_jacobi_smooth(int bdim, int nrow, int64_t nnz, int64_t ncap, const int* offsets, const int* columns,
-                                const float* values, const float* r, const float* z, const float* dinv, float omega,
-                                float* z_out, int* status, cudaStream_t stream)
+// z_out must not alias z.  fp32 vectors; fp32 or bf16 values (val_dtype); 1x1 or 3x3 blocks.
+template <int BR, typename VT>
+static int launch_smooth(int nrow, int64_t nnz, int64_t ncap, const int* offsets, const int* columns, const VT* values,
+                         const float* r, const float* z, const float* dinv, float omega, float* z_out, int* status,
+                         int val_dtype, cudaStream_t stream)
 {
-    GB_REQUIRE(bdim == 1 || bdim == 3, "jacobi_smooth: block dim must be 1 or 3");
-    GB_REQUIRE(nrow > 0 && offsets && columns && values && r && z && dinv && z_out && z_out != z,
-               "jacobi_smooth: bad arguments");
     const bool aligned = ((uintptr_t)columns % 16 == 0) && ((uintptr_t)values % 16 == 0);
-    SpmvShape sh = default_shape(bdim, bdim, GB_F32, nrow, nnz, ncap, aligned);
-    size_t smem = (bdim == 1) ? spmv_smem_bytes<1, 1, float>(sh.rows, sh.cap, sh.stages)
-                              : spmv_smem_bytes<3, 3, float>(sh.rows, sh.cap, sh.stages);
+    SpmvShape sh = default_shape(BR, BR, val_dtype, nrow, nnz, ncap, aligned);
+    const size_t smem = spmv_smem_bytes<BR, BR, VT>(sh.rows, sh.cap, sh.stages);
     finalize_shape(sh, nrow, smem, offsets);
-    static size_t attr_bytes[2] = {48 * 1024, 48 * 1024};  // raised only when a launch needs more
-    if (bdim == 1) {
-        if (smem > attr_bytes[0]) {
-            GB_CHECK_CUDA(cudaFuncSetAttribute(k_bsr_smooth<1, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            attr_bytes[0] = smem;
-        }
-        GB_CHECK_CUDA(launch_pdl(k_bsr_smooth<1, float>, sh.grid, SPMV_THREADS, smem, stream, nrow, sh, offsets,
-                                 columns, values, z, r, dinv, omega, z_out, status));
-    } else {
-        if (smem > attr_bytes[1]) {
-            GB_CHECK_CUDA(cudaFuncSetAttribute(k_bsr_smooth<3, float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            attr_bytes[1] = smem;
-        }
-        GB_CHECK_CUDA(launch_pdl(k_bsr_smooth<3, float>, sh.grid, SPMV_THREADS, smem, stream, nrow, sh, offsets,
-                                 columns, values, z, r, dinv, omega, z_out, status));
+    static size_t attr_bytes = 48 * 1024;  // raised only when a launch needs more
+    if (smem > attr_bytes) {
+        GB_CHECK_CUDA(cudaFuncSetAttribute(k_bsr_smooth<BR, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr_bytes = smem;
     }
+    GB_CHECK_CUDA(launch_pdl(k_bsr_smooth<BR, VT>, sh.grid, SPMV_THREADS, smem, stream, nrow, sh, offsets, columns,
+                             values, z, r, dinv, omega, z_out, status));
     GB_CHECK_CUDA(cudaGetLastError());
     return GB_OK;
+}
+
+GB_API int gb_bsr_jacobi_smooth(int bdim, int nrow, int64_t nnz, int64_t ncap, const int* offsets, const int* columns,
+                                const void* values, int val_dtype, const float* r, const float* z, const float* dinv,
+                                float omega, float* z_out, int* status, cudaStream_t stream)
+{
+    GB_REQUIRE(bdim == 1 || bdim == 3, "jacobi_smooth: block dim must be 1 or 3");
+    GB_REQUIRE(val_dtype == GB_F32 || val_dtype == GB_BF16, "jacobi_smooth: fp32 or bf16 values");
+    GB_REQUIRE(nrow > 0 && offsets && columns && values && r && z && dinv && z_out && z_out != z,
+               "jacobi_smooth: bad arguments");
+    if (val_dtype == GB_F32)
+        return bdim == 1 ? launch_smooth<1, float>(nrow, nnz, ncap, offsets, columns, (const float*)values, r, z, dinv,
+                                                   omega, z_out, status, val_dtype, stream)
+                         : launch_smooth<3, float>(nrow, nnz, ncap, offsets, columns, (const float*)values, r, z, dinv,
+                                                   omega, z_out, status, val_dtype, stream);
+    return bdim == 1 ? launch_smooth<1, __nv_bfloat16>(nrow, nnz, ncap, offsets, columns, (const __nv_bfloat16*)values,
+                                                       r, z, dinv, omega, z_out, status, val_dtype, stream)
+                     : launch_smooth<3, __nv_bfloat16>(nrow, nnz, ncap, offsets, columns, (const __nv_bfloat16*)values,
+                                                       r, z, dinv, omega, z_out, status, val_dtype, stream);
 }
 
 // Reports the tile shape the heuristic picks (for the autotuner and the roofline accounting).

@@ -38,8 +38,11 @@ from . import _arrays as A
 from . import _native as N
 from . import multigrid, sparse
 
-LAYERS = ((16, 16, True), (16, 16, True), (16, 16, True), (16, 1, False))  # (cin, cout, relu)
+# (cin, cout, relu) per layer: scalar fields, and vec3 fields (3 outputs per node)
+LAYERS = ((16, 16, True), (16, 16, True), (16, 16, True), (16, 1, False))
+LAYERS_VEC3 = ((16, 16, True), (16, 16, True), (16, 16, True), (16, 3, False))
 CH = 16
+ELASTICITY_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "smoother_q1_elasticity.npz")
 SIGMA_DEFAULT = 1.5
 DEFAULT_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data", "smoother_q1_diffusion.npz")
 
@@ -51,13 +54,17 @@ def _stream():
 class ConvNet:
     """Weights (fp32 masters W[t][ci][co], t = 9 (dx+1) + 3 (dy+1) + (dz+1)), Adam state, gradients."""
 
-    def __init__(self, seed: int = 0, device="cuda"):
+    def __init__(self, seed: int = 0, device="cuda", ncomp: int = 1):
+        if ncomp not in (1, 3):
+            raise ValueError("ncomp: 1 (scalar fields) or 3 (vec3 fields)")
+        self.ncomp = int(ncomp)
+        self.layers = LAYERS if ncomp == 1 else LAYERS_VEC3
         g = torch.Generator().manual_seed(seed)
         self.W, self.gW, self.m, self.v = [], [], [], []
-        for li, (ci, co, _) in enumerate(LAYERS):
+        for li, (ci, co, _) in enumerate(self.layers):
             std = math.sqrt(2.0 / (27 * ci))
             w = torch.randn(27 * ci * co, generator=g, dtype=torch.float32) * std
-            if li == len(LAYERS) - 1:
+            if li == len(self.layers) - 1:
                 w.zero_()
             self.W.append(w.to(device))
             self.gW.append(torch.zeros(27 * ci * co, device=device))
@@ -72,13 +79,13 @@ class ConvNet:
     def save(self, path: str, **meta) -> None:
         arrs = {f"W{i}": w.detach().cpu().numpy() for i, w in enumerate(self.W)}
         np.savez(path, mean_log=self.mean_log, inv_std=self.inv_std, omega=self.omega, steps=self.step_count,
-                 **arrs, **{k: np.asarray(v) for k, v in meta.items()})
+                 ncomp=self.ncomp, **arrs, **{k: np.asarray(v) for k, v in meta.items()})
 
     @classmethod
     def load(cls, path: str = DEFAULT_WEIGHTS, device="cuda") -> "ConvNet":
         d = np.load(path)
-        net = cls(device=device)
-        for i in range(len(LAYERS)):
+        net = cls(device=device, ncomp=int(d["ncomp"]) if "ncomp" in d else 1)
+        for i in range(len(net.layers)):
             net.W[i] = torch.from_numpy(np.asarray(d[f"W{i}"], np.float32)).to(device)
         net.mean_log, net.inv_std, net.omega = float(d["mean_log"]), float(d["inv_std"]), float(d["omega"])
         net.step_count = int(d["steps"])
@@ -87,7 +94,7 @@ class ConvNet:
     def bf16_weights(self, last_cout: int = 16) -> list[torch.Tensor]:
         """Inference layout Wt[t][co_pad][ci] bf16 (co padded to ``last_cout`` for the last layer)."""
         out = []
-        for (ci, co, _), w in zip(LAYERS, self.W):
+        for (ci, co, _), w in zip(self.layers, self.W):
             wt = w.reshape(27, ci, co).permute(0, 2, 1)  # [t][co][ci]
             cop = 16 if co == 16 else last_cout
             full = torch.zeros(27, cop, CH, device=w.device, dtype=torch.float32)
@@ -97,24 +104,24 @@ class ConvNet:
 
     # --- fp32 training passes ----------------------------------------------------------------
     def forward_f32(self, dims, feats: torch.Tensor, acts: list[torch.Tensor], stream) -> None:
-        """acts[i] <- layer i output (acts[-1] is the [n][1] network output)."""
+        """acts[i] <- layer i output (acts[-1] is the [n][ncomp] network output)."""
         L = N.lib()
         nx, ny, nz = dims
         x = feats
-        for (ci, co, relu), w, a in zip(LAYERS, self.W, acts):
+        for (ci, co, relu), w, a in zip(self.layers, self.W, acts):
             N.check(L.gb_conv3_fwd_f32(nx, ny, nz, ci, co, A.ptr(x), A.ptr(w), int(relu), A.ptr(a), stream), "conv fwd")
             x = a
 
     def backward_f32(self, dims, feats, acts, g_out: torch.Tensor, gbuf: list[torch.Tensor], ws: torch.Tensor,
                      stream, need_input_grad: bool = False) -> None:
-        """Accumulates dL/dW into self.gW given g_out = dL/d(network output) ([n][1]); gbuf holds
+        """Accumulates dL/dW into self.gW given g_out = dL/d(network output) ([n][ncomp]); gbuf holds
         two [n][16] fp32 scratch buffers (and a third one for the input gradient if requested)."""
         L = N.lib()
         nx, ny, nz = dims
         n = nx * ny * nz
         g = g_out
-        for li in range(len(LAYERS) - 1, -1, -1):
-            ci, co, relu = LAYERS[li]
+        for li in range(len(self.layers) - 1, -1, -1):
+            ci, co, relu = self.layers[li]
             inp = feats if li == 0 else acts[li - 1]
             N.check(L.gb_conv3_bwd_weight_f32(nx, ny, nz, ci, co, A.ptr(inp), A.ptr(g), A.ptr(self.gW[li]), A.ptr(ws),
                                               ws.numel(), stream), "conv bwd weight")
@@ -123,7 +130,7 @@ class ConvNet:
             gin = gbuf[li % 2] if li > 0 else gbuf[2]
             N.check(L.gb_conv3_bwd_data_f32(nx, ny, nz, ci, co, A.ptr(g), A.ptr(self.W[li]), A.ptr(gin), stream),
                     "conv bwd data")
-            if li > 0 and LAYERS[li - 1][2]:
+            if li > 0 and self.layers[li - 1][2]:
                 N.check(L.gb_relu_bwd(n * ci, A.ptr(acts[li - 1]), A.ptr(gin), stream), "relu bwd")
             g = gin
 
@@ -141,7 +148,7 @@ class ConvNet:
 
     def bwd_weight_workspace(self, dims) -> torch.Tensor:
         L = N.lib()
-        nb = max(L.gb_conv3_bwd_weight_workspace_bytes(*dims, ci, co) for ci, co, _ in LAYERS)
+        nb = max(L.gb_conv3_bwd_weight_workspace_bytes(*dims, ci, co) for ci, co, _ in self.layers)
         return A.workspace(nb)
 
 
@@ -188,18 +195,21 @@ class LearnedSmoother:
     with the Jacobi step: 5 launches)."""
 
     def __init__(self, net: ConvNet, mg: multigrid.MultigridPreconditioner, coef, backend: str = "tc"):
-        if getattr(mg, "bdim", 1) != 1:
-            raise ValueError("learned smoother: scalar (1x1) hierarchies only")
+        bdim = getattr(mg, "bdim", 1)
+        if bdim != net.ncomp:
+            raise ValueError(f"learned smoother: a network for {net.ncomp}-component fields on a {bdim}x{bdim} "
+                             "hierarchy")
         lv = mg.levels[0]
         if len(lv.dims) != 3:
             raise ValueError("learned smoother: 3-D grids only")
         if backend != "tc":
             raise ValueError(f"unknown backend {backend!r} (the tcgen05 layers are the only inference path)")
         self.backend = backend
+        self.ncomp = bdim
         self.mg = mg
         self.dims = lv.dims
         self.n = lv.n
-        self.omega = mg.omega
+        self.omega = float(lv.omega)
         self.mask, self.dinv = lv.mask, lv.dinv
         self.status = mg.status
         coef_t = coef if isinstance(coef, torch.Tensor) else A.from_numpy(np.asarray(coef, np.float32).reshape(-1))
@@ -211,12 +221,13 @@ class LearnedSmoother:
 
     def launch(self, stream, r: int, w: int) -> None:
         L = N.lib()
-        N.check(L.gb_net_features_planar(*self.dims, r, A.ptr(self.dinv), A.ptr(self.chat), A.ptr(self.mask),
-                                         A.ptr(self.buf[0]), stream), "features")
+        N.check(L.gb_net_features_planar(self.ncomp, *self.dims, r, A.ptr(self.dinv), A.ptr(self.chat),
+                                         A.ptr(self.mask), A.ptr(self.buf[0]), stream), "features")
         src, dst = self.buf[0], self.buf[1]
         for li, wt in enumerate(self.Wt):
             last = li == len(self.Wt) - 1
-            N.check(L.gb_conv3_fwd_tc(*self.dims, int(last), A.ptr(src), A.ptr(wt), None if last else A.ptr(dst),
+            mode = (1 if self.ncomp == 1 else 3) if last else 0
+            N.check(L.gb_conv3_fwd_tc(*self.dims, mode, A.ptr(src), A.ptr(wt), None if last else A.ptr(dst),
                                       w if last else None, r if last else None, A.ptr(self.dinv) if last else None,
                                       A.ptr(self.mask) if last else None, self.omega, A.ptr(self.status), stream),
                     "conv tc")
@@ -231,20 +242,21 @@ class TrainingSmoother:
     def __init__(self, net: ConvNet, mg: multigrid.MultigridPreconditioner, coef):
         lv = mg.levels[0]
         self.net, self.mg = net, mg
-        self.dims, self.n, self.omega = lv.dims, lv.n, mg.omega
+        self.ncomp = getattr(mg, "bdim", 1)
+        self.dims, self.n, self.omega = lv.dims, lv.n, float(lv.omega)
         self.mask, self.dinv = lv.mask, lv.dinv
         coef_t = coef if isinstance(coef, torch.Tensor) else A.from_numpy(np.asarray(coef, np.float32).reshape(-1))
         self.chat = cell_features(self.dims, coef_t.reshape(-1).float().contiguous(), net.mean_log, net.inv_std)
         self.feats = A.empty(self.n * CH, torch.float32)
-        self.acts = [A.empty(self.n * co, torch.float32) for _, co, _ in LAYERS]
+        self.acts = [A.empty(self.n * co, torch.float32) for _, co, _ in net.layers]
 
     def launch(self, stream, r: int, w: int) -> None:
         L = N.lib()
-        N.check(L.gb_net_features(N.GB_F32, self.n, r, A.ptr(self.dinv), A.ptr(self.chat), A.ptr(self.mask),
-                                  A.ptr(self.feats), stream), "features")
+        N.check(L.gb_net_features(N.GB_F32, self.ncomp, self.n, r, A.ptr(self.dinv), A.ptr(self.chat),
+                                  A.ptr(self.mask), A.ptr(self.feats), stream), "features")
         self.net.forward_f32(self.dims, self.feats, self.acts, stream)
-        N.check(L.gb_net_combine(N.GB_F32, self.n, 1, A.ptr(self.acts[-1]), A.ptr(self.mask), self.omega,
-                                 A.ptr(self.dinv), r, w, stream), "combine")
+        N.check(L.gb_net_combine(N.GB_F32, self.ncomp, self.n, self.ncomp, A.ptr(self.acts[-1]), A.ptr(self.mask),
+                                 self.omega, A.ptr(self.dinv), r, w, stream), "combine")
 
 
 class _Field:
@@ -252,17 +264,23 @@ class _Field:
 
     def __init__(self, system, net: ConvNet):
         self.sys = system
-        self.mg = multigrid.MultigridPreconditioner(system.A, system.geo, system.coef)
+        faces = ("x-",) if system.A.block_shape == (3, 3) else ("x-", "x+", "y-", "y+", "z-", "z+")
+        self.mg = multigrid.MultigridPreconditioner(system.A, system.geo, system.coef, faces=faces)
+        self.bdim = self.mg.bdim
         self.sm = TrainingSmoother(net, self.mg, system.coef)
         n = self.mg.n
         self.n = n
         self.z, self.gz, self.u, self.g, self.p = (A.zeros(n, torch.float32) for _ in range(5))
-        self.coarse_rhs = A.zeros(self.mg.levels[1].n, torch.float32) if len(self.mg.levels) > 1 else None
-        self.coarse_sol = A.zeros(self.mg.levels[1].n, torch.float32) if len(self.mg.levels) > 1 else None
+        # per-dof Dirichlet mask of the fine level (the hierarchy keeps one per node)
+        self.mask_dof = self.mg.levels[0].mask.repeat_interleave(self.bdim).contiguous()
+        nc = self.mg.levels[1].n * self.bdim if len(self.mg.levels) > 1 else 0
+        self.coarse_rhs = A.zeros(nc, torch.float32) if nc else None
+        self.coarse_sol = A.zeros(nc, torch.float32) if nc else None
 
 
 def _spmv(Am: sparse.BsrMatrix, x: torch.Tensor, y: torch.Tensor, alpha: float, beta: float, stream, status) -> None:
-    N.check(N.lib().gb_bsr_mv(1, 1, Am.nrow, Am.ncol, Am.nnz_sync(), Am.capacity, A.ptr(Am.offsets), None,
+    br, bc = Am.block_shape
+    N.check(N.lib().gb_bsr_mv(br, bc, Am.nrow, Am.ncol, Am.nnz_sync(), Am.capacity, A.ptr(Am.offsets), None,
                               A.ptr(Am.columns), A.ptr(Am.values), N.GB_F32, A.ptr(x), A.ptr(y), A.ptr(y), N.GB_F32,
                               alpha, beta, 0, 0, 0, -1, A.ptr(status), stream), "spmv")
 
@@ -321,19 +339,20 @@ class SmootherTrainer:
         # g_w2 = gz - omega A D^-1 gz
         torch.mul(lv0.dinv, f.gz, out=f.u)
         f.g.copy_(f.gz)
-        _spmv(lv0.A, f.u, f.g, -mg.omega, 1.0, stream, st)
+        _spmv(lv0.A, f.u, f.g, -float(lv0.omega), 1.0, stream, st)
         # g_w = g_w2 - A P Vc R g_w2
         if len(mg.levels) > 1:
             lv1 = mg.levels[1]
-            N.check(L.gb_mg_restrict(*lv0.dims, *lv1.dims, A.ptr(f.g), A.ptr(lv0.mask), A.ptr(lv1.mask),
-                                     A.ptr(f.coarse_rhs), stream), "restrict")
+            N.check(L.gb_mg_restrict_c(f.bdim, *lv0.dims, *lv1.dims, A.ptr(f.g), A.ptr(lv0.mask), A.ptr(lv1.mask),
+                                       A.ptr(f.coarse_rhs), stream), "restrict")
             mg._vcycle(1, A.ptr(f.coarse_rhs), A.ptr(f.coarse_sol), stream)
             f.p.zero_()
-            N.check(L.gb_mg_prolong_add(*lv0.dims, *lv1.dims, A.ptr(f.coarse_sol), A.ptr(lv0.mask), 1.0, A.ptr(f.p),
-                                        stream), "prolong")
+            N.check(L.gb_mg_prolong_add_c(f.bdim, *lv0.dims, *lv1.dims, A.ptr(f.coarse_sol), A.ptr(lv0.mask), 1.0,
+                                          A.ptr(f.p), stream), "prolong")
             _spmv(lv0.A, f.p, f.g, -1.0, 1.0, stream, st)
-        # network output gradient (masked nodes do not take the network's value)
-        f.g.mul_(1.0 - lv0.mask)
+        # network output gradient (masked nodes do not take the network's value); [n][ncomp] is the
+        # interleaved dof layout
+        f.g.mul_(1.0 - f.mask_dof)
         ws, gbuf = self._scratch(f.sm.dims)
         self.net.backward_f32(f.sm.dims, f.sm.feats, f.sm.acts, f.g, gbuf, ws, stream)
         return loss
@@ -380,7 +399,7 @@ def cg_pairs(f: _Field, nrhs: int, rng: np.random.Generator, iters=(0, 1, 2, 4, 
 
     A_ = f.sys.A
     n = f.n
-    keep = 1.0 - f.mg.levels[0].mask
+    keep = 1.0 - f.mask_dof
     out = []
     M = linear.preconditioner(A_, "diag")
     for _ in range(nrhs):
@@ -414,7 +433,7 @@ def cg_pairs(f: _Field, nrhs: int, rng: np.random.Generator, iters=(0, 1, 2, 4, 
 def slow_pairs(f: _Field, nrhs: int, rng: np.random.Generator, sweeps=(1, 2, 3, 5), smoother="current"):
     """Errors left by stationary V-cycle sweeps e <- e - V(A e) from random starts (normalised)."""
     n = f.n
-    keep = 1.0 - f.mg.levels[0].mask
+    keep = 1.0 - f.mask_dof
     A_ = f.sys.A
     out = []
     saved = f.mg.smoother

@@ -54,12 +54,20 @@ class MultigridPreconditioner:
         coarsest_nodes: stop coarsening at or below this many nodes.
         stencil: apply the level operators in 27-point stencil form (else the CSR kernels; 1x1 only).
         poisson: Poisson ratio of the elasticity levels (3x3).
+        fine_values: scalar type of the fine level's matrix values inside the V-cycle (CSR levels):
+            ``torch.bfloat16`` keeps a bf16 copy for the cycle's residual and smoothing passes, about
+            half their matrix traffic; the flexible solver's own product keeps the fp32 matrix, so
+            its tolerance and the FP64 refinement are unaffected (the cycle only has to be a good
+            approximate inverse).
 
     Vectors of a 3x3 hierarchy hold 3 interleaved components per node; masks are per node.
     """
 
     def __init__(self, Am: sparse.BsrMatrix, geo, coef, faces=("x-", "x+", "y-", "y+", "z-", "z+"), omega=None,
-                 coarsest_nodes: int = 400, max_levels: int = 12, stencil: bool = True, poisson: float = 0.3):
+                 coarsest_nodes: int = 400, max_levels: int = 12, stencil: bool = True, poisson: float = 0.3,
+                 fine_values: torch.dtype = torch.float32):
+        if fine_values not in (torch.float32, torch.bfloat16):
+            raise ValueError("fine_values: torch.float32 or torch.bfloat16")
         if Am.block_shape not in ((1, 1), (3, 3)) or Am.scalar_type != torch.float32:
             raise ValueError("multigrid preconditioner: fp32 BSR matrix with 1x1 or 3x3 blocks required")
         self.bdim = Am.block_shape[0]
@@ -95,6 +103,12 @@ class MultigridPreconditioner:
                                               A.ptr(cur_A.values), 0, A.ptr(lv.dinv), stream), "dinv")
             lv.w = A.zeros(lv.n * C, torch.float32)
             lv.t = A.zeros(lv.n * C, torch.float32)
+            # the values the cycle's CSR passes read (a bf16 copy on the fine level when asked)
+            lv.vals = cur_A.values
+            lv.vals_dtype = N.GB_F32
+            if not levels and fine_values == torch.bfloat16:
+                lv.vals = cur_A.values[: lv.nnz].to(torch.bfloat16).contiguous()
+                lv.vals_dtype = N.GB_BF16
             levels.append(lv)
             res = cur_geo.res
             if lv.n <= coarsest_nodes or any(r % 2 for r in res) or len(levels) >= max_levels:
@@ -225,15 +239,15 @@ class MultigridPreconditioner:
             N.check(L.gb_st27_apply(2, *lv.dims, A.ptr(lv.S), w, r, A.ptr(lv.dinv), lv.omega, None, z,
                                     A.ptr(self.status), stream), "smooth")
         else:
-            N.check(L.gb_bsr_jacobi_smooth(self.bdim, lv.n, lv.nnz, Am.capacity, A.ptr(Am.offsets),
-                                           A.ptr(Am.columns), A.ptr(Am.values), r, w, A.ptr(lv.dinv), lv.omega, z,
+            N.check(L.gb_bsr_jacobi_smooth(self.bdim, lv.n, lv.nnz, lv.nnz, A.ptr(Am.offsets), A.ptr(Am.columns),
+                                           A.ptr(lv.vals), lv.vals_dtype, r, w, A.ptr(lv.dinv), lv.omega, z,
                                            A.ptr(self.status), stream), "smooth")
 
     def _csr_residual(self, lv, w: int, r: int, t: int, stream) -> None:
         Am = lv.A
         C = self.bdim
-        N.check(N.lib().gb_bsr_mv(C, C, lv.n, lv.n, lv.nnz, Am.capacity, A.ptr(Am.offsets), None, A.ptr(Am.columns),
-                                  A.ptr(Am.values), N.GB_F32, w, r, t, N.GB_F32, -1.0, 1.0, 0, 0, 0, -1,
+        N.check(N.lib().gb_bsr_mv(C, C, lv.n, lv.n, lv.nnz, lv.nnz, A.ptr(Am.offsets), None, A.ptr(Am.columns),
+                                  A.ptr(lv.vals), lv.vals_dtype, w, r, t, N.GB_F32, -1.0, 1.0, 0, 0, 0, -1,
                                   A.ptr(self.status), stream), "residual")
 
     @A.on_caller_stream

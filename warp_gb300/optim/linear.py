@@ -381,7 +381,8 @@ class LinearSolverState:
         return self._run_generic(Aop, b_t.reshape(-1), x_t.reshape(-1), Mop)
 
     def _run_batched(self, Aop, b, x, Mop):
-        raise NotImplementedError(f"{type(self).__name__}: batched operators (batch_offsets) are solved by cg only")
+        raise NotImplementedError(f"{type(self).__name__}: batched operators (batch_offsets) are solved by cg and "
+                                  "bicgstab")
 
     # -- generic path (any LinearOperator) ------------------------------------------------
     def _dots(self, pairs):
@@ -695,6 +696,37 @@ class BiCGSTAB(LinearSolverState):
                  use_cuda_graph=True, is_left_preconditioner=False):
         self._is_left_preconditioner = bool(is_left_preconditioner)
         super().__init__(A_, b, x, tol, atol, maxiter, M, callback, check_every, use_cuda_graph)
+
+    def _run_batched(self, Aop, b, x, Mop):
+        """Batched operator: one persistent launch, one CTA per subproblem running its BiCGSTAB to its
+        own tolerance (reference: ``linear.py:1377-1574`` with ``batch_offsets``)."""
+        from .. import batched
+
+        if b.dtype != torch.float32 or x.dtype != torch.float32:
+            raise NotImplementedError("batched BiCGSTAB: float32 systems")
+        inv = None
+        if Mop is not None:
+            inv = getattr(Mop, "_inv_diag", None)
+            if inv is None:
+                raise NotImplementedError("batched BiCGSTAB: Jacobi ('diag') or no preconditioner")
+        if getattr(self, "_batched", None) is None or self._batched_op is not Aop:
+            csr = batched.as_block_csr(Aop)
+            rtol, atol = _get_tolerances(torch.float32, self._tol, self._atol)
+            self._batched = batched.BatchedBiCGSTAB(csr, Aop.batch_offsets, inv, rtol, atol, self._maxiter,
+                                                    left_precond=self._is_left_preconditioner,
+                                                    use_cuda_graph=self._use_cuda_graph)
+            self._batched_op = Aop
+        self._batched.inv_diag = inv
+        self._batched.solve(b, x)
+        it, rr, atol_sq = self._batched.results()
+        if self._check_every == 0:
+            return it, rr, atol_sq
+        it_h = int(it.item())
+        err = math.sqrt(float(rr.max())) if rr.numel() else 0.0
+        atol_v = math.sqrt(float(atol_sq.max())) if atol_sq.numel() else 0.0
+        if self._callback is not None:
+            self._callback(it_h, err, atol_v)
+        return it_h, err, atol_v
 
     def _run_generic(self, Aop, b, x, Mop):
         dt = b.dtype

@@ -1,6 +1,8 @@
 """Train the learned smoother on the GPU with the package's own kernels.
 
     python -m warp_gb300.train_smoother --fields 2000 --res 48 --out warp_gb300/data/smoother_q1_diffusion.npz
+    python -m warp_gb300.train_smoother --problem elasticity --fields 400 --res 32 \
+        --out warp_gb300/data/smoother_q1_elasticity.npz
 
 Each seeded coefficient field (lognormal, squared-exponential GRF, sigma 1.5, correlation length 0.1
 on cells of size 1/96: a 48^3 sub-block of the 96^3 unit-cube problem) contributes (residual, error)
@@ -42,13 +44,27 @@ def make_field(res: int, seed: int, sigma: float = learned.SIGMA_DEFAULT, corr_l
     return problems.diffusion((res, res, res), seed=seed, coef=np.exp(g))
 
 
+def make_elasticity_field(res: int, seed: int, sigma: float = learned.SIGMA_DEFAULT, corr_length: float = 0.05,
+                          cell_size: float = 1.0 / 128):
+    """Q1 vec3 elasticity on res^3 cells whose lognormal Young's modulus has the statistics of the 128^3
+    unit-cube configuration (correlation length corr_length on cells of size 1/128), x = 0 clamped."""
+    return problems.elasticity((res, res, res), sigma=sigma, corr_length=corr_length / (cell_size * res), seed=seed)
+
+
 def train(fields: int = 2000, res: int = 48, steps_per_field: int = 2, batch: int = 6, lr: float = 2e-3,
           lr_min: float = 1e-4, seed0: int = 10_000, eval_every: int = 250, out: str | None = None, log=print,
-          net: learned.ConvNet | None = None, max_minutes: float | None = None) -> learned.ConvNet:
-    net = learned.ConvNet(seed=0) if net is None else net
+          net: learned.ConvNet | None = None, max_minutes: float | None = None,
+          problem: str = "diffusion") -> learned.ConvNet:
+    if problem not in ("diffusion", "elasticity"):
+        raise ValueError("problem: diffusion or elasticity")
+    field_of = make_field if problem == "diffusion" else make_elasticity_field
+    if net is None:
+        net = learned.ConvNet(seed=0, ncomp=1 if problem == "diffusion" else 3)
+        if problem == "elasticity":  # E = 1e3 exp(g), g ~ N(0, sigma^2)
+            net.mean_log, net.inv_std = math.log(1e3), 1.0 / learned.SIGMA_DEFAULT
     tr = learned.SmootherTrainer(net, lr=lr)
     rng = np.random.default_rng(seed0)
-    held = tr.field(make_field(res, seed=seed0 - 1))
+    held = tr.field(field_of(res, seed=seed0 - 1))
     held_pairs = learned.slow_pairs(held, 2, np.random.default_rng(1), smoother=None)
     base = np.mean([tr.eval_loss(held, r, e, None) for r, e in held_pairs])
     log(f"held-out field: Jacobi-smoothed V-cycle loss {base:.5f}")
@@ -57,7 +73,7 @@ def train(fields: int = 2000, res: int = 48, steps_per_field: int = 2, batch: in
     t0 = time.time()
     hist = []
     for k in range(fields):
-        f = tr.field(make_field(res, seed=seed0 + k))
+        f = tr.field(field_of(res, seed=seed0 + k))
         pairs = (learned.cg_pairs(f, 1, rng, iters=(0, 2, 8, 32))
                  + learned.slow_pairs(f, 1, rng, sweeps=(1, 2, 4))
                  + learned.slow_pairs(f, 1, rng, sweeps=(2,), smoother=None))
@@ -89,12 +105,13 @@ def main():
     ap.add_argument("--eval-every", type=int, default=250)
     ap.add_argument("--out", default=learned.DEFAULT_WEIGHTS)
     ap.add_argument("--max-minutes", type=float, default=None)
+    ap.add_argument("--problem", choices=["diffusion", "elasticity"], default="diffusion")
     a = ap.parse_args()
     import os
 
     os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)
     train(a.fields, a.res, a.steps_per_field, a.batch, a.lr, eval_every=a.eval_every, out=a.out,
-          log=lambda m: print(m, flush=True), max_minutes=a.max_minutes)
+          log=lambda m: print(m, flush=True), max_minutes=a.max_minutes, problem=a.problem)
 
 
 if __name__ == "__main__":
