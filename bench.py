@@ -556,6 +556,21 @@ def run_profile(args):
     A = system.A
     torch.cuda.synchronize()
     torch.cuda.empty_cache()  # keep the device footprint of the capture small (assembly temporaries)
+    if args.profile == "assembly":  # fem.integrate once by each construction (direct, triplets, row compress)
+        from warp_gb300 import fem
+
+        space = fem.make_polynomial_space(system.geo, degree=1)
+        coef = torch.from_numpy(np.asarray(system.coef, np.float32)).cuda()
+        fields = {"u": fem.make_trial(space), "v": fem.make_test(space)}
+        for construction in ("auto", "triplets", "row_compress"):
+            m = fem.integrate(fem.diffusion_form, fields=fields, values={"nu": coef},
+                              bsr_options={"construction": construction})
+            m.nnz_sync()
+            del m
+            torch.cuda.empty_cache()
+        torch.cuda.synchronize()
+        print("profile run done", flush=True)
+        return 0
     if args.profile == "spmv":
         x = torch.randn(A.nrow, dtype=torch.float32, device="cuda")
         y = torch.empty_like(x)
@@ -603,13 +618,15 @@ def main():
     p.add_argument("--elasticity-large-res", type=int, default=128,
                    help="cells per axis of the large elasticity extra (0 skips it)")
     p.add_argument("--weights", default=os.path.join(ROOT, "warp_gb300", "data", "smoother_q1_diffusion.npz"))
-    p.add_argument("--profile", choices=["spmv", "cg", "jacobi_solve", "solve", "conv", "batched", "vcycle"],
+    p.add_argument("--profile", choices=["spmv", "cg", "jacobi_solve", "solve", "conv", "batched", "vcycle",
+                                         "assembly"],
                    default=None,
                    help="run a fixed kernel sequence for an ncu capture and exit (prints no bench line): "
                         "spmv = 8 bsr_mv launches, cg = 30 eager (non-graph) Jacobi-CG iterations, "
                         "jacobi_solve = one refined Jacobi-CG solve, solve = two learned-FCG solves (eager launches), "
                         "conv = 3 launches of one tcgen05 conv layer on the node grid, batched = two launches of "
-                        "the batched CG on 512 uneven systems, vcycle = 3 eager multigrid V-cycles (stencil levels)")
+                        "the batched CG on 512 uneven systems, vcycle = 3 eager multigrid V-cycles (stencil levels), "
+                        "assembly = one 96^3 fem.integrate per construction (direct, triplets, row compress)")
     args = p.parse_args()
     args.warmup = max(args.warmup, 3) if args.impl == "gb300" else args.warmup
 

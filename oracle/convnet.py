@@ -107,6 +107,31 @@ def combine(out0, mask, omega, dinv, r) -> np.ndarray:
     return np.where(mask != 0, 0.0, out0) + omega * dinv * r
 
 
+def features_vec3(r, dinv, chat, mask) -> np.ndarray:
+    """Vec3 fields (3 interleaved components per node): [n, 16] with x_c = dinv_c r_c (0 at masked
+    nodes) in channels 0..2 and x_c * s_j in channel 3 + 4c + j, where s_0 is the mean of the node's 8
+    cell values chat[:, k] and s_1..3 their x / y / z contrasts (mean over the cells with bit 2 / 1 / 0 of
+    k set minus the others)."""
+    n = len(mask)
+    x = np.where((mask != 0)[:, None], 0.0, (np.asarray(dinv, np.float64) * r).reshape(n, 3))
+    k = np.arange(8)
+    sign = np.stack([np.ones(8), np.where(k >> 2, 1.0, -1.0), np.where((k >> 1) & 1, 1.0, -1.0),
+                     np.where(k & 1, 1.0, -1.0)])  # [4, 8]
+    s = np.asarray(chat, np.float64) @ sign.T / 8.0  # [n, 4]
+    f = np.zeros((n, 16))
+    f[:, 0:3] = x
+    for c in range(3):
+        f[:, 3 + 4 * c:7 + 4 * c] = x[:, c:c + 1] * s
+    return f
+
+
+def combine_vec3(out, mask, omega, dinv, r) -> np.ndarray:
+    """[3n]: omega dinv r + (mask[node] ? 0 : out[node][c])."""
+    n = len(mask)
+    return (np.where((mask != 0)[:, None], 0.0, np.asarray(out).reshape(n, 3)).reshape(-1)
+            + omega * np.asarray(dinv, np.float64) * r)
+
+
 def net_forward(dims, feats, Ws, relus):
     acts = []
     x = feats

@@ -288,3 +288,98 @@ def test_trained_network_gains_over_jacobi_smoothing(cuda):
         it, err, atol = linear.fcg(test.A, test.b, x, tol=1e-7, atol=0.0, maxiter=100, M=mg, check_every=1)
         iters[name] = it
     assert iters["learned"] < iters["jacobi"], iters
+
+
+def test_vec3_features_combine_and_last_layer_match_oracle(cuda):
+    """Vec3 (elasticity) pieces of the smoother: features (fp32 and the planar bf16 layout), the combine
+    step, and the tcgen05 last layer with three outputs fused with the per-dof Jacobi step."""
+    import warp_gb300._native as N
+    from warp_gb300 import learned
+
+    L = N.lib()
+    dims = (9, 7, 11)
+    n = int(np.prod(dims))
+    rng = np.random.default_rng(14)
+    coef = np.exp(rng.standard_normal(8 * 6 * 10)).astype(np.float32)
+    chat = torch.empty(n * 8, device="cuda")
+    N.check(L.gb_net_cell_features(*dims, _dev(coef).data_ptr(), 0.1, 0.5, chat.data_ptr(), STREAM()))
+    chat_h = chat.cpu().numpy().reshape(n, 8)
+    r = rng.standard_normal(3 * n).astype(np.float32)
+    dinv = rng.uniform(0.5, 2, 3 * n).astype(np.float32)
+    mask = (rng.uniform(size=n) < 0.2).astype(np.float32)
+    rd, dd, md = _dev(r), _dev(dinv), _dev(mask)
+    f = torch.empty(n * 16, device="cuda")
+    N.check(L.gb_net_features(N.GB_F32, 3, n, rd.data_ptr(), dd.data_ptr(), chat.data_ptr(), md.data_ptr(),
+                              f.data_ptr(), STREAM()))
+    ref_f = C.features_vec3(r, dinv, chat_h, mask)
+    np.testing.assert_allclose(f.cpu().numpy().reshape(n, 16), ref_f, rtol=1e-5, atol=1e-6)
+    planar = torch.zeros(2 * learned.planar_rows(dims) * 8, dtype=torch.bfloat16, device="cuda")
+    N.check(L.gb_net_features_planar(3, *dims, rd.data_ptr(), dd.data_ptr(), chat.data_ptr(), md.data_ptr(),
+                                     planar.data_ptr(), STREAM()))
+    got = learned.from_planar(planar.view(2, -1, 8), dims).float().cpu().numpy()
+    np.testing.assert_allclose(got, ref_f, rtol=8e-3, atol=1e-6)
+    act = rng.standard_normal((n, 3)).astype(np.float32)
+    out = torch.empty(3 * n, device="cuda")
+    N.check(L.gb_net_combine(N.GB_F32, 3, n, 3, _dev(act).data_ptr(), md.data_ptr(), 0.4, dd.data_ptr(), rd.data_ptr(),
+                             out.data_ptr(), STREAM()))
+    np.testing.assert_allclose(out.cpu().numpy(), C.combine_vec3(act, mask, 0.4, dinv, r), rtol=1e-5, atol=1e-6)
+    # last layer, three outputs
+    x = _bf16_round(rng.standard_normal((n, 16)))
+    W = np.zeros((27, 16, 16), np.float32)
+    W[:, :, :3] = _bf16_round(rng.standard_normal((27, 16, 3)) * 0.2)
+    src = learned.to_planar(_dev(x), dims)
+    Wt = _dev(W.transpose(0, 2, 1), torch.bfloat16)
+    w = torch.full((3 * n,), float("nan"), device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    N.check(L.gb_conv3_fwd_tc(*dims, 3, src.data_ptr(), Wt.data_ptr(), None, w.data_ptr(), rd.data_ptr(),
+                              dd.data_ptr(), md.data_ptr(), 0.4, status.data_ptr(), STREAM()))
+    out3 = C.conv3_fwd(dims, x, W)[:, :3]
+    ref = C.combine_vec3(out3, mask, 0.4, dinv, r)
+    np.testing.assert_allclose(w.cpu().numpy(), ref, rtol=1e-4, atol=1e-4 * np.abs(ref).max())
+    assert int(status.item()) == 0
+
+
+def test_vec3_training_gradient_matches_a_directional_difference(cuda):
+    """The vec3 trainer's dLoss/dW through the elasticity V-cycle agrees with a central difference of the
+    loss along a random weight direction, and the bf16 tcgen05 smoother equals the fp32 training forward up
+    to bf16 rounding."""
+    from warp_gb300 import learned, problems
+
+    s = problems.elasticity((12, 12, 12), sigma=1.0, corr_length=0.3, seed=3)
+    net = learned.ConvNet(seed=2, ncomp=3)
+    gen = torch.Generator().manual_seed(5)
+    net.W[3] = (torch.randn(net.W[3].numel(), generator=gen) * 0.05).cuda()
+    tr = learned.SmootherTrainer(net)
+    f = tr.field(s)
+    assert f.bdim == 3 and f.n == 3 * 13 ** 3
+    rng = np.random.default_rng(0)
+    e = torch.from_numpy(rng.standard_normal(f.n).astype(np.float32)).cuda() * (1 - f.mask_dof)
+    r = torch.zeros_like(e)
+    learned._spmv(s.A, e, r, 1.0, 0.0, STREAM(), f.mg.status)
+    net.zero_grad()
+    tr.loss_and_grad(f, r, e)
+    torch.cuda.synchronize()
+    dirs = [torch.randn(w.numel(), generator=gen).cuda() for w in net.W]
+    analytic = sum(float((g * d).sum()) for g, d in zip(net.gW, dirs))
+    eps = 5e-4
+    W0 = [w.clone() for w in net.W]
+
+    def loss_at(t):
+        for w, w0, d in zip(net.W, W0, dirs):
+            w.copy_(w0 + t * d)
+        return tr.eval_loss(f, r, e, f.sm)
+
+    fd = (loss_at(eps) - loss_at(-eps)) / (2 * eps)
+    for w, w0 in zip(net.W, W0):
+        w.copy_(w0)
+    assert abs(fd - analytic) <= 0.05 * abs(analytic) + 1e-6, (fd, analytic)
+    # inference smoother (bf16 tcgen05 layers, 3 outputs) against the fp32 training forward
+    rr = torch.randn(f.n, device="cuda") * (1 - f.mask_dof)
+    w32 = torch.empty_like(rr)
+    f.sm.launch(STREAM(), rr.data_ptr(), w32.data_ptr())
+    inf = learned.LearnedSmoother(net, f.mg, s.coef)
+    w16 = torch.empty_like(rr)
+    inf.launch(STREAM(), rr.data_ptr(), w16.data_ptr())
+    err = float((w16 - w32).norm() / w32.norm())
+    assert err < 2e-2, err
+    assert int(f.mg.status.item()) == 0

@@ -328,14 +328,22 @@ __device__ void solve_one_bicgstab(const BatchArgs& a, int pid, double* red)
             break;
         }
         const float alpha = (float)alpha_d;
-        // ---- x += alpha y, r -= alpha v, z = M r ----------------------------------------------
+        // ---- x += alpha y, r -= alpha v, z = M r, r.r (a converged half step ends the solve) -------
+        float ph[1] = {0.f};
         for (int i = r0 + tid; i < r1; i += nthr) {
             a.x[i] += alpha * a.y[i];
             const float ri = a.r[i] - alpha * a.v[i];
             a.r[i] = ri;
             a.z[i] = M(i, ri);
+            ph[0] += ri * ri;
         }
-        __syncthreads();
+        double rh[1];
+        cta_allreduce<1>(ph, rh, red);  // includes the barriers: z is complete for the product below
+        if (!(rh[0] > atol_sq)) {
+            rr = rh[0];
+            ++it;
+            break;
+        }
         // ---- t = A z, omega = st / tt -------------------------------------------------------------
         batch_spmv<LPR>(a, r0, r1, a.z, a.t);
         __syncthreads();
