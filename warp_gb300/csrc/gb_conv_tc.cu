@@ -26,8 +26,7 @@
 // run are written (N = 48 or 96).  The epilogue then forms
 //     out[p] = Z[p-1][dz=-1] + Z[p][0] + Z[p+1][+1]
 // for the 126 rows whose neighbours lie in the same 128-row window (lane shuffles, plus one value
-// exchanged between neighbouring epilogue warps).  The first dy's MMA into a fresh plane's chunk
-// overwrites it (no accumulate), so a chunk is free again as soon as the epilogue has loaded it.
+// exchanged between neighbouring epilogue warps), and zeroes the chunk for its next plane.
 //
 // A work item is one output x-plane of a column of TC_SUB = 2 windows (252 output rows); a CTA walks
 // x through a contiguous range of items, so each input x-plane block (both planes, rows
@@ -37,7 +36,7 @@
 // the groups take alternate output planes) that read a finished chunk with tcgen05.ld, sum the dz
 // taps, apply ReLU and store bf16 rows of interior voxels -- or, for the last layer, write
 // w[v] = omega dinv[v] r[v] + (mask[v] ? 0 : out[v][0]) in fp32 (the Jacobi step fused; for vec3
-// fields the node's three dofs from output channels 0..2).
+// fields the node's three dofs from output channels 0..2) -- then zero the chunk with tcgen05.st.
 // Every wait is bounded (globaltimer); a timeout sets GB_DEV_WAIT_TIMEOUT, the CTA drains its own
 // copies and MMAs (bounded) and frees its TMEM before returning.
 #include "gb_bulk.cuh"
@@ -164,6 +163,17 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16])
     for (int k = 0; k < 16; ++k) v[k] = __uint_as_float(r[k]);
 }
 
+// zero 16 consecutive accumulator columns of this warp's lane quarter
+__device__ __forceinline__ void tc_st16_zero(uint32_t taddr)
+{
+    const uint32_t z = 0u;
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, %1, "
+        "%1, %1};" ::"r"(taddr),
+        "r"(z)
+        : "memory");
+}
+
 __device__ __forceinline__ float tc_ld1(uint32_t taddr)
 {
     uint32_t r;
@@ -201,7 +211,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
     uint64_t* full = reinterpret_cast<uint64_t*>(wsm + TC_W_BYTES + TC_XCHG_BYTES);
     uint64_t* empty = full + TC_MAX_SLOTS;
     uint64_t* accfull = empty + TC_MAX_SLOTS;  // [TC_RING]: an output plane's chunks are complete
-    uint64_t* accempty = accfull + TC_RING;    // [TC_RING]: a chunk's values were loaded by the epilogue
+    uint64_t* accempty = accfull + TC_RING;    // [TC_RING]: a chunk was drained and zeroed
     uint64_t* done = accempty + TC_RING;       // every issuer's last commit: all MMAs of the CTA completed
     uint32_t* s_tmem = reinterpret_cast<uint32_t*>(done + 1);
     volatile int* s_abort = reinterpret_cast<volatile int*>(s_tmem + 1);
@@ -310,7 +320,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
                 for (int xi = x0 - 1; xi <= x1 + 1; ++xi) {
                     const int q = q0 + (xi - x0 + 1);
                     // output planes this input feeds inside the run, and whether the last of them is
-                    // touched for the first time (its chunk must have been drained)
+                    // touched for the first time (its chunk must have been drained and zeroed)
                     const int lo = max(x0, xi - 1), hi = min(x1, xi + 1);
                     const bool fresh = (hi == xi + 1) || (xi == x0 - 1);
                     ok = tc_wait(&full[q % NS], (q / NS) & 1, s_abort);
@@ -323,27 +333,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
                         break;
                     }
                     tc_fence_after();
-                    const int np = hi - lo + 1;                   // planes fed (1..3)
+                    const int np = hi - lo + 1;                 // planes fed (1..3)
                     const int clo = (it0 + (lo - x0)) % TC_RING;  // chunk of plane lo
+                    const int n1 = min(np, TC_RING - clo);      // planes before the ring wraps
+                    const uint32_t boff = (uint32_t)((lo - (xi - 1)) * TC_CHUNK * 16);  // B rows of plane lo
                     const uint32_t arow0 = rbase + (uint32_t)(q % NS) * c.block_bytes + (uint32_t)(j * TC_OUT) * 16u;
 #pragma unroll
                     for (int g = 0; g < 3; ++g) {
                         const uint64_t adesc = umma_desc(arow0 + (uint32_t)(g * c.sy) * 16u, c.rows_bytes, 128);
-                        const uint32_t bg = wbase + (uint32_t)(g * TC_WB_DY);
-                        // planes [lo, hi] as runs of adjacent chunks: cut where the ring wraps and, for the
-                        // first dy, before a fresh plane, whose chunk that MMA overwrites (no accumulate)
-                        int k0 = 0;
-                        while (k0 < np) {
-                            const int ck = (clo + k0) % TC_RING;
-                            int kn = min(np - k0, TC_RING - ck);
-                            const bool first_fresh = (g == 0) && fresh;
-                            if (first_fresh && k0 + kn == np && kn > 1) --kn;  // the fresh plane alone
-                            const bool acc = !(first_fresh && k0 == np - 1);
-                            const uint32_t b0 = bg + (uint32_t)((lo + k0 - (xi - 1)) * TC_CHUNK * 16);
-                            tc_mma(dwin + (uint32_t)(ck * TC_CHUNK), adesc, umma_desc(b0, TC_WB_KHALF, 128),
-                                   tc_idesc(kn * TC_CHUNK), acc ? 1u : 0u);
-                            k0 += kn;
-                        }
+                        const uint32_t b0 = wbase + (uint32_t)(g * TC_WB_DY) + boff;
+                        tc_mma(dwin + (uint32_t)(clo * TC_CHUNK), adesc, umma_desc(b0, TC_WB_KHALF, 128),
+                               tc_idesc(n1 * TC_CHUNK), 1u);
+                        if (n1 < np)
+                            tc_mma(dwin, adesc, umma_desc(b0 + (uint32_t)(n1 * TC_CHUNK * 16), TC_WB_KHALF, 128),
+                                   tc_idesc((np - n1) * TC_CHUNK), 1u);
                     }
                     tc_commit(&empty[q % NS]);  // the block is not read again
                     if (xi - 1 >= x0) tc_commit(&accfull[(it0 + (xi - 1 - x0)) % TC_RING]);  // plane xi - 1 done
@@ -365,19 +368,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
         const uint32_t usx = (uint32_t)c.sx, usy = (uint32_t)c.sy;
         const uint32_t tq = tmem + ((uint32_t)(quarter * 32) << 16) + (uint32_t)win * TC_WIN_COLS;
         float* xg = xchg + group * (2 * 4 * 2 * 16);
-        // every chunk starts free: the parity-0 groups give its first "drained" arrival (the first MMA
-        // into a fresh plane's chunk overwrites it, so nothing needs clearing)
+        // the accumulator chunks start at zero (every MMA accumulates); the parity-0 groups clear them
+        // and give the first "drained" arrival of every chunk
         if (par == 0) {
+            for (int a = 0; a < TC_RING; ++a) {
+#pragma unroll
+                for (int h = 0; h < 3; ++h) tc_st16_zero(tq + (uint32_t)(a * TC_CHUNK + 16 * h));
+            }
+            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+            tc_fence_before();
             __syncwarp();
             if (lane == 0)
                 for (int a = 0; a < TC_RING; ++a) mbar_arrive1(&accempty[a]);
         }
-        // the chunk's values are in registers: the MMA warps may start the plane TC_RING items later in it
-        auto release_chunk = [&](int a) {
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive1(&accempty[a]);
-        };
         int xp = 0;  // exchange buffer parity
         for (int64_t k = k_begin + par; k < k_end; k += TC_EPI_PAR) {
             const int it = (int)(k - k_begin);
@@ -418,7 +421,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
                     zp[q] = tc_ld1(taddr + 32 + q);
                 }
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                release_chunk(a);
 #pragma unroll
                 for (int q = 0; q < NOUT; ++q) {
                     if (lane == 31) xb[(quarter * 2 + 0) * 16 + q] = zm[q];
@@ -445,7 +447,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
                 tc_ld16(taddr + 16, z0);
                 tc_ld16(taddr + 32, zp);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                release_chunk(a);
                 float4* lo_dst = reinterpret_cast<float4*>(xb + (quarter * 2 + 0) * 16);
                 float4* hi_dst = reinterpret_cast<float4*>(xb + (quarter * 2 + 1) * 16);
                 if (lane == 31) {
@@ -493,7 +494,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
                     *reinterpret_cast<uint4*>(c.out + (c.plane_rows + pr) * 16) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
                 }
             }
+            // the chunk starts the plane TC_RING items later at zero
+#pragma unroll
+            for (int h = 0; h < 3; ++h) tc_st16_zero(taddr + (uint32_t)(16 * h));
+            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
             xp ^= 1;
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive1(&accempty[a]);
         }
     }
 

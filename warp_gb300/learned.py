@@ -430,6 +430,44 @@ def cg_pairs(f: _Field, nrhs: int, rng: np.random.Generator, iters=(0, 1, 2, 4, 
     return out
 
 
+def fcg_pairs(f: _Field, nrhs: int, rng: np.random.Generator, iters=(1, 2, 4, 6, 8, 12)):
+    """(r_k, e_k) along the flexible-CG runs the network will serve in: FCG preconditioned by the V-cycle
+    with the current (training) network, on random right-hand sides (e_k = x* - x_k, x* from a tight
+    solve with the Jacobi-smoothed cycle; normalised)."""
+    from .optim import linear
+
+    A_ = f.sys.A
+    n = f.n
+    keep = 1.0 - f.mask_dof
+    out = []
+    for _ in range(nrhs):
+        b = A.from_numpy(rng.uniform(-1.0, 1.0, n).astype(np.float32)) * keep
+        xs = torch.zeros(n, device=b.device)
+        saved = f.mg.smoother
+        f.mg.smoother = None
+        linear.fcg(A_, b, xs, tol=1e-7, atol=0.0, maxiter=400, M=f.mg, check_every=0)
+        f.mg.smoother = saved
+        x = torch.zeros(n, device=b.device)
+        snaps = {}
+
+        def grab(it, err, atol_v, x=x, snaps=snaps):
+            if it in iters:
+                snaps[it] = x.clone()
+
+        linear.fcg(A_, b, x, tol=0.0, atol=0.0, maxiter=max(iters), M=f.mg, callback=grab, check_every=1,
+                   use_cuda_graph=False)
+        for k in iters:
+            if k not in snaps:
+                continue
+            xk = snaps[k]
+            r = b.clone()
+            _spmv(A_, xk, r, -1.0, 1.0, _stream(), f.mg.status)
+            e = xs - xk
+            s = 1.0 / float(e.norm().clamp_min(1e-30))
+            out.append((r * s, e * s))
+    return out
+
+
 def slow_pairs(f: _Field, nrhs: int, rng: np.random.Generator, sweeps=(1, 2, 3, 5), smoother="current"):
     """Errors left by stationary V-cycle sweeps e <- e - V(A e) from random starts (normalised)."""
     n = f.n

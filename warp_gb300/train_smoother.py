@@ -54,7 +54,7 @@ def make_elasticity_field(res: int, seed: int, sigma: float = learned.SIGMA_DEFA
 def train(fields: int = 2000, res: int = 48, steps_per_field: int = 2, batch: int = 6, lr: float = 2e-3,
           lr_min: float = 1e-4, seed0: int = 10_000, eval_every: int = 250, out: str | None = None, log=print,
           net: learned.ConvNet | None = None, max_minutes: float | None = None,
-          problem: str = "diffusion") -> learned.ConvNet:
+          problem: str = "diffusion", fcg_rhs: int = 0) -> learned.ConvNet:
     if problem not in ("diffusion", "elasticity"):
         raise ValueError("problem: diffusion or elasticity")
     field_of = make_field if problem == "diffusion" else make_elasticity_field
@@ -77,6 +77,8 @@ def train(fields: int = 2000, res: int = 48, steps_per_field: int = 2, batch: in
         pairs = (learned.cg_pairs(f, 1, rng, iters=(0, 2, 8, 32))
                  + learned.slow_pairs(f, 1, rng, sweeps=(1, 2, 4))
                  + learned.slow_pairs(f, 1, rng, sweeps=(2,), smoother=None))
+        if fcg_rhs:  # residuals of the flexible solver the network serves, with the current network
+            pairs += learned.fcg_pairs(f, fcg_rhs, rng)
         for _ in range(steps_per_field):
             tr.lr = lr_min + 0.5 * (lr - lr_min) * (1.0 + math.cos(math.pi * step / max(total - 1, 1)))
             idx = rng.choice(len(pairs), size=min(batch, len(pairs)), replace=False)
@@ -106,12 +108,17 @@ def main():
     ap.add_argument("--out", default=learned.DEFAULT_WEIGHTS)
     ap.add_argument("--max-minutes", type=float, default=None)
     ap.add_argument("--problem", choices=["diffusion", "elasticity"], default="diffusion")
+    ap.add_argument("--fcg-rhs", type=int, default=0,
+                    help="right-hand sides per field whose flexible-CG residuals (current network) join the pairs")
+    ap.add_argument("--init", default=None, help="start from these weights instead of a fresh network")
     a = ap.parse_args()
     import os
 
     os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)
+    net = learned.ConvNet.load(a.init) if a.init else None
     train(a.fields, a.res, a.steps_per_field, a.batch, a.lr, eval_every=a.eval_every, out=a.out,
-          log=lambda m: print(m, flush=True), max_minutes=a.max_minutes, problem=a.problem)
+          log=lambda m: print(m, flush=True), max_minutes=a.max_minutes, problem=a.problem, fcg_rhs=a.fcg_rhs,
+          net=net)
 
 
 if __name__ == "__main__":
