@@ -449,10 +449,35 @@ def bench_elasticity_large(args, hbm_peak):
     out["mg_fcg_bf16_vcycle_inner_iterations"] = infos16[-1]["inner_iterations"]
     out["mg_fcg_bf16_vcycle_converged"] = infos16[-1]["converged"]
     out["mg_fcg_bf16_vcycle_oracle_rel_residual"] = _oracle_residual_3x3(A, s.b, xs16[-1])
+    # the 3-channel learned smoother (vec3 network, trained on elasticity fields with the 128^3 statistics)
+    from warp_gb300 import learned
+
+    if os.path.exists(learned.ELASTICITY_WEIGHTS):
+        del mg16, solver16
+        torch.cuda.empty_cache()
+        net3 = learned.ConvNet.load(learned.ELASTICITY_WEIGHTS)
+        mgL = multigrid.MultigridPreconditioner(A, s.geo, s.coef, faces=("x-",), fine_values=torch.bfloat16)
+        mgL.smoother = learned.LearnedSmoother(net3, mgL, s.coef)
+        solverL = linear.RefinedSolver(A, M=mgL, method="fcg", inner_tol=args.inner_tol, inner_maxiter=5000)
+        solverL.solve(s.b, tol=1e-8, max_outer=10)
+        infosL, xsL = [], []
+
+        def solveL():
+            x_, info_ = solverL.solve(s.b, tol=1e-8, max_outer=10)
+            infosL.append(info_)
+            xsL.append(x_)
+
+        out["learned_fcg_ms"] = _event_ms(solveL, 2, warmup=0)
+        out["learned_fcg_inner_iterations"] = infosL[-1]["inner_iterations"]
+        out["learned_fcg_converged"] = infosL[-1]["converged"]
+        out["learned_fcg_fallbacks"] = solverL.fallbacks
+        out["learned_fcg_oracle_rel_residual"] = _oracle_residual_3x3(A, s.b, xsL[-1])
+        out["learned_weights"] = os.path.relpath(learned.ELASTICITY_WEIGHTS, ROOT)
     out["note"] = ("flexible CG with the vec3 geometric V-cycle (point-Jacobi smoothing, damping 4/(3 rho) per "
                    "level); fp32 values, and bf16 fine-level values inside the V-cycle with fp32 values in the "
                    "flexible solver's product (bf16 values as the refinement's inner operator diverge on this "
-                   "field, sigma 1.5); the 3-channel conv-net smoother for this configuration is not built")
+                   "field, sigma 1.5); learned_fcg: the same bf16 cycle with the 3-channel conv-net smoother "
+                   "(16 hidden channels, tcgen05 layers) on the fine level")
     return out
 
 

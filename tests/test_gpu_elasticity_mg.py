@@ -158,3 +158,27 @@ def test_bf16_values_inside_the_vcycle_converge_on_the_rough_field(cuda):
     res = np.linalg.norm(bd - Ah @ x16.cpu().numpy()) / np.linalg.norm(bd)
     assert res <= 2e-8, res
     assert int(mg16.status.item()) == 0
+
+
+def test_trained_3_channel_smoother_solves_elasticity(cuda):
+    """The committed 3-channel network (vec3 fields, tcgen05 layers) inside the vec3 V-cycle: flexible CG
+    with FP64 refinement reaches 1e-8 on a rough elasticity field without falling back to Jacobi-CG."""
+    from warp_gb300 import learned, multigrid, problems
+    from warp_gb300.optim import linear
+
+    net = learned.ConvNet.load(learned.ELASTICITY_WEIGHTS)
+    assert net.ncomp == 3 and net.layers[-1][1] == 3
+    s = problems.elasticity((32,) * 3, sigma=1.5, corr_length=0.05 * 128 / 32, seed=1)
+    mg = multigrid.MultigridPreconditioner(s.A, s.geo, s.coef, faces=FACES, fine_values=torch.bfloat16)
+    mg.smoother = learned.LearnedSmoother(net, mg, s.coef)
+    solver = linear.RefinedSolver(s.A, M=mg, method="fcg", inner_maxiter=3000)
+    x, info = solver.solve(s.b, tol=1e-8)
+    assert info["converged"] and solver.fallbacks == 0, info
+    nnz = s.A.nnz_sync()
+    sp = pytest.importorskip("scipy.sparse")
+    n = s.A.nrow * 3
+    Ah = sp.bsr_matrix((s.A.values[:nnz].cpu().numpy().astype(np.float64).reshape(-1, 3, 3),
+                        s.A.columns[:nnz].cpu().numpy(), s.A.offsets.cpu().numpy()), shape=(n, n))
+    bd = s.b.cpu().numpy().astype(np.float64)
+    assert np.linalg.norm(bd - Ah @ x.cpu().numpy()) / np.linalg.norm(bd) <= 2e-8
+    assert int(mg.status.item()) == 0
