@@ -731,6 +731,10 @@ def main():
     M = linear.preconditioner(A, "diag")
     jsolver = linear.RefinedSolver(A, M=M, inner_tol=args.inner_tol)
     jms, jinfos, _, jclocks = timed(jsolver, system.b, args.steps, sample_clocks=True)
+    # the same solve with three kernels per CG iteration under a conditional graph node (the
+    # persistent cooperative launch switched off), for comparison
+    jsolver3 = linear.RefinedSolver(A, M=M, inner_tol=args.inner_tol, persistent=False)
+    j3ms, j3infos, _, _ = timed(jsolver3, system.b, max(3, args.steps // 4))
 
     # ---- the same flexible CG without the network (Jacobi-smoothed V-cycle) -------------------
     torch.cuda.synchronize()
@@ -963,7 +967,12 @@ def main():
                       "rel_residual": max(i["rel_residual"] for i in jinfos), "clocks": jclocks,
                       "iteration_frac_of_hbm": (jit_bytes * statistics.median([i["inner_iterations"] for i in jinfos])
                                                 / (jms * 1e-3) / 1e9 / hbm_peak),
-                      "iteration_bytes": jit_bytes, **oracle_check(jsolver.last_x)},
+                      "iteration_bytes": jit_bytes, "persistent_launch": jsolver.inner.persistent_active,
+                      "three_kernel_iteration": {
+                          "ms": j3ms, "inner_iterations": statistics.median([i["inner_iterations"] for i in j3infos]),
+                          "iteration_frac_of_hbm": (jit_bytes * statistics.median([i["inner_iterations"] for i in j3infos])
+                                                    / (j3ms * 1e-3) / 1e9 / hbm_peak)},
+                      **oracle_check(jsolver.last_x)},
         "mg_fcg_no_net": {"ms": fcg_ms, "inner_iterations": statistics.median([f["inner_iterations"] for f in finfos]),
                           "rel_residual": max(f["rel_residual"] for f in finfos), "fallbacks": fsolver.fallbacks,
                           "setup_ms": mg_setup_ms, **oracle_check(fsolver.last_x)},

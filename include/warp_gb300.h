@@ -121,7 +121,12 @@ int gb_axpby(int dtype, int64_t n, double alpha, const void* x, double beta, con
  * _update_condition / capture_while, :2086-2179; warp/native/warp.h:777).
  * gb_krylov_launch modes: 0 whole solve (init + device-side while loop, one graph), 1 init,
  * 2 `chunk_iters` iterations, 3 one eager iteration, 4 eager init.  Inside a caller's stream
- * capture, mode 0 appends the conditional loop to that capture. */
+ * capture, mode 0 appends the conditional loop to that capture.
+ * CG handles run their iterations as one persistent cooperative launch (three phases per iteration
+ * separated by grid barriers) when the device holds the whole SpMV grid at once; modes 0, 2 and 3
+ * then launch it for "until converged", `chunk_iters` and one iteration.  gb_krylov_set_persistent
+ * switches this off (three kernels per iteration under a conditional graph node) or back on and
+ * reports through active_out (may be null) whether the persistent launch will be used. */
 size_t gb_krylov_workspace_bytes(int kind, int block_dim, int nrow, int64_t nnz, int val_dtype);
 int gb_krylov_create(int kind, int block_dim, int nrow, int64_t nnz, int64_t ncap, int val_dtype, int rows_per_cta,
                      int lanes_per_row, int cap_blocks, void* workspace, size_t workspace_bytes, void** handle_out);
@@ -133,6 +138,7 @@ int gb_krylov_launch(void* handle, int what, int chunk_iters, gb_stream_t stream
 int gb_krylov_scalars(void* handle, int** iter, double** rr, double** atol_sq, int** status);
 int gb_krylov_read(void* handle, int* host_ints3, double* host_doubles3, gb_stream_t stream);
 int gb_krylov_vectors(void* handle, float** r, float** p, float** Ap);
+int gb_krylov_set_persistent(void* handle, int enable, int* active_out);
 
 /* ---- FP64 refinement pieces (no reference counterpart: the reference solves in the matrix
  * scalar type only; these wrap the fp32 solver of CG._run in iterative refinement) ------------- */

@@ -36,6 +36,10 @@ struct KrylovScalars {
     double rr_ref;  // residual^2 at the start of the current stagnation window
     int iter, cond, maxiter, status;
     unsigned int counters[8];
+    // grid barrier of the persistent CG: arrival count and generation on cache lines of their own
+    // (the generation is polled by every CTA; the count takes one atomic per CTA)
+    alignas(128) unsigned int bar_count;
+    alignas(128) unsigned int bar_gen;
 };
 
 struct SolveArgs {
@@ -247,6 +251,7 @@ __global__ __launch_bounds__(VEC_THREADS) void k_cg_update(const SolveArgs* __re
             S->status |= GB_DEV_NONFINITE;
             cond = 0;
         }
+        if (S->status & GB_DEV_BREAKDOWN) cond = 0;  // a non-finite alpha or beta ends the loop
         if (a.stag_window > 0 && cond && (S->iter % a.stag_window) == 0) {
             if (S->iter > a.stag_window && t[0] > a.stag_factor * a.stag_factor * S->rr_ref) {
                 S->status |= GB_DEV_STAGNATION;
@@ -292,6 +297,385 @@ __global__ __launch_bounds__(VEC_THREADS) void k_cg_pupdate(const SolveArgs* __r
         const float zi = a.dinv ? a.dinv[i] * a.r[i] : a.r[i];
         a.p[i] = zi + beta * a.p[i];
     }
+}
+
+// ---------------------------------------------------------------------------------------------
+// CG as one persistent cooperative launch
+// ---------------------------------------------------------------------------------------------
+// The three phases of an iteration -- (1) Ap = A p with p.Ap, (2) x += alpha p, r -= alpha Ap with
+// r.r and r.z, (3) p = D^-1 r + beta p -- run inside one kernel whose CTAs are all resident
+// (cooperative launch) and meet at a grid barrier after each phase.  Phase 1 is the SpMV pipeline
+// over the CTA's tiles of block rows (blockIdx.x + k gridDim.x); phases 2 and 3 walk the vectors
+// grid-stride (after a barrier every CTA may read any row).  Every CTA sums all CTAs' partials in the
+// same fixed order, so all derive bit-identical alpha, beta and loop condition without a broadcast.
+// The producer warp streams the matrix tiles continuously across iterations (the matrix does not
+// change), so the copy ring does not drain at the barriers; those copies carry an L2 evict-first
+// policy so that the vectors of phases 2 and 3 stay in L2.  p is gathered with coherent (non-.nc)
+// loads since it changes between phases of the same launch.  Per iteration the arithmetic is that of
+// k_cg_spmv / k_cg_update / k_cg_pupdate; only the order of the partial sums differs.
+// Every wait is bounded: a barrier that does not complete within kWaitLimitNs sets
+// GB_DEV_WAIT_TIMEOUT and ends the CTA's loop.
+
+__device__ __forceinline__ void consumer_sync()
+{
+    asm volatile("bar.sync 1, %0;" ::"r"(SPMV_CONSUMERS) : "memory");
+}
+
+__device__ __forceinline__ unsigned int ld_acquire_u32(const unsigned int* p)
+{
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_u32(unsigned int* p, unsigned int v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid barrier among the consumer threads of every CTA (thread 32 arrives for its CTA): the last
+// arrival resets the count and advances the generation; the others poll the generation.  Returns
+// the same value in every consumer thread of the CTA: false if the wait ran out or a warp of the CTA
+// flagged a failed wait beforehand (*s_fail).
+__device__ __forceinline__ bool cg_grid_barrier(KrylovScalars* S, volatile int* s_ok, volatile int* s_fail)
+{
+    consumer_sync();
+    if (threadIdx.x == 32) {
+        const unsigned int g = ld_acquire_u32(&S->bar_gen);
+        __threadfence();
+        const unsigned int prev = atomicAdd(&S->bar_count, 1u);
+        int ok = 1;
+        if (prev == gridDim.x - 1) {
+            atomicExch(&S->bar_count, 0u);
+            __threadfence();
+            st_release_u32(&S->bar_gen, g + 1u);
+        } else {
+            const uint64_t t0 = globaltimer_ns();
+            while (ld_acquire_u32(&S->bar_gen) == g) {
+                if (globaltimer_ns() - t0 > kWaitLimitNs) {
+                    ok = 0;
+                    break;
+                }
+            }
+        }
+        *s_ok = ok && !*s_fail;
+    }
+    consumer_sync();
+    return *s_ok != 0;
+}
+
+// Sum of NV per-thread values over the 512 consumer threads; the result is valid in thread 32.
+template <int NV> __device__ __forceinline__ void consumer_sum(const float (&v)[NV], double* s_red, double (&out)[NV])
+{
+    const int cw = (threadIdx.x >> 5) - 1, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        const double w = (double)warp_sum(v[k]);
+        if (lane == 0) s_red[cw * NV + k] = w;
+    }
+    consumer_sync();
+    if (cw == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            const double w = lane < SPMV_CONSUMER_WARPS ? s_red[lane * NV + k] : 0.0;
+            out[k] = warp_sum(w);
+        }
+    }
+}
+
+// Sum of every CTA's partials part[k * gridDim.x + c] by the first consumer warp, in a fixed order
+// (the same in every CTA); thread 32 passes the totals to `update` (which changes the shared solver
+// state), and the consumers resynchronise so that all of them see the new state.
+template <int NV, typename Update> __device__ __forceinline__ void all_partials(const double* part, Update update)
+{
+    if ((threadIdx.x >> 5) == 1) {
+        const int lane = threadIdx.x & 31;
+        double t[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double acc = 0.0;
+            for (int c = lane; c < (int)gridDim.x; c += 32) acc += __ldcg(part + (size_t)k * gridDim.x + c);
+            t[k] = warp_sum(acc);
+        }
+        if (lane == 0) update(t);
+    }
+    consumer_sync();
+}
+
+struct LoopState {
+    double rz, rr, rr_ref, atol_sq, pAp, alpha, beta;
+    int iter, cond, maxiter, breakdown;
+};
+
+template <int BR, typename VT>
+__global__ __launch_bounds__(SPMV_THREADS, 2) void k_cg_loop(const SolveArgs* __restrict__ args, int nrow, SpmvShape sh,
+                                                          int max_iters)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double s_red[SPMV_CONSUMER_WARPS * 2];
+    __shared__ LoopState st;
+    __shared__ int s_ok, s_fail, s_stop;
+    const SolveArgs a = *args;
+    KrylovScalars* S = a.S;
+    const SpmvRing R = spmv_ring<BR, BR, VT>(smem, sh);
+    const int NS = sh.stages;
+    const int ntiles = (nrow + sh.rows - 1) / sh.rows;
+    const int own = blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const VT* values = (const VT*)a.values;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < NS; ++s) {
+            mbar_init(&R.full[s], 1);
+            mbar_init(&R.empty[s], SPMV_CONSUMER_WARPS);
+        }
+        fence_mbar_init();
+        s_stop = 0;
+        s_fail = 0;
+    }
+    __syncthreads();
+
+    if (warp == 0) {
+        // ------------------ producer: tiles of successive iterations, until told to stop -----------
+        if (lane == 0 && own > 0) {
+            const uint64_t policy = l2_policy_evict_first();
+            auto range = [&](int j, int& b0, int& b1) {
+                const int r0 = ((int)blockIdx.x + j * (int)gridDim.x) * sh.rows;
+                b0 = a.offsets[r0];
+                b1 = a.offsets[min(r0 + sh.rows, nrow)];
+            };
+            int nb0, nb1;
+            range(0, nb0, nb1);
+            int issued = 0;
+            bool timed_out = false, stop = false;
+            for (int i = 0; !stop; ++i) {
+                const int j = i % own;
+                const int s = i % NS;
+                const uint32_t ph = (uint32_t)(i / NS) & 1u;
+                const int b0 = nb0, b1 = nb1;
+                range(j + 1 < own ? j + 1 : 0, nb0, nb1);
+                if (i >= NS) {
+                    const uint64_t t0 = globaltimer_ns();
+                    for (;;) {
+                        if (mbar_try_wait(&R.empty[s], ph ^ 1u)) break;
+                        if (*(volatile int*)&s_stop) {
+                            stop = true;
+                            break;
+                        }
+                        if (globaltimer_ns() - t0 > kWaitLimitNs) {
+                            timed_out = stop = true;
+                            break;
+                        }
+                    }
+                    if (stop) break;
+                } else if (*(volatile int*)&s_stop) {
+                    break;
+                }
+                spmv_issue<BR, BR, VT>(R, sh, nrow, s, (int)blockIdx.x + j * (int)gridDim.x, b0, b1, a.offsets,
+                                       a.columns, values, true, policy);
+                ++issued;
+            }
+            if (timed_out) atomicOr(&S->status, GB_DEV_WAIT_TIMEOUT);
+            // drain: no bulk copy of this CTA may still be in flight when it exits
+            for (int q = max(0, issued - NS); q < issued; ++q)
+                mbar_wait_bounded(&R.full[q % NS], (uint32_t)(q / NS) & 1u);
+        }
+    } else {
+        // ------------------ consumers: the three phases of every iteration ------------------------
+        // The solver scalars live in shared memory, updated by thread 32 from the grid-wide sums
+        // (identical in every CTA); CTA 0 writes them back to the device scalars at the end.
+        const int ct = threadIdx.x - 32;
+        if (threadIdx.x == 32) {
+            st.rz = S->rz;
+            st.rr = S->rr;
+            st.rr_ref = S->rr_ref;
+            st.atol_sq = S->atol_sq;
+            st.pAp = S->pAp;
+            st.alpha = S->alpha;
+            st.beta = S->beta;
+            st.iter = S->iter;
+            st.cond = S->cond;
+            st.maxiter = S->maxiter;
+            st.breakdown = 0;
+        }
+        consumer_sync();
+        const bool lead = (blockIdx.x == 0 && threadIdx.x == 32);
+        double* partA = a.partials;              // [gridDim.x]: p.Ap
+        double* partB = a.partials + gridDim.x;  // [2][gridDim.x]: r.r, r.z
+        const bool vec4 = ((((uintptr_t)a.x | (uintptr_t)a.r | (uintptr_t)a.p | (uintptr_t)a.Ap |
+                             (uintptr_t)(a.dinv ? a.dinv : a.r)) & 15) == 0);
+        int i = 0, done = 0;
+        bool ok = true;
+        while (st.cond && (max_iters <= 0 || done < max_iters)) {
+            // (1) Ap = A p, p.Ap
+            EpiCgAp<BR, float> epi{a.Ap, a.p};
+            for (int j = 0; j < own; ++j, ++i) {
+                const int s = i % NS;
+                const uint32_t ph = (uint32_t)(i / NS) & 1u;
+                const bool full_ok = __all_sync(0xffffffffu, mbar_wait_bounded(&R.full[s], ph));
+                if (full_ok) {
+                    spmv_consume<BR, BR, VT, float, float, true>(R, sh, s, ct, a.row_counts, a.columns, values, a.p,
+                                                                 epi);
+                } else if (lane == 0) {
+                    *(volatile int*)&s_fail = 1;
+                }
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&R.empty[s]);
+            }
+            {
+                const float v[1] = {epi.pAp};
+                double t[1];
+                consumer_sum<1>(v, s_red, t);
+                if (threadIdx.x == 32) partA[blockIdx.x] = t[0];
+            }
+            if (!cg_grid_barrier(S, &s_ok, &s_fail)) {
+                ok = false;
+                break;
+            }
+            all_partials<1>(partA, [&](const double (&t)[1]) {
+                st.pAp = t[0];
+                double alpha = 0.0;
+                if (st.rr > st.atol_sq) {
+                    alpha = st.rz / t[0];
+                    if (!finite(alpha)) {
+                        if (blockIdx.x == 0) atomicOr(&S->status, GB_DEV_BREAKDOWN);
+                        st.breakdown = 1;
+                        alpha = 0.0;
+                    }
+                }
+                st.alpha = alpha;
+            });
+            // (2) x += alpha p, r -= alpha Ap; r.r and r.z (grid-stride: after the barrier every CTA
+            // may read any row of Ap)
+            float prr = 0.f, prz = 0.f;
+            {
+                const float al = (float)st.alpha;
+                int64_t e = 0;
+                if (vec4) {
+                    const int64_t n4 = a.n >> 2;
+                    for (int64_t q = (int64_t)blockIdx.x * SPMV_CONSUMERS + ct; q < n4;
+                         q += (int64_t)gridDim.x * SPMV_CONSUMERS) {
+                        float4 xv = reinterpret_cast<float4*>(a.x)[q], rv = reinterpret_cast<float4*>(a.r)[q];
+                        const float4 pv = reinterpret_cast<const float4*>(a.p)[q];
+                        const float4 av = reinterpret_cast<const float4*>(a.Ap)[q];
+                        xv.x += al * pv.x; xv.y += al * pv.y; xv.z += al * pv.z; xv.w += al * pv.w;
+                        rv.x -= al * av.x; rv.y -= al * av.y; rv.z -= al * av.z; rv.w -= al * av.w;
+                        float4 zv = rv;
+                        if (a.dinv) {
+                            const float4 dv = reinterpret_cast<const float4*>(a.dinv)[q];
+                            zv.x *= dv.x; zv.y *= dv.y; zv.z *= dv.z; zv.w *= dv.w;
+                        }
+                        reinterpret_cast<float4*>(a.x)[q] = xv;
+                        reinterpret_cast<float4*>(a.r)[q] = rv;
+                        prr += rv.x * rv.x + rv.y * rv.y + rv.z * rv.z + rv.w * rv.w;
+                        prz += rv.x * zv.x + rv.y * zv.y + rv.z * zv.z + rv.w * zv.w;
+                    }
+                    e = n4 << 2;
+                }
+                for (int64_t k = e + (int64_t)blockIdx.x * SPMV_CONSUMERS + ct; k < a.n;
+                     k += (int64_t)gridDim.x * SPMV_CONSUMERS) {
+                    const float ri = a.r[k] - al * a.Ap[k];
+                    const float zi = a.dinv ? a.dinv[k] * ri : ri;
+                    a.x[k] += al * a.p[k];
+                    a.r[k] = ri;
+                    prr += ri * ri;
+                    prz += ri * zi;
+                }
+            }
+            {
+                const float v[2] = {prr, prz};
+                double t[2];
+                consumer_sum<2>(v, s_red, t);
+                if (threadIdx.x == 32) {
+                    partB[blockIdx.x] = t[0];
+                    partB[gridDim.x + blockIdx.x] = t[1];
+                }
+            }
+            if (!cg_grid_barrier(S, &s_ok, &s_fail)) {
+                ok = false;
+                break;
+            }
+            all_partials<2>(partB, [&](const double (&t)[2]) {
+                const double rz_old = st.rz;
+                st.rr = t[0];
+                st.rz = t[1];
+                double beta = 0.0;
+                if (t[0] > st.atol_sq) {
+                    beta = t[1] / rz_old;
+                    if (!finite(beta)) {
+                        if (blockIdx.x == 0) atomicOr(&S->status, GB_DEV_BREAKDOWN);
+                        st.breakdown = 1;
+                        beta = 0.0;
+                    }
+                }
+                st.beta = beta;
+                st.iter += 1;
+                int cond = (t[0] > st.atol_sq) && (st.iter < st.maxiter) && !st.breakdown;
+                if (!finite(t[0])) {
+                    if (blockIdx.x == 0) atomicOr(&S->status, GB_DEV_NONFINITE);
+                    cond = 0;
+                }
+                if (a.stag_window > 0 && cond && (st.iter % a.stag_window) == 0) {
+                    if (st.iter > a.stag_window && t[0] > a.stag_factor * a.stag_factor * st.rr_ref) {
+                        if (blockIdx.x == 0) atomicOr(&S->status, GB_DEV_STAGNATION);
+                        cond = 0;
+                    }
+                    st.rr_ref = t[0];
+                }
+                st.cond = cond;
+            });
+            ++done;
+            if (!st.cond) break;
+            // (3) p = D^-1 r + beta p (grid-stride)
+            {
+                const float be = (float)st.beta;
+                int64_t e = 0;
+                if (vec4) {
+                    const int64_t n4 = a.n >> 2;
+                    for (int64_t q = (int64_t)blockIdx.x * SPMV_CONSUMERS + ct; q < n4;
+                         q += (int64_t)gridDim.x * SPMV_CONSUMERS) {
+                        float4 zv = reinterpret_cast<const float4*>(a.r)[q];
+                        if (a.dinv) {
+                            const float4 dv = reinterpret_cast<const float4*>(a.dinv)[q];
+                            zv.x *= dv.x; zv.y *= dv.y; zv.z *= dv.z; zv.w *= dv.w;
+                        }
+                        float4 pv = reinterpret_cast<float4*>(a.p)[q];
+                        pv.x = zv.x + be * pv.x; pv.y = zv.y + be * pv.y; pv.z = zv.z + be * pv.z;
+                        pv.w = zv.w + be * pv.w;
+                        reinterpret_cast<float4*>(a.p)[q] = pv;
+                    }
+                    e = n4 << 2;
+                }
+                for (int64_t k = e + (int64_t)blockIdx.x * SPMV_CONSUMERS + ct; k < a.n;
+                     k += (int64_t)gridDim.x * SPMV_CONSUMERS) {
+                    const float zi = a.dinv ? a.dinv[k] * a.r[k] : a.r[k];
+                    a.p[k] = zi + be * a.p[k];
+                }
+            }
+            if (!cg_grid_barrier(S, &s_ok, &s_fail)) {
+                ok = false;
+                break;
+            }
+        }
+        consumer_sync();
+        if (threadIdx.x == 32 && !ok) {
+            atomicOr(&S->status, GB_DEV_WAIT_TIMEOUT);
+            st.cond = 0;
+        }
+        if (lead) {
+            S->rr = st.rr;
+            S->rz = st.rz;
+            S->rr_ref = st.rr_ref;
+            S->pAp = st.pAp;
+            S->alpha = st.alpha;
+            S->beta = st.beta;
+            S->iter = st.iter;
+            S->cond = ok ? st.cond : 0;
+        }
+        consumer_sync();
+        if (threadIdx.x == 32) *(volatile int*)&s_stop = 1;
+    }
+    __syncthreads();
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -585,6 +969,7 @@ __global__ void k_store_args(SolveArgs* dst, SolveArgs src, int reset_status)
     if (reset_status) {
         src.S->status = 0;
         for (int k = 0; k < 8; ++k) src.S->counters[k] = 0u;
+        src.S->bar_count = 0u;
         src.S->cond = 1;
     }
 }
@@ -605,7 +990,11 @@ struct Solver {
     int chunk_iters = 0;
     gb_precond_fn precond = nullptr;  // flexible solver only
     void* precond_user = nullptr;
+    int loop_grid = 0;   // CTAs of the persistent CG launch (0: the device cannot hold the SpMV grid at once)
+    int persistent = 1;  // CG: run iterations as one cooperative launch when loop_grid > 0
 };
+
+static bool use_loop(const Solver* s) { return s->kind == KRYLOV_CG && s->persistent && s->loop_grid > 0; }
 
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
@@ -635,7 +1024,48 @@ template <int BR, typename VT> static void set_smem_attr(Solver* s)
         cudaFuncSetAttribute(k_bi_init<BR, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->spmv_smem);
         cudaFuncSetAttribute(k_bi_spmv_v<BR, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->spmv_smem);
         cudaFuncSetAttribute(k_bi_spmv_t<BR, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->spmv_smem);
+        cudaFuncSetAttribute(k_cg_loop<BR, VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s->spmv_smem);
     }
+    // the persistent CG needs every CTA resident at once: as many as the device holds, at most the
+    // SpMV's own grid
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_loop<BR, VT>, SPMV_THREADS, s->spmv_smem) !=
+        cudaSuccess) {
+        (void)cudaGetLastError();
+        per_sm = 0;
+    }
+    int coop = 0, dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess) {
+        (void)cudaGetLastError();
+        coop = 0;
+    }
+    s->loop_grid = coop ? std::min(s->spmv_grid, per_sm * sm_count()) : 0;
+}
+
+// One cooperative launch of the persistent CG: at most max_iters iterations (0: until the loop
+// condition clears).
+template <int BR, typename VT> static int launch_loop_t(Solver* s, cudaStream_t st, int max_iters)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)s->loop_grid);
+    cfg.blockDim = dim3(SPMV_THREADS);
+    cfg.dynamicSmemBytes = s->spmv_smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    GB_CHECK_CUDA(cudaLaunchKernelEx(&cfg, k_cg_loop<BR, VT>, (const SolveArgs*)s->d_args, s->nrow, s->sh, max_iters));
+    return GB_OK;
+}
+
+static int launch_loop(Solver* s, cudaStream_t st, int max_iters)
+{
+    if (s->br == 1) return s->val_dtype == GB_BF16 ? launch_loop_t<1, __nv_bfloat16>(s, st, max_iters)
+                                                   : launch_loop_t<1, float>(s, st, max_iters);
+    return s->val_dtype == GB_BF16 ? launch_loop_t<3, __nv_bfloat16>(s, st, max_iters)
+                                   : launch_loop_t<3, float>(s, st, max_iters);
 }
 
 template <int BR, typename VT>
@@ -665,6 +1095,8 @@ static int launch_iter_t(Solver* s, cudaStream_t st, cudaGraphConditionalHandle 
         GB_CHECK_CUDA(launch_pdl(k_fcg_p, s->vec_grid, VEC_THREADS, 0, st, s->d_args));
         GB_CHECK_CUDA(launch_pdl(k_cg_spmv<BR, VT>, s->spmv_grid, SPMV_THREADS, s->spmv_smem, st, s->d_args, s->nrow, s->sh));
         GB_CHECK_CUDA(launch_pdl(k_cg_update, s->vec_grid, VEC_THREADS, 0, st, s->d_args, h, has_cond));
+    } else if (s->kind == KRYLOV_CG && use_loop(s)) {
+        return launch_loop(s, st, 1);
     } else if (s->kind == KRYLOV_CG) {
         GB_CHECK_CUDA(launch_pdl(k_cg_spmv<BR, VT>, s->spmv_grid, SPMV_THREADS, s->spmv_smem, st, s->d_args, s->nrow, s->sh));
         GB_CHECK_CUDA(launch_pdl(k_cg_update, s->vec_grid, VEC_THREADS, 0, st, s->d_args, h, has_cond));
@@ -710,6 +1142,11 @@ static int capture_full_solve(Solver* s, cudaStream_t st)
     if (cs != cudaStreamCaptureStatusActive) {
         gb::set_error("capture_full_solve: stream is not capturing");
         return GB_ERR_INVALID;
+    }
+    if (use_loop(s)) {  // init, then the whole loop in one launch: no conditional node needed
+        int rc = launch_init(s, st, 0, 0);
+        if (rc) return rc;
+        return launch_loop(s, st, 0);
     }
     cudaGraphConditionalHandle h;
     GB_CHECK_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0, 0));
@@ -769,7 +1206,9 @@ static int build_graphs(Solver* s, int chunk_iters)
         s->exec_chunk = nullptr;
         GB_CHECK_CUDA(cudaStreamBeginCapture(s->cap_stream, cudaStreamCaptureModeRelaxed));
         int rc = GB_OK;
-        for (int k = 0; k < chunk_iters && rc == GB_OK; ++k) rc = launch_iter(s, s->cap_stream, 0, 0);
+        if (use_loop(s)) rc = launch_loop(s, s->cap_stream, chunk_iters);
+        else
+            for (int k = 0; k < chunk_iters && rc == GB_OK; ++k) rc = launch_iter(s, s->cap_stream, 0, 0);
         cudaError_t e = cudaStreamEndCapture(s->cap_stream, &g);
         if (rc) return rc;
         GB_CHECK_CUDA(e);
@@ -955,6 +1394,7 @@ GB_API int gb_krylov_launch(void* handle, int what, int chunk_iters, cudaStream_
     if (capturing) {
         if (what == 0) return capture_full_solve(s, stream);
         if (what == 1) return launch_init(s, stream, 0, 0);
+        if (use_loop(s)) return chunk_iters > 0 ? launch_loop(s, stream, chunk_iters) : GB_OK;
         int rc = GB_OK;
         for (int k = 0; k < chunk_iters && rc == GB_OK; ++k) rc = launch_iter(s, stream, 0, 0);
         return rc;
@@ -1026,5 +1466,23 @@ GB_API int gb_krylov_set_precond(void* handle, gb_precond_fn fn, void* user, int
     if (s->exec_chunk) cudaGraphExecDestroy(s->exec_chunk);
     s->exec_while = s->exec_init = s->exec_chunk = nullptr;
     s->chunk_iters = 0;
+    return GB_OK;
+}
+
+// CG only: enable (1, the default) or disable (0) running the iterations as one persistent
+// cooperative launch (used when the device holds the whole SpMV grid at once); 0 keeps the three
+// kernels per iteration under a conditional graph node.  Drops any cached graphs.  Returns, through
+// active_out (may be null), whether the persistent launch will be used.
+GB_API int gb_krylov_set_persistent(void* handle, int enable, int* active_out)
+{
+    Solver* s = static_cast<Solver*>(handle);
+    GB_REQUIRE(s, "krylov_set_persistent: null handle");
+    s->persistent = enable ? 1 : 0;
+    if (s->exec_while) cudaGraphExecDestroy(s->exec_while);
+    if (s->exec_init) cudaGraphExecDestroy(s->exec_init);
+    if (s->exec_chunk) cudaGraphExecDestroy(s->exec_chunk);
+    s->exec_while = s->exec_init = s->exec_chunk = nullptr;
+    s->chunk_iters = 0;
+    if (active_out) *active_out = use_loop(s) ? 1 : 0;
     return GB_OK;
 }

@@ -250,6 +250,7 @@ class LinearSolverState:
         self._maxiter = int(maxiter)
         self._native = None
         self._ws = None
+        self.persistent_active = False
         self._fused = self._fused_eligible(self._A, self._M, self._b, self._x)
         if self._fused:
             self._create_native()
@@ -286,6 +287,11 @@ class LinearSolverState:
                                    self._ws.data_ptr(), self._ws.numel(), ctypes.byref(h)), "krylov_create")
         self._native = h
         self._native_key = (bsr.nrow, nnz, bdim, vdt)
+        active = ctypes.c_int(0)
+        if self._kind == N.KRYLOV_CG:
+            N.check(L.gb_krylov_set_persistent(h, 1 if getattr(self, "_persistent", True) else 0,
+                                               ctypes.byref(active)), "krylov_set_persistent")
+        self.persistent_active = bool(active.value)
         it = ctypes.c_void_p()
         rr = ctypes.c_void_p()
         at = ctypes.c_void_p()
@@ -408,7 +414,12 @@ class CG(LinearSolverState):
     _kind = N.KRYLOV_CG
 
     def __init__(self, A_, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_every=10,
-                 use_cuda_graph=True, restart=None):
+                 use_cuda_graph=True, restart=None, *, persistent: bool = True):
+        """``persistent`` (not in the reference): on the fused path, run the iterations as one
+        persistent cooperative launch (three phases per iteration separated by grid barriers) when
+        the device holds the SpMV grid at once, else three kernels per iteration under a
+        conditional graph node.  ``persistent_active`` tells which one runs."""
+        self._persistent = bool(persistent)
         if restart is not None:
             if isinstance(restart, bool) or not isinstance(restart, int):
                 raise TypeError("restart must be an integer or None")
@@ -938,7 +949,7 @@ class RefinedSolver:
 
     def __init__(self, Am: sparse.BsrMatrix, M: LinearOperator | None = None, method: str = "cg",
                  inner_tol: float = 1e-5, inner_maxiter: int = 0, inner_values: torch.Tensor | None = None,
-                 residual: str = "df32", use_cuda_graph: bool = True):
+                 residual: str = "df32", use_cuda_graph: bool = True, persistent: bool = True):
         self.A = Am
         self.M = M
         self.n = Am.nrow * Am.block_shape[0]
@@ -966,11 +977,13 @@ class RefinedSolver:
             # Jacobi-CG: the fallback when the flexible solve stagnates
             self._jacobi_M = preconditioner(self._inner_A, "diag")
             self._jacobi = CG(self._inner_A, self._r32, self._d, tol=self.inner_tol, atol=0.0,
-                              maxiter=self.inner_maxiter, M=self._jacobi_M, **loop)
+                              maxiter=self.inner_maxiter, M=self._jacobi_M, persistent=persistent, **loop)
+        elif method == "cg":
+            self.inner = CG(self._inner_A, self._r32, self._d, tol=self.inner_tol, atol=0.0,
+                            maxiter=self.inner_maxiter, M=M, persistent=persistent, **loop)
         else:
-            cls = CG if method == "cg" else BiCGSTAB
-            self.inner = cls(self._inner_A, self._r32, self._d, tol=self.inner_tol, atol=0.0,
-                             maxiter=self.inner_maxiter, M=M, **loop)
+            self.inner = BiCGSTAB(self._inner_A, self._r32, self._d, tol=self.inner_tol, atol=0.0,
+                                  maxiter=self.inner_maxiter, M=M, **loop)
         if not self.inner._fused:
             raise ValueError("solve_refined needs a BSR operator with 1x1/3x3 float32 blocks and a Jacobi or no "
                              "preconditioner")
@@ -1035,8 +1048,12 @@ class RefinedSolver:
             self._d.zero_()
             self.inner._run_fused(Aop, self._r32, self._d, self.inner._M, x_is_zero=True)
             it = int(self.inner._dev_iter.item())
-            per_it = 3 if self.method != "fcg" else 4 + getattr(self.inner._precond_obj, "kernels_per_apply", 0)
-            self.kernel_launches += 2 + per_it * it  # argument store, init, kernels per iteration
+            if self.inner.persistent_active:
+                # argument store, init and the persistent loop (one launch per host-checked chunk)
+                self.kernel_launches += 3 if self.inner._check_every == 0 else 2 + it
+            else:
+                per_it = 3 if self.method != "fcg" else 4 + getattr(self.inner._precond_obj, "kernels_per_apply", 0)
+                self.kernel_launches += 2 + per_it * it  # argument store, init, kernels per iteration
             if self.method == "fcg":
                 status = int(self.inner._dev_status.item())
                 if status & (N.DEV_STAGNATION | N.DEV_BREAKDOWN | N.DEV_NONFINITE):
@@ -1046,7 +1063,10 @@ class RefinedSolver:
                     self._jacobi._run_fused(Aop, self._r32, self._d, self._jacobi_M, x_is_zero=False)
                     jt = int(self._jacobi._dev_iter.item())
                     it += jt
-                    self.kernel_launches += 2 + 3 * jt
+                    if self._jacobi.persistent_active:
+                        self.kernel_launches += 3 if self._jacobi._check_every == 0 else 2 + jt
+                    else:
+                        self.kernel_launches += 2 + 3 * jt
             N.check(L.gb_update_solution(self.n, A.ptr(x64), A.ptr(self._x2), A.ptr(self._d), 1.0, A.stream()),
                     "update_solution")
             self.kernel_launches += 1
