@@ -342,12 +342,13 @@ __device__ __forceinline__ bool cg_grid_barrier(KrylovScalars* S, volatile int* 
     consumer_sync();
     if (threadIdx.x == 32) {
         const unsigned int g = ld_acquire_u32(&S->bar_gen);
-        __threadfence();
-        const unsigned int prev = atomicAdd(&S->bar_count, 1u);
+        unsigned int prev;
+        // release: the CTA's writes (ordered before this thread by the barrier above) become visible
+        // to every CTA that acquires the new generation
+        asm volatile("atom.add.release.gpu.global.u32 %0, [%1], 1;" : "=r"(prev) : "l"(&S->bar_count) : "memory");
         int ok = 1;
         if (prev == gridDim.x - 1) {
             atomicExch(&S->bar_count, 0u);
-            __threadfence();
             st_release_u32(&S->bar_gen, g + 1u);
         } else {
             const uint64_t t0 = globaltimer_ns();
@@ -383,20 +384,31 @@ template <int NV> __device__ __forceinline__ void consumer_sum(const float (&v)[
     }
 }
 
-// Sum of every CTA's partials part[k * gridDim.x + c] by the first consumer warp, in a fixed order
-// (the same in every CTA); thread 32 passes the totals to `update` (which changes the shared solver
-// state), and the consumers resynchronise so that all of them see the new state.
-template <int NV, typename Update> __device__ __forceinline__ void all_partials(const double* part, Update update)
+// Sum of every CTA's partials part[k * gridDim.x + c] over the consumer threads (one or two loads
+// each, then warp sums and a sum of the 16 warp totals), in the same fixed order in every CTA;
+// thread 32 passes the totals to `update` (which changes the shared solver state), and the consumers
+// resynchronise so that all of them see the new state.
+template <int NV, typename Update>
+__device__ __forceinline__ void all_partials(const double* part, double* s_red, Update update)
 {
-    if ((threadIdx.x >> 5) == 1) {
-        const int lane = threadIdx.x & 31;
+    const int ct = threadIdx.x - 32, cw = ct >> 5, lane = threadIdx.x & 31;
+    double acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) acc[k] = 0.0;
+    for (int c = ct; c < (int)gridDim.x; c += SPMV_CONSUMERS) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) acc[k] += __ldcg(part + (size_t)k * gridDim.x + c);
+    }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        const double w = warp_sum(acc[k]);
+        if (lane == 0) s_red[cw * NV + k] = w;
+    }
+    consumer_sync();
+    if (cw == 0) {
         double t[NV];
 #pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            double acc = 0.0;
-            for (int c = lane; c < (int)gridDim.x; c += 32) acc += __ldcg(part + (size_t)k * gridDim.x + c);
-            t[k] = warp_sum(acc);
-        }
+        for (int k = 0; k < NV; ++k) t[k] = warp_sum(lane < SPMV_CONSUMER_WARPS ? s_red[lane * NV + k] : 0.0);
         if (lane == 0) update(t);
     }
     consumer_sync();
@@ -532,7 +544,7 @@ __global__ __launch_bounds__(SPMV_THREADS, 2) void k_cg_loop(const SolveArgs* __
                 ok = false;
                 break;
             }
-            all_partials<1>(partA, [&](const double (&t)[1]) {
+            all_partials<1>(partA, s_red, [&](const double (&t)[1]) {
                 st.pAp = t[0];
                 double alpha = 0.0;
                 if (st.rr > st.atol_sq) {
@@ -595,7 +607,7 @@ __global__ __launch_bounds__(SPMV_THREADS, 2) void k_cg_loop(const SolveArgs* __
                 ok = false;
                 break;
             }
-            all_partials<2>(partB, [&](const double (&t)[2]) {
+            all_partials<2>(partB, s_red, [&](const double (&t)[2]) {
                 const double rz_old = st.rz;
                 st.rr = t[0];
                 st.rz = t[1];
