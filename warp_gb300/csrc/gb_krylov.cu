@@ -18,6 +18,7 @@
 // Kernels read the operand pointers through a small device-side argument block so one captured
 // graph serves every right-hand side / solution vector / matrix with the same shape.
 #include "gb_common.cuh"
+#include "gb_df32.cuh"
 #include "gb_spmv.cuh"
 
 #include <new>
@@ -40,6 +41,8 @@ struct KrylovScalars {
     // (the generation is polled by every CTA; the count takes one atomic per CTA)
     alignas(128) unsigned int bar_count;
     alignas(128) unsigned int bar_gen;
+    // tile queues of the persistent CG's SpMV phase, one per iteration parity (zero between launches)
+    alignas(128) unsigned int tile_ctr[2];
 };
 
 struct SolveArgs {
@@ -304,15 +307,17 @@ __global__ __launch_bounds__(VEC_THREADS) void k_cg_pupdate(const SolveArgs* __r
 // ---------------------------------------------------------------------------------------------
 // The three phases of an iteration -- (1) Ap = A p with p.Ap, (2) x += alpha p, r -= alpha Ap with
 // r.r and r.z, (3) p = D^-1 r + beta p -- run inside one kernel whose CTAs are all resident
-// (cooperative launch) and meet at a grid barrier after each phase.  Phase 1 is the SpMV pipeline
-// over the CTA's tiles of block rows (blockIdx.x + k gridDim.x); phases 2 and 3 walk the vectors
-// grid-stride (after a barrier every CTA may read any row).  Every CTA sums all CTAs' partials in the
-// same fixed order, so all derive bit-identical alpha, beta and loop condition without a broadcast.
+// (cooperative launch) and meet at a grid barrier after each phase.  Phase 1 is the SpMV pipeline over
+// tiles of block rows that each CTA's producer takes from the iteration's queue (an atomic counter),
+// so SMs that stream faster take more tiles; phases 2 and 3 walk the vectors grid-stride (after a
+// barrier every CTA may read any row).  Every CTA sums all CTAs' partials in the same fixed order
+// (double-float), so all derive bit-identical alpha, beta and loop condition without a broadcast.
 // The producer warp streams the matrix tiles continuously across iterations (the matrix does not
 // change), so the copy ring does not drain at the barriers; those copies carry an L2 evict-first
 // policy so that the vectors of phases 2 and 3 stay in L2.  p is gathered with coherent (non-.nc)
 // loads since it changes between phases of the same launch.  Per iteration the arithmetic is that of
-// k_cg_spmv / k_cg_update / k_cg_pupdate; only the order of the partial sums differs.
+// k_cg_spmv / k_cg_update / k_cg_pupdate except for the sums: double-float instead of FP64, and
+// alpha, beta formed in fp32 (the three-kernel path rounds its FP64 quotients to fp32 before use).
 // Every wait is bounded: a barrier that does not complete within kWaitLimitNs sets
 // GB_DEV_WAIT_TIMEOUT and ends the CTA's loop.
 
@@ -336,8 +341,10 @@ __device__ __forceinline__ void st_release_u32(unsigned int* p, unsigned int v)
 // Grid barrier among the consumer threads of every CTA (thread 32 arrives for its CTA): the last
 // arrival resets the count and advances the generation; the others poll the generation.  Returns
 // the same value in every consumer thread of the CTA: false if the wait ran out or a warp of the CTA
-// flagged a failed wait beforehand (*s_fail).
-__device__ __forceinline__ bool cg_grid_barrier(KrylovScalars* S, volatile int* s_ok, volatile int* s_fail)
+// flagged a failed wait beforehand (*s_fail).  The last arrival also zeroes *reset_on_last, if given,
+// before it releases the others.
+__device__ __forceinline__ bool cg_grid_barrier(KrylovScalars* S, volatile int* s_ok, volatile int* s_fail,
+                                                unsigned int* reset_on_last = nullptr)
 {
     consumer_sync();
     if (threadIdx.x == 32) {
@@ -349,6 +356,7 @@ __device__ __forceinline__ bool cg_grid_barrier(KrylovScalars* S, volatile int* 
         int ok = 1;
         if (prev == gridDim.x - 1) {
             atomicExch(&S->bar_count, 0u);
+            if (reset_on_last) atomicExch(reset_on_last, 0u);
             st_release_u32(&S->bar_gen, g + 1u);
         } else {
             const uint64_t t0 = globaltimer_ns();
@@ -365,57 +373,88 @@ __device__ __forceinline__ bool cg_grid_barrier(KrylovScalars* S, volatile int* 
     return *s_ok != 0;
 }
 
-// Sum of NV per-thread values over the 512 consumer threads; the result is valid in thread 32.
-template <int NV> __device__ __forceinline__ void consumer_sum(const float (&v)[NV], double* s_red, double (&out)[NV])
+// Sums inside the persistent CG run in double-float (unevaluated hi + lo pairs of fp32, ~44 bits;
+// gb_df32.cuh): GB300's FP64 pipe is a small fraction of its FP32 rate and its latency sat on the
+// critical path between the grid barriers.  A butterfly of df32 adds leaves every lane with the same
+// value (two_sum is exact, so a + b and b + a agree bit for bit).
+__device__ __forceinline__ df32 warp_sum_df(df32 d)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const df32 other(__shfl_xor_sync(0xffffffffu, d.hi, o), __shfl_xor_sync(0xffffffffu, d.lo, o));
+        d = d + other;
+    }
+    return d;
+}
+
+__device__ __forceinline__ bool df_gt(const df32& a, const df32& b) { return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo); }
+
+__device__ __forceinline__ df32 df_from_double(double v)
+{
+    const float h = (float)v;
+    return df32(h, (float)(v - (double)h));
+}
+
+__device__ __forceinline__ double df_to_double(const df32& d) { return (double)d.hi + (double)d.lo; }
+
+// Sum of NV per-thread fp32 values over the 512 consumer threads (fp32 within a warp, double-float
+// across warps); the result is valid in thread 32.
+template <int NV> __device__ __forceinline__ void consumer_sum(const float (&v)[NV], float* s_red, df32 (&out)[NV])
 {
     const int cw = (threadIdx.x >> 5) - 1, lane = threadIdx.x & 31;
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-        const double w = (double)warp_sum(v[k]);
+        const float w = warp_sum(v[k]);
         if (lane == 0) s_red[cw * NV + k] = w;
     }
     consumer_sync();
     if (cw == 0) {
 #pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            const double w = lane < SPMV_CONSUMER_WARPS ? s_red[lane * NV + k] : 0.0;
-            out[k] = warp_sum(w);
-        }
+        for (int k = 0; k < NV; ++k)
+            out[k] = warp_sum_df(df32(lane < SPMV_CONSUMER_WARPS ? s_red[lane * NV + k] : 0.f, 0.f));
     }
 }
 
-// Sum of every CTA's partials part[k * gridDim.x + c] over the consumer threads (one or two loads
-// each, then warp sums and a sum of the 16 warp totals), in the same fixed order in every CTA;
+// Sum of every CTA's double-float partials part[k * gridDim.x + c] over the consumer threads (one or
+// two loads each, warp sums, then a sum of the 16 warp totals), in the same fixed order in every CTA;
 // thread 32 passes the totals to `update` (which changes the shared solver state), and the consumers
 // resynchronise so that all of them see the new state.
 template <int NV, typename Update>
-__device__ __forceinline__ void all_partials(const double* part, double* s_red, Update update)
+__device__ __forceinline__ void all_partials(const float2* part, float* s_red, Update update)
 {
     const int ct = threadIdx.x - 32, cw = ct >> 5, lane = threadIdx.x & 31;
-    double acc[NV];
-#pragma unroll
-    for (int k = 0; k < NV; ++k) acc[k] = 0.0;
+    df32 acc[NV];
     for (int c = ct; c < (int)gridDim.x; c += SPMV_CONSUMERS) {
 #pragma unroll
-        for (int k = 0; k < NV; ++k) acc[k] += __ldcg(part + (size_t)k * gridDim.x + c);
+        for (int k = 0; k < NV; ++k) {
+            const float2 v = __ldcg(part + (size_t)k * gridDim.x + c);
+            acc[k] += df32(v.x, v.y);
+        }
     }
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-        const double w = warp_sum(acc[k]);
-        if (lane == 0) s_red[cw * NV + k] = w;
+        const df32 w = warp_sum_df(acc[k]);
+        if (lane == 0) {
+            s_red[(cw * NV + k) * 2] = w.hi;
+            s_red[(cw * NV + k) * 2 + 1] = w.lo;
+        }
     }
     consumer_sync();
     if (cw == 0) {
-        double t[NV];
+        df32 t[NV];
 #pragma unroll
-        for (int k = 0; k < NV; ++k) t[k] = warp_sum(lane < SPMV_CONSUMER_WARPS ? s_red[lane * NV + k] : 0.0);
+        for (int k = 0; k < NV; ++k) {
+            const bool in = lane < SPMV_CONSUMER_WARPS;
+            t[k] = warp_sum_df(df32(in ? s_red[(lane * NV + k) * 2] : 0.f, in ? s_red[(lane * NV + k) * 2 + 1] : 0.f));
+        }
         if (lane == 0) update(t);
     }
     consumer_sync();
 }
 
 struct LoopState {
-    double rz, rr, rr_ref, atol_sq, pAp, alpha, beta;
+    df32 rz, rr, rr_ref, atol_sq, pAp;
+    float alpha, beta;
     int iter, cond, maxiter, breakdown;
 };
 
@@ -424,15 +463,15 @@ __global__ __launch_bounds__(SPMV_THREADS, 2) void k_cg_loop(const SolveArgs* __
                                                           int max_iters)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ double s_red[SPMV_CONSUMER_WARPS * 2];
-    __shared__ LoopState st;
-    __shared__ int s_ok, s_fail, s_stop;
+    __shared__ float s_red[SPMV_CONSUMER_WARPS * 2 * 2];
+    __shared__ __align__(16) unsigned char st_raw[sizeof(LoopState)];  // no constructor: thread 32 fills it
+    LoopState& st = *reinterpret_cast<LoopState*>(st_raw);
+    __shared__ int s_ok, s_fail, s_stop, s_citer, s_pdone;
     const SolveArgs a = *args;
     KrylovScalars* S = a.S;
     const SpmvRing R = spmv_ring<BR, BR, VT>(smem, sh);
     const int NS = sh.stages;
     const int ntiles = (nrow + sh.rows - 1) / sh.rows;
-    const int own = blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const VT* values = (const VT*)a.values;
 
@@ -444,32 +483,35 @@ __global__ __launch_bounds__(SPMV_THREADS, 2) void k_cg_loop(const SolveArgs* __
         fence_mbar_init();
         s_stop = 0;
         s_fail = 0;
+        s_citer = 0;
+        s_pdone = 0;
     }
     __syncthreads();
 
     if (warp == 0) {
         // ------------------ producer: tiles of successive iterations, until told to stop -----------
-        if (lane == 0 && own > 0) {
+        // Tiles are taken from the iteration's queue (an atomic counter), so CTAs that stream faster
+        // take more of them; each CTA's run of tiles for an iteration ends with a sentinel slot (no
+        // copy, header nr = -1).  The producer starts on iteration j once the consumers are in
+        // iteration j - 1: the queue of iteration j (parity j & 1) was zeroed at the phase-1 barrier
+        // of iteration j - 2, after every CTA's last take from it.
+        if (lane == 0) {
             const uint64_t policy = l2_policy_evict_first();
-            auto range = [&](int j, int& b0, int& b1) {
-                const int r0 = ((int)blockIdx.x + j * (int)gridDim.x) * sh.rows;
-                b0 = a.offsets[r0];
-                b1 = a.offsets[min(r0 + sh.rows, nrow)];
+            int t = 0, b0 = 0, b1 = 0;
+            auto take = [&](int j) {
+                t = (int)atomicAdd(&S->tile_ctr[j & 1], 1u);
+                if (t < ntiles) {
+                    const int r0 = t * sh.rows;
+                    b0 = a.offsets[r0];
+                    b1 = a.offsets[min(r0 + sh.rows, nrow)];
+                }
             };
-            int nb0, nb1;
-            range(0, nb0, nb1);
-            int issued = 0;
+            int i = 0;
             bool timed_out = false, stop = false;
-            for (int i = 0; !stop; ++i) {
-                const int j = i % own;
-                const int s = i % NS;
-                const uint32_t ph = (uint32_t)(i / NS) & 1u;
-                const int b0 = nb0, b1 = nb1;
-                range(j + 1 < own ? j + 1 : 0, nb0, nb1);
-                if (i >= NS) {
+            for (int j = 0; !stop; ++j) {
+                if (j >= 2) {  // gate: the consumers have entered iteration j - 1
                     const uint64_t t0 = globaltimer_ns();
-                    for (;;) {
-                        if (mbar_try_wait(&R.empty[s], ph ^ 1u)) break;
+                    while (*(volatile int*)&s_citer < j - 1) {
                         if (*(volatile int*)&s_stop) {
                             stop = true;
                             break;
@@ -478,19 +520,47 @@ __global__ __launch_bounds__(SPMV_THREADS, 2) void k_cg_loop(const SolveArgs* __
                             timed_out = stop = true;
                             break;
                         }
+                        __nanosleep(128);
                     }
                     if (stop) break;
-                } else if (*(volatile int*)&s_stop) {
-                    break;
                 }
-                spmv_issue<BR, BR, VT>(R, sh, nrow, s, (int)blockIdx.x + j * (int)gridDim.x, b0, b1, a.offsets,
-                                       a.columns, values, true, policy);
-                ++issued;
+                take(j);
+                for (;;) {
+                    const int s = i % NS;
+                    const uint32_t ph = (uint32_t)(i / NS) & 1u;
+                    if (i >= NS) {
+                        const uint64_t t0 = globaltimer_ns();
+                        for (;;) {
+                            if (mbar_try_wait(&R.empty[s], ph ^ 1u)) break;
+                            if (*(volatile int*)&s_stop) {
+                                stop = true;
+                                break;
+                            }
+                            if (globaltimer_ns() - t0 > kWaitLimitNs) {
+                                timed_out = stop = true;
+                                break;
+                            }
+                        }
+                    } else if (*(volatile int*)&s_stop) {
+                        stop = true;
+                    }
+                    if (stop) break;
+                    if (t >= ntiles) {  // sentinel: this CTA's tiles of iteration j are all issued
+                        R.hdr[s].nr = -1;
+                        mbar_arrive(&R.full[s]);
+                        ++i;
+                        break;
+                    }
+                    spmv_issue<BR, BR, VT>(R, sh, nrow, s, t, b0, b1, a.offsets, a.columns, values, true, policy);
+                    ++i;
+                    take(j);  // the next tile's take and offsets overlap the copies just issued
+                }
             }
             if (timed_out) atomicOr(&S->status, GB_DEV_WAIT_TIMEOUT);
             // drain: no bulk copy of this CTA may still be in flight when it exits
-            for (int q = max(0, issued - NS); q < issued; ++q)
-                mbar_wait_bounded(&R.full[q % NS], (uint32_t)(q / NS) & 1u);
+            for (int q = max(0, i - NS); q < i; ++q) mbar_wait_bounded(&R.full[q % NS], (uint32_t)(q / NS) & 1u);
+            __threadfence_block();
+            *(volatile int*)&s_pdone = 1;
         }
     } else {
         // ------------------ consumers: the three phases of every iteration ------------------------
@@ -498,13 +568,13 @@ __global__ __launch_bounds__(SPMV_THREADS, 2) void k_cg_loop(const SolveArgs* __
         // (identical in every CTA); CTA 0 writes them back to the device scalars at the end.
         const int ct = threadIdx.x - 32;
         if (threadIdx.x == 32) {
-            st.rz = S->rz;
-            st.rr = S->rr;
-            st.rr_ref = S->rr_ref;
-            st.atol_sq = S->atol_sq;
-            st.pAp = S->pAp;
-            st.alpha = S->alpha;
-            st.beta = S->beta;
+            st.rz = df_from_double(S->rz);
+            st.rr = df_from_double(S->rr);
+            st.rr_ref = df_from_double(S->rr_ref);
+            st.atol_sq = df_from_double(S->atol_sq);
+            st.pAp = df_from_double(S->pAp);
+            st.alpha = (float)S->alpha;
+            st.beta = (float)S->beta;
             st.iter = S->iter;
             st.cond = S->cond;
             st.maxiter = S->maxiter;
@@ -512,47 +582,55 @@ __global__ __launch_bounds__(SPMV_THREADS, 2) void k_cg_loop(const SolveArgs* __
         }
         consumer_sync();
         const bool lead = (blockIdx.x == 0 && threadIdx.x == 32);
-        double* partA = a.partials;              // [gridDim.x]: p.Ap
-        double* partB = a.partials + gridDim.x;  // [2][gridDim.x]: r.r, r.z
+        float2* partA = reinterpret_cast<float2*>(a.partials);  // [gridDim.x]: p.Ap (double-float)
+        float2* partB = partA + gridDim.x;                        // [2][gridDim.x]: r.r, r.z
         const bool vec4 = ((((uintptr_t)a.x | (uintptr_t)a.r | (uintptr_t)a.p | (uintptr_t)a.Ap |
                              (uintptr_t)(a.dinv ? a.dinv : a.r)) & 15) == 0);
         int i = 0, done = 0;
         bool ok = true;
         while (st.cond && (max_iters <= 0 || done < max_iters)) {
-            // (1) Ap = A p, p.Ap
+            if (threadIdx.x == 32) *(volatile int*)&s_citer = done;
+            // (1) Ap = A p, p.Ap over the tiles this CTA's producer took, up to its sentinel
             EpiCgAp<BR, float> epi{a.Ap, a.p};
-            for (int j = 0; j < own; ++j, ++i) {
+            for (;; ++i) {
                 const int s = i % NS;
                 const uint32_t ph = (uint32_t)(i / NS) & 1u;
                 const bool full_ok = __all_sync(0xffffffffu, mbar_wait_bounded(&R.full[s], ph));
-                if (full_ok) {
+                const bool tile = full_ok && R.hdr[s].nr >= 0;
+                if (tile) {
                     spmv_consume<BR, BR, VT, float, float, true>(R, sh, s, ct, a.row_counts, a.columns, values, a.p,
                                                                  epi);
-                } else if (lane == 0) {
+                } else if (!full_ok && lane == 0) {
                     *(volatile int*)&s_fail = 1;
                 }
                 __syncwarp();
                 if (lane == 0) mbar_arrive(&R.empty[s]);
+                if (!tile) {
+                    ++i;
+                    break;
+                }
             }
             {
                 const float v[1] = {epi.pAp};
-                double t[1];
+                df32 t[1];
                 consumer_sum<1>(v, s_red, t);
-                if (threadIdx.x == 32) partA[blockIdx.x] = t[0];
+                if (threadIdx.x == 32) partA[blockIdx.x] = make_float2(t[0].hi, t[0].lo);
             }
-            if (!cg_grid_barrier(S, &s_ok, &s_fail)) {
+            // every CTA's producer has made its last take for this iteration: its queue is zeroed for
+            // iteration done + 2
+            if (!cg_grid_barrier(S, &s_ok, &s_fail, &S->tile_ctr[done & 1])) {
                 ok = false;
                 break;
             }
-            all_partials<1>(partA, s_red, [&](const double (&t)[1]) {
+            all_partials<1>(partA, s_red, [&](const df32 (&t)[1]) {
                 st.pAp = t[0];
-                double alpha = 0.0;
-                if (st.rr > st.atol_sq) {
-                    alpha = st.rz / t[0];
-                    if (!finite(alpha)) {
+                float alpha = 0.f;
+                if (df_gt(st.rr, st.atol_sq)) {
+                    alpha = (st.rz.hi + st.rz.lo) / (t[0].hi + t[0].lo);
+                    if (!isfinite(alpha)) {
                         if (blockIdx.x == 0) atomicOr(&S->status, GB_DEV_BREAKDOWN);
                         st.breakdown = 1;
-                        alpha = 0.0;
+                        alpha = 0.f;
                     }
                 }
                 st.alpha = alpha;
@@ -561,7 +639,7 @@ __global__ __launch_bounds__(SPMV_THREADS, 2) void k_cg_loop(const SolveArgs* __
             // may read any row of Ap)
             float prr = 0.f, prz = 0.f;
             {
-                const float al = (float)st.alpha;
+                const float al = st.alpha;
                 int64_t e = 0;
                 if (vec4) {
                     const int64_t n4 = a.n >> 2;
@@ -596,39 +674,41 @@ __global__ __launch_bounds__(SPMV_THREADS, 2) void k_cg_loop(const SolveArgs* __
             }
             {
                 const float v[2] = {prr, prz};
-                double t[2];
+                df32 t[2];
                 consumer_sum<2>(v, s_red, t);
                 if (threadIdx.x == 32) {
-                    partB[blockIdx.x] = t[0];
-                    partB[gridDim.x + blockIdx.x] = t[1];
+                    partB[blockIdx.x] = make_float2(t[0].hi, t[0].lo);
+                    partB[gridDim.x + blockIdx.x] = make_float2(t[1].hi, t[1].lo);
                 }
             }
             if (!cg_grid_barrier(S, &s_ok, &s_fail)) {
                 ok = false;
                 break;
             }
-            all_partials<2>(partB, s_red, [&](const double (&t)[2]) {
-                const double rz_old = st.rz;
+            all_partials<2>(partB, s_red, [&](const df32 (&t)[2]) {
+                const float rz_old = st.rz.hi + st.rz.lo;
                 st.rr = t[0];
                 st.rz = t[1];
-                double beta = 0.0;
-                if (t[0] > st.atol_sq) {
-                    beta = t[1] / rz_old;
-                    if (!finite(beta)) {
+                float beta = 0.f;
+                const bool above = df_gt(t[0], st.atol_sq);
+                if (above) {
+                    beta = (t[1].hi + t[1].lo) / rz_old;
+                    if (!isfinite(beta)) {
                         if (blockIdx.x == 0) atomicOr(&S->status, GB_DEV_BREAKDOWN);
                         st.breakdown = 1;
-                        beta = 0.0;
+                        beta = 0.f;
                     }
                 }
                 st.beta = beta;
                 st.iter += 1;
-                int cond = (t[0] > st.atol_sq) && (st.iter < st.maxiter) && !st.breakdown;
-                if (!finite(t[0])) {
+                int cond = above && (st.iter < st.maxiter) && !st.breakdown;
+                if (!isfinite(t[0].hi)) {
                     if (blockIdx.x == 0) atomicOr(&S->status, GB_DEV_NONFINITE);
                     cond = 0;
                 }
                 if (a.stag_window > 0 && cond && (st.iter % a.stag_window) == 0) {
-                    if (st.iter > a.stag_window && t[0] > a.stag_factor * a.stag_factor * st.rr_ref) {
+                    const float f2 = (float)(a.stag_factor * a.stag_factor);
+                    if (st.iter > a.stag_window && t[0].hi > f2 * st.rr_ref.hi) {
                         if (blockIdx.x == 0) atomicOr(&S->status, GB_DEV_STAGNATION);
                         cond = 0;
                     }
@@ -640,7 +720,7 @@ __global__ __launch_bounds__(SPMV_THREADS, 2) void k_cg_loop(const SolveArgs* __
             if (!st.cond) break;
             // (3) p = D^-1 r + beta p (grid-stride)
             {
-                const float be = (float)st.beta;
+                const float be = st.beta;
                 int64_t e = 0;
                 if (vec4) {
                     const int64_t n4 = a.n >> 2;
@@ -675,17 +755,33 @@ __global__ __launch_bounds__(SPMV_THREADS, 2) void k_cg_loop(const SolveArgs* __
             st.cond = 0;
         }
         if (lead) {
-            S->rr = st.rr;
-            S->rz = st.rz;
-            S->rr_ref = st.rr_ref;
-            S->pAp = st.pAp;
+            S->rr = df_to_double(st.rr);
+            S->rz = df_to_double(st.rz);
+            S->rr_ref = df_to_double(st.rr_ref);
+            S->pAp = df_to_double(st.pAp);
             S->alpha = st.alpha;
             S->beta = st.beta;
             S->iter = st.iter;
             S->cond = ok ? st.cond : 0;
         }
         consumer_sync();
-        if (threadIdx.x == 32) *(volatile int*)&s_stop = 1;
+        // stop the producer; once every CTA's producer has stopped taking tiles, CTA 0 zeroes both
+        // queues for the next launch
+        if (threadIdx.x == 32) {
+            *(volatile int*)&s_stop = 1;
+            const uint64_t t0 = globaltimer_ns();
+            while (!*(volatile int*)&s_pdone) {
+                if (globaltimer_ns() - t0 > kWaitLimitNs) {
+                    atomicOr(&S->status, GB_DEV_WAIT_TIMEOUT);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        if (cg_grid_barrier(S, &s_ok, &s_fail) && lead) {
+            S->tile_ctr[0] = 0u;
+            S->tile_ctr[1] = 0u;
+        }
     }
     __syncthreads();
 }
@@ -982,6 +1078,7 @@ __global__ void k_store_args(SolveArgs* dst, SolveArgs src, int reset_status)
         src.S->status = 0;
         for (int k = 0; k < 8; ++k) src.S->counters[k] = 0u;
         src.S->bar_count = 0u;
+        src.S->tile_ctr[0] = src.S->tile_ctr[1] = 0u;
         src.S->cond = 1;
     }
 }
