@@ -582,6 +582,11 @@ __global__ __launch_bounds__(SPMV_THREADS, 2) void k_cg_loop(const SolveArgs* __
         }
         consumer_sync();
         const bool lead = (blockIdx.x == 0 && threadIdx.x == 32);
+        constexpr int BB = BR * BR;
+        const int G = sh.G;
+        const int lane_g = ct & (G - 1);
+        const int grp = ct / G;
+        const int ngroups = SPMV_CONSUMERS / G;
         float2* partA = reinterpret_cast<float2*>(a.partials);  // [gridDim.x]: p.Ap (double-float)
         float2* partB = partA + gridDim.x;                        // [2][gridDim.x]: r.r, r.z
         const bool vec4 = ((((uintptr_t)a.x | (uintptr_t)a.r | (uintptr_t)a.p | (uintptr_t)a.Ap |
@@ -598,8 +603,57 @@ __global__ __launch_bounds__(SPMV_THREADS, 2) void k_cg_loop(const SolveArgs* __
                 const bool full_ok = __all_sync(0xffffffffu, mbar_wait_bounded(&R.full[s], ph));
                 const bool tile = full_ok && R.hdr[s].nr >= 0;
                 if (tile) {
-                    spmv_consume<BR, BR, VT, float, float, true>(R, sh, s, ct, a.row_counts, a.columns, values, a.p,
-                                                                 epi);
+                    // the rows of the staged tile (the loop of spmv_run, with coherent gathers of p)
+                    const StageHeader h = R.hdr[s];
+                    const unsigned char* stg = R.ring + (size_t)s * R.stage_bytes;
+                    const int* s_off = reinterpret_cast<const int*>(stg);
+                    const int* cbase = h.staged ? reinterpret_cast<const int*>(stg + R.off_bytes) - h.a0 : a.columns;
+                    const VT* vbase = h.staged ? reinterpret_cast<const VT*>(stg + R.off_bytes + R.col_bytes) -
+                                                     (size_t)h.a0 * BB
+                                               : values;
+                    for (int kb = 0; kb < h.nr; kb += ngroups) {
+                        const int k = kb + grp;
+                        const bool active = k < h.nr;
+                        int beg = 0, end = 0;
+                        if (active) {
+                            beg = s_off[k];
+                            end = a.row_counts ? beg + a.row_counts[h.r0 + k] : s_off[k + 1];
+                        }
+                        float acc[BR];
+#pragma unroll
+                        for (int q = 0; q < BR; ++q) acc[q] = 0.f;
+                        constexpr int U = (BB == 1) ? 8 : 4;
+                        for (int base = beg + lane_g; base < end; base += U * G) {
+                            int cc[U];
+#pragma unroll
+                            for (int u = 0; u < U; ++u) {
+                                const int bi = base + u * G;
+                                cc[u] = (bi < end) ? cbase[bi] : -1;
+                            }
+                            float xv[U][BR];
+#pragma unroll
+                            for (int u = 0; u < U; ++u) {
+#pragma unroll
+                                for (int jj = 0; jj < BR; ++jj)
+                                    xv[u][jj] = (cc[u] >= 0) ? __ldca(a.p + (size_t)cc[u] * BR + jj) : 0.f;
+                            }
+#pragma unroll
+                            for (int u = 0; u < U; ++u) {
+                                const int bi = base + u * G;
+                                if (cc[u] >= 0) {
+                                    const VT* vv = vbase + (size_t)bi * BB;
+#pragma unroll
+                                    for (int q = 0; q < BR; ++q) {
+#pragma unroll
+                                        for (int jj = 0; jj < BR; ++jj) acc[q] += cvt<float>(vv[q * BR + jj]) * xv[u][jj];
+                                    }
+                                }
+                            }
+                        }
+#pragma unroll
+                        for (int q = 0; q < BR; ++q) acc[q] = group_reduce(acc[q], G);
+                        if (active) epi(h.r0 + k, acc, lane_g);
+                    }
                 } else if (!full_ok && lane == 0) {
                     *(volatile int*)&s_fail = 1;
                 }

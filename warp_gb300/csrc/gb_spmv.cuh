@@ -174,78 +174,6 @@ __device__ __forceinline__ void spmv_issue(const SpmvRing& R, const SpmvShape& s
     }
 }
 
-// Consumer threads (ct = 0 .. SPMV_CONSUMERS-1): the rows of the tile staged in slot s.  COHERENT
-// gathers x with plain L1-cached loads instead of the read-only path, for kernels in which x changes
-// between passes of the same launch (ordered by a grid barrier).
-template <int BR, int BC, typename VT, typename XT, typename AT, bool COHERENT, typename Epi>
-__device__ __forceinline__ void spmv_consume(const SpmvRing& R, const SpmvShape& sh, int s, int ct,
-                                             const int* __restrict__ row_counts, const int* __restrict__ columns,
-                                             const VT* __restrict__ values, const XT* x, Epi& epi)
-{
-    constexpr int BB = BR * BC;
-    const StageHeader h = R.hdr[s];
-    const unsigned char* st = R.ring + (size_t)s * R.stage_bytes;
-    const int* s_off = reinterpret_cast<const int*>(st);
-    const int* cbase = h.staged ? reinterpret_cast<const int*>(st + R.off_bytes) - h.a0 : columns;
-    const VT* vbase = h.staged ? reinterpret_cast<const VT*>(st + R.off_bytes + R.col_bytes) - (size_t)h.a0 * BB
-                               : values;
-    const int G = sh.G;
-    const int lane_g = ct & (G - 1);
-    const int g = ct / G;
-    const int ngroups = SPMV_CONSUMERS / G;
-    // warp-uniform trip count: rows past the tile end are inactive lanes, so the full-mask shuffles
-    // below never wait on an exited lane
-    for (int kb = 0; kb < h.nr; kb += ngroups) {
-        const int k = kb + g;
-        const bool active = k < h.nr;
-        int beg = 0, end = 0;
-        if (active) {
-            beg = s_off[k];
-            end = row_counts ? beg + row_counts[h.r0 + k] : s_off[k + 1];
-        }
-        AT acc[BR];
-#pragma unroll
-        for (int q = 0; q < BR; ++q) acc[q] = AT(0);
-        // U blocks per lane per batch, predicated: all U gathers are issued before any is consumed,
-        // so each lane keeps U * BC loads in flight
-        constexpr int U = (BB == 1) ? 8 : 4;
-        for (int base = beg + lane_g; base < end; base += U * G) {
-            int cc[U];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int bi = base + u * G;
-                cc[u] = (bi < end) ? cbase[bi] : -1;
-            }
-            AT xv[U][BC];
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-#pragma unroll
-                for (int j = 0; j < BC; ++j) {
-                    if constexpr (COHERENT)
-                        xv[u][j] = (cc[u] >= 0) ? (AT)__ldca(x + (size_t)cc[u] * BC + j) : AT(0);
-                    else
-                        xv[u][j] = (cc[u] >= 0) ? ldx<AT>(x + (size_t)cc[u] * BC + j) : AT(0);
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < U; ++u) {
-                const int bi = base + u * G;
-                if (cc[u] >= 0) {
-                    const VT* vv = vbase + (size_t)bi * BB;
-#pragma unroll
-                    for (int q = 0; q < BR; ++q) {
-#pragma unroll
-                        for (int j = 0; j < BC; ++j) acc[q] += cvt<AT>(vv[q * BC + j]) * xv[u][j];
-                    }
-                }
-            }
-        }
-#pragma unroll
-        for (int q = 0; q < BR; ++q) acc[q] = group_reduce(acc[q], G);
-        if (active) epi(h.r0 + k, acc, lane_g);
-    }
-}
-
 // Computes acc[BR] = (A x)[row] for every block row of every tile this CTA owns and calls
 // epi(row, acc, lane_in_group) on the consumer lanes of the row's group (all lanes of the group
 // hold the sums).  Must be called by all SPMV_THREADS threads; returns with the CTA converged
@@ -256,15 +184,22 @@ __device__ __forceinline__ void spmv_run(int nrow, const SpmvShape sh, const int
                                          const VT* __restrict__ values, const XT* __restrict__ x, unsigned char* smem,
                                          int* status, Epi& epi)
 {
-    const SpmvRing R = spmv_ring<BR, BC, VT>(smem, sh);
+    constexpr int BB = BR * BC;
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem);
+    uint64_t* empty = full + SPMV_MAX_STAGES;
+    StageHeader* hdr = reinterpret_cast<StageHeader*>(smem + 64);
+    const size_t off_bytes = align16((size_t)(sh.rows + 8) * sizeof(int));
+    const size_t col_bytes = align16((size_t)sh.cap * sizeof(int));
+    const size_t stage_bytes = spmv_stage_bytes<BR, BC, VT>(sh.rows, sh.cap);
+    unsigned char* ring = smem + 192;
     const int S = sh.stages;
     const int ntiles = (nrow + sh.rows - 1) / sh.rows;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < S; ++s) {
-            mbar_init(&R.full[s], 1);
-            mbar_init(&R.empty[s], SPMV_CONSUMER_WARPS);
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], SPMV_CONSUMER_WARPS);
         }
         fence_mbar_init();
     }
@@ -280,11 +215,14 @@ __device__ __forceinline__ void spmv_run(int nrow, const SpmvShape sh, const int
                 nb0 = offsets[r0];
                 nb1 = offsets[min(r0 + sh.rows, nrow)];
             }
+            const int64_t ncap8 = sh.ncap & ~(int64_t)(SPMV_ALIGN - 1);
             bool timed_out = false;
             int issued = 0;
             for (int i = 0; tile < ntiles; ++i, tile += gridDim.x) {
                 const int s = i % S;
                 const uint32_t ph = (uint32_t)(i / S) & 1u;
+                const int r0 = tile * sh.rows;
+                const int nr = min(sh.rows, nrow - r0);
                 const int b0 = nb0, b1 = nb1;
                 // prefetch the next tile's range while this one is being issued / consumed
                 const int ntile = tile + gridDim.x;
@@ -293,33 +231,121 @@ __device__ __forceinline__ void spmv_run(int nrow, const SpmvShape sh, const int
                     nb0 = offsets[nr0];
                     nb1 = offsets[min(nr0 + sh.rows, nrow)];
                 }
-                if (i >= S && !mbar_wait_bounded(&R.empty[s], ph ^ 1u)) {
+                if (i >= S && !mbar_wait_bounded(&empty[s], ph ^ 1u)) {
                     timed_out = true;
                     break;
                 }
-                spmv_issue<BR, BC, VT>(R, sh, nrow, s, tile, b0, b1, offsets, columns, values, false, 0ull);
+                unsigned char* st = ring + (size_t)s * stage_bytes;
+                int* s_off = reinterpret_cast<int*>(st);
+                int* s_cols = reinterpret_cast<int*>(st + off_bytes);
+                VT* s_vals = reinterpret_cast<VT*>(st + off_bytes + col_bytes);
+                const int a0 = b0 & ~(SPMV_ALIGN - 1);
+                const bool staged = (sh.cap > 0) && (b1 - a0 <= sh.cap);
+                // offsets slice [r0, r0 + nr]: bulk part (multiple of 4 entries inside the array)
+                int n_off = sh.off_bulk ? min((nr + 1 + 3) & ~3, (nrow + 1 - r0) & ~3) : 0;
+                n_off = max(n_off, 0);
+                for (int k = n_off; k <= nr; ++k) s_off[k] = offsets[r0 + k];
+                uint32_t bytes = (uint32_t)n_off * 4u;
+                int a1 = a0, nb = 0;
+                if (staged) {
+                    a1 = (int)min((int64_t)((b1 + SPMV_ALIGN - 1) & ~(SPMV_ALIGN - 1)), ncap8);
+                    a1 = max(a1, a0);
+                    nb = a1 - a0;
+                    for (int b = a1; b < b1; ++b) {
+                        s_cols[b - a0] = columns[b];
+#pragma unroll
+                        for (int q = 0; q < BB; ++q) s_vals[(size_t)(b - a0) * BB + q] = values[(size_t)b * BB + q];
+                    }
+                    bytes += (uint32_t)nb * (uint32_t)(sizeof(int) + BB * sizeof(VT));
+                }
+                StageHeader& h = hdr[s];
+                h.r0 = r0;
+                h.nr = nr;
+                h.a0 = a0;
+                h.staged = staged ? 1 : 0;
+                mbar_arrive_expect_tx(&full[s], bytes);
+                if (n_off > 0) bulk_g2s(s_off, offsets + r0, (uint32_t)n_off * 4u, &full[s]);
+                if (nb > 0) {
+                    bulk_g2s(s_cols, columns + a0, (uint32_t)nb * 4u, &full[s]);
+                    bulk_g2s(s_vals, values + (size_t)a0 * BB, (uint32_t)nb * (uint32_t)(BB * sizeof(VT)), &full[s]);
+                }
                 ++issued;
             }
             if (timed_out && status) atomicOr(status, GB_DEV_WAIT_TIMEOUT);
             // drain: no bulk copy of this CTA may still be in flight when it moves on
             for (int j = max(0, issued - S); j < issued; ++j)
-                mbar_wait_bounded(&R.full[j % S], (uint32_t)(j / S) & 1u);
+                mbar_wait_bounded(&full[j % S], (uint32_t)(j / S) & 1u);
         }
     } else {
         // ------------------------------- consumers -----------------------------------------
         const int ct = threadIdx.x - 32;
+        const int G = sh.G;
+        const int lane_g = ct & (G - 1);
+        const int g = ct / G;
+        const int ngroups = SPMV_CONSUMERS / G;
         int i = 0;
         for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
             const int s = i % S;
             const uint32_t ph = (uint32_t)(i / S) & 1u;
-            const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&R.full[s], ph));
+            const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&full[s], ph));
             if (ok) {
-                spmv_consume<BR, BC, VT, XT, AT, false>(R, sh, s, ct, row_counts, columns, values, x, epi);
+                const StageHeader h = hdr[s];
+                unsigned char* st = ring + (size_t)s * stage_bytes;
+                const int* s_off = reinterpret_cast<const int*>(st);
+                const int* cbase = h.staged ? reinterpret_cast<const int*>(st + off_bytes) - h.a0 : columns;
+                const VT* vbase = h.staged ? reinterpret_cast<const VT*>(st + off_bytes + col_bytes) - (size_t)h.a0 * BB
+                                           : values;
+                // warp-uniform trip count: rows past the tile end are inactive lanes, so the
+                // full-mask shuffles below never wait on an exited lane
+                for (int kb = 0; kb < h.nr; kb += ngroups) {
+                    const int k = kb + g;
+                    const bool active = k < h.nr;
+                    int beg = 0, end = 0;
+                    if (active) {
+                        beg = s_off[k];
+                        end = row_counts ? beg + row_counts[h.r0 + k] : s_off[k + 1];
+                    }
+                    AT acc[BR];
+#pragma unroll
+                    for (int q = 0; q < BR; ++q) acc[q] = AT(0);
+                    // U blocks per lane per batch, predicated: all U gathers are issued before
+                    // any is consumed, so each lane keeps U * BC loads in flight
+                    constexpr int U = (BB == 1) ? 8 : 4;
+                    for (int base = beg + lane_g; base < end; base += U * G) {
+                        int cc[U];
+#pragma unroll
+                        for (int u = 0; u < U; ++u) {
+                            const int bi = base + u * G;
+                            cc[u] = (bi < end) ? cbase[bi] : -1;
+                        }
+                        AT xv[U][BC];
+#pragma unroll
+                        for (int u = 0; u < U; ++u) {
+#pragma unroll
+                            for (int j = 0; j < BC; ++j) xv[u][j] = (cc[u] >= 0) ? ldx<AT>(x + (size_t)cc[u] * BC + j) : AT(0);
+                        }
+#pragma unroll
+                        for (int u = 0; u < U; ++u) {
+                            const int bi = base + u * G;
+                            if (cc[u] >= 0) {
+                                const VT* vv = vbase + (size_t)bi * BB;
+#pragma unroll
+                                for (int q = 0; q < BR; ++q) {
+#pragma unroll
+                                    for (int j = 0; j < BC; ++j) acc[q] += cvt<AT>(vv[q * BC + j]) * xv[u][j];
+                                }
+                            }
+                        }
+                    }
+#pragma unroll
+                    for (int q = 0; q < BR; ++q) acc[q] = group_reduce(acc[q], G);
+                    if (active) epi(h.r0 + k, acc, lane_g);
+                }
             } else if (lane == 0 && status) {
                 atomicOr(status, GB_DEV_WAIT_TIMEOUT);
             }
             __syncwarp();
-            if (lane == 0) mbar_arrive(&R.empty[s]);
+            if (lane == 0) mbar_arrive(&empty[s]);
         }
     }
     __syncthreads();
