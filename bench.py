@@ -38,6 +38,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "Solve time to 1e-8 rel. residual: learned-FCG vs Jacobi-CG; bsr_mv HBM GB/s"
+# scalar type of the fine level's stencil coefficients inside the V-cycle (the flexible solver's own
+# product and the FP64 refinement keep fp32 values); resolved to a torch dtype where torch is imported
+VCYCLE_FINE = "bf16"
 WORKLOAD = ("96^3 Q1 lognormal diffusion (GRF l=0.1, sigma=1.5), 912,673 dofs, 24.1M nnz; "
             "learned-preconditioned FCG (multigrid V-cycle + trained conv-net smoother) FP32 inner + FP64 "
             "refinement to 1e-8 FP64 relative residual")
@@ -50,6 +53,12 @@ def _peaks():
         return float(d["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
+
+
+def _fine_values():
+    import torch
+
+    return torch.bfloat16 if VCYCLE_FINE == "bf16" else torch.float32
 
 
 def _tensor_peak():
@@ -612,7 +621,7 @@ def run_profile(args):
         from warp_gb300 import learned, multigrid
 
         net = learned.ConvNet.load(args.weights)
-        mg = multigrid.MultigridPreconditioner(A, system.geo, system.coef)
+        mg = multigrid.MultigridPreconditioner(A, system.geo, system.coef, fine_values=_fine_values())
         mg.smoother = learned.LearnedSmoother(net, mg, system.coef, backend="tc")
         # eager launches (host check per iteration) so that every kernel of the solve is listed
         solver = linear.RefinedSolver(A, M=mg, method="fcg", inner_tol=args.inner_tol, use_cuda_graph=False)
@@ -720,7 +729,7 @@ def main():
         torch.cuda.synchronize()
         s0 = time.perf_counter()
         net = learned.ConvNet.load(args.weights)
-        lmg = multigrid.MultigridPreconditioner(A, system.geo, system.coef)
+        lmg = multigrid.MultigridPreconditioner(A, system.geo, system.coef, fine_values=_fine_values())
         lmg.smoother = learned.LearnedSmoother(net, lmg, system.coef, backend="tc")
         lsolver = linear.RefinedSolver(A, M=lmg, method="fcg", inner_tol=args.inner_tol)
         torch.cuda.synchronize()
@@ -739,11 +748,18 @@ def main():
     # ---- the same flexible CG without the network (Jacobi-smoothed V-cycle) -------------------
     torch.cuda.synchronize()
     s0 = time.perf_counter()
-    mg = multigrid.MultigridPreconditioner(A, system.geo, system.coef)
+    mg = multigrid.MultigridPreconditioner(A, system.geo, system.coef, fine_values=_fine_values())
     fsolver = linear.RefinedSolver(A, M=mg, method="fcg", inner_tol=args.inner_tol)
     torch.cuda.synchronize()
     mg_setup_ms = (time.perf_counter() - s0) * 1e3
     fcg_ms, finfos, _, _ = timed(fsolver, system.b, args.steps)
+
+    # ---- the learned solve with fp32 fine-level coefficients in the V-cycle, for comparison -----
+    l32 = multigrid.MultigridPreconditioner(A, system.geo, system.coef)
+    l32.smoother = learned.LearnedSmoother(net, l32, system.coef, backend="tc")
+    l32solver = linear.RefinedSolver(A, M=l32, method="fcg", inner_tol=args.inner_tol)
+    l32ms, l32infos, _, _ = timed(l32solver, system.b, max(3, args.steps // 4))
+    del l32solver, l32
 
     # ---- the learned smoother's layers (tensor-core roofline) ----------------------------------
     sm = lmg.smoother
@@ -940,7 +956,7 @@ def main():
         "config": {"workload": WORKLOAD, "solver": "learned_fcg_refined", "n_dofs": n, "nnz": nnz,
                    "parallelism": f"replicas{ws}", "l2": "inputs > L2 (matrix 204 MB vs 129 MB L2), no flush",
                    "inner_tol": args.inner_tol, "weights": os.path.relpath(args.weights, ROOT),
-                   "mg_levels": lmg.describe()},
+                   "mg_levels": lmg.describe(), "vcycle_fine_values": VCYCLE_FINE},
         "roofline": {"bound": "hbm", "kernel": "k_bsr_mv<1,1,float>", "achieved": mv_gbs, "peak": hbm_peak,
                      "unit": "GB/s", "frac": mv_gbs / hbm_peak, "peak_kind": peak_kind,
                      "algorithmic_bytes": mv_bytes, "traffic": traffic, "launch_us": mv_s * 1e6,
@@ -961,7 +977,10 @@ def main():
         "learned_fcg": {"ms": ms, "inner_iterations": statistics.median(inner_iters),
                         "outer_iterations": statistics.median(outer),
                         "rel_residual": max(i["rel_residual"] for i in linfos), "fallbacks": lsolver.fallbacks,
-                        "setup_ms": setup_ms, "speedup_vs_jacobi_cg": jms / ms, **oracle_check(lsolver.last_x)},
+                        "setup_ms": setup_ms, "speedup_vs_jacobi_cg": jms / ms, "vcycle_fine_values": VCYCLE_FINE,
+                        "fp32_vcycle_ms": l32ms,
+                        "fp32_vcycle_inner_iterations": statistics.median([i["inner_iterations"] for i in l32infos]),
+                        **oracle_check(lsolver.last_x)},
         "jacobi_cg": {"ms": jms, "inner_iterations": statistics.median([i["inner_iterations"] for i in jinfos]),
                       "outer_iterations": statistics.median([i["outer"] for i in jinfos]),
                       "rel_residual": max(i["rel_residual"] for i in jinfos), "clocks": jclocks,
@@ -975,7 +994,7 @@ def main():
                       **oracle_check(jsolver.last_x)},
         "mg_fcg_no_net": {"ms": fcg_ms, "inner_iterations": statistics.median([f["inner_iterations"] for f in finfos]),
                           "rel_residual": max(f["rel_residual"] for f in finfos), "fallbacks": fsolver.fallbacks,
-                          "setup_ms": mg_setup_ms, **oracle_check(fsolver.last_x)},
+                          "setup_ms": mg_setup_ms, "vcycle_fine_values": VCYCLE_FINE, **oracle_check(fsolver.last_x)},
         "conv_net": {"smoother_us": smoother_us, "launches": sm.kernels_per_apply, "useful_tflops": net_tflops,
                      "backend": "tcgen05 kind::f16 bf16 x bf16 -> fp32"},
         "bsr_mv_gbs": mv_gbs,

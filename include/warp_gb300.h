@@ -232,6 +232,12 @@ int gb_st27_build(int nx, int ny, int nz, const int* offsets, const int* columns
                   int* status, gb_stream_t stream);
 int gb_st27_apply(int mode, int nx, int ny, int nz, const float* S, const float* w, const float* r, const float* dinv,
                   float omega, float* w_out, float* out, int* status, gb_stream_t stream);
+/* bf16 copy of S (28 values per node, the last zero; gb_st27_bytes_bf16, 16-byte aligned) and the same
+ * three passes reading it, with fp32 accumulation. */
+size_t gb_st27_bytes_bf16(int nx, int ny, int nz);
+int gb_st27_to_bf16(int nx, int ny, int nz, const float* S, void* Sb, gb_stream_t stream);
+int gb_st27_apply_bf16(int mode, int nx, int ny, int nz, const void* Sb, const float* w, const float* r,
+                       const float* dinv, float omega, float* w_out, float* out, int* status, gb_stream_t stream);
 /* 3x3x3 convolutions on a node grid, channels-last activations act[v][C], v = (x*ny + y)*nz + z,
  * weights W[t][ci][co] (t = 9(dx+1) + 3(dy+1) + (dz+1)), zero padding.  fp32 training kernels
  * (gb_conv3_bwd_weight_f32 accumulates into gW, deterministic), Adam, features and the combine step

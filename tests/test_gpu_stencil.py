@@ -148,3 +148,86 @@ def test_vcycle_and_fcg_stencil_match_csr(cuda, learned_smoother):
         assert res <= atol
         its[st] = it
     assert abs(its[True] - its[False]) <= 1, its
+
+
+def _bf16_round(a):
+    """Round-to-nearest-even to bf16, returned as float64 (the coefficients the bf16 kernels read)."""
+    return torch.from_numpy(np.asarray(a, np.float32)).to(torch.bfloat16).to(torch.float64).numpy()
+
+
+@pytest.mark.parametrize("cells", [(6, 5, 4), (9, 7, 12), (1, 3, 2)])
+def test_st27_bf16_modes_match_rounded_product(cuda, cells):
+    """The bf16 coefficient copy: every mode against a float64 product with the bf16-rounded CSR values
+    (accumulation in fp32, so within fp32 summation error)."""
+    from warp_gb300 import _native as N
+
+    s = _system(cells, seed=5)
+    dims = tuple(c + 1 for c in cells)
+    n, off, col, val = _csr(s.A)
+    L = N.lib()
+    S = torch.empty(int(L.gb_st27_bytes(*dims)) // 4, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    N.check(L.gb_st27_build(*dims, s.A.offsets.data_ptr(), s.A.columns.data_ptr(), s.A.values.data_ptr(),
+                            S.data_ptr(), status.data_ptr(), 0))
+    Sb = torch.empty(int(L.gb_st27_bytes_bf16(*dims)) // 2, dtype=torch.bfloat16, device="cuda")
+    assert Sb.numel() % 8 == 0
+    N.check(L.gb_st27_to_bf16(*dims, S.data_ptr(), Sb.data_ptr(), 0))
+    torch.cuda.synchronize()
+    # layout: 28 values per node, the 27 taps of S rounded to bf16 and one zero
+    Sh = S.cpu().numpy()[: n * 27].reshape(n, 27)
+    Sbh = Sb.float().cpu().numpy()[: n * 28].reshape(n, 28)
+    np.testing.assert_array_equal(Sbh[:, :27], _bf16_round(Sh).astype(np.float32))
+    assert not Sbh[:, 27].any()
+    valb = _bf16_round(val)
+    rng = np.random.default_rng(4)
+    r = rng.standard_normal(n).astype(np.float32)
+    w = rng.standard_normal(n).astype(np.float32)
+    d = np.zeros(n)
+    rows = np.repeat(np.arange(n), np.diff(off))
+    d[rows[col == rows]] = val[col == rows]
+    dinv = (1.0 / d).astype(np.float32)
+    omega = 0.6
+    rt, wt, dt = (torch.from_numpy(a).cuda() for a in (r, w, dinv))
+    out = torch.empty_like(rt)
+    w_out = torch.empty_like(rt)
+    scale = np.abs(val).max() * np.abs(w).max() * 27
+    st = status.data_ptr()
+    N.check(L.gb_st27_apply_bf16(0, *dims, Sb.data_ptr(), wt.data_ptr(), rt.data_ptr(), None, omega, None,
+                                 out.data_ptr(), st, 0))
+    ref = r - _matvec(off, col, valb, w.astype(np.float64))
+    np.testing.assert_allclose(out.cpu().numpy(), ref, atol=1e-5 * scale, rtol=1e-5)
+    N.check(L.gb_st27_apply_bf16(1, *dims, Sb.data_ptr(), None, rt.data_ptr(), dt.data_ptr(), omega,
+                                 w_out.data_ptr(), out.data_ptr(), st, 0))
+    w1 = omega * dinv.astype(np.float64) * r
+    np.testing.assert_allclose(w_out.cpu().numpy(), w1, rtol=1e-6, atol=1e-7)
+    np.testing.assert_allclose(out.cpu().numpy(), r - _matvec(off, col, valb, w1), atol=1e-5 * scale, rtol=1e-5)
+    N.check(L.gb_st27_apply_bf16(2, *dims, Sb.data_ptr(), wt.data_ptr(), rt.data_ptr(), dt.data_ptr(), omega, None,
+                                 out.data_ptr(), st, 0))
+    ref = w + omega * dinv * (r - _matvec(off, col, valb, w.astype(np.float64)))
+    np.testing.assert_allclose(out.cpu().numpy(), ref, atol=1e-5 * scale * np.abs(dinv).max(), rtol=1e-5)
+    assert int(status.item()) == 0
+
+
+@pytest.mark.parametrize("learned_smoother", [False, True])
+def test_bf16_fine_stencil_fcg_converges(cuda, learned_smoother):
+    """Flexible CG with the bf16 fine-level stencil in the V-cycle reaches the same tolerance in at most
+    one more iteration than with fp32 coefficients (the cycle is only an approximate inverse)."""
+    import os
+
+    from warp_gb300 import learned, multigrid
+    from warp_gb300.optim import linear
+
+    s = _system((24, 24, 24), seed=11)
+    its = {}
+    for fv in (torch.float32, torch.bfloat16):
+        mg = multigrid.MultigridPreconditioner(s.A, s.geo, s.coef, fine_values=fv)
+        assert (mg.levels[0].Sb is not None) == (fv == torch.bfloat16)
+        if learned_smoother:
+            w = os.path.join(os.path.dirname(__file__), "..", "warp_gb300", "data", "smoother_q1_diffusion.npz")
+            mg.smoother = learned.LearnedSmoother(learned.ConvNet.load(w), mg, s.coef)
+        x = torch.zeros_like(s.b)
+        it, res, atol = linear.fcg(s.A, s.b, x, tol=1e-7, atol=0.0, maxiter=300, M=mg, check_every=1)
+        assert res <= atol
+        assert int(mg.status.item()) == 0
+        its[fv] = it
+    assert its[torch.bfloat16] <= its[torch.float32] + 1, its

@@ -18,7 +18,12 @@
 // (16 warps) was latency-bound at 31 us, and a planar S[k][i] layout read with 27 plain loads per
 // thread ran 1.5-2x slower than the CSR kernel (27 concurrent streams per warp).
 //
+// A bf16 copy of S (28 values per node: the 27 taps and one zero, 56 bytes, read as 7 eight-byte words)
+// halves the coefficient stream for the fine level of a V-cycle that only has to be an approximate
+// inverse; products still accumulate in fp32.
+//
 // Kernels:
+//   gb_st27_to_bf16  S -> bf16 copy (gb_st27_bytes_bf16)
 //   gb_st27_build  CSR (1x1 fp32, compact) -> S; an entry outside the 27-neighbourhood sets
 //                  status bit 1 (the caller keeps the CSR form then)
 //   gb_st27_apply  mode 0: t = r - A w
@@ -80,31 +85,66 @@ __global__ void k_st27_build(St27Grid g, const int* __restrict__ offsets, const 
 }
 
 constexpr int ST_TILE = 256;    // nodes per tile = threads per CTA
-constexpr int ST_STAGES = 2;     // 2 stages x 27.6 KB: four CTAs (32 warps) per SM
-constexpr int ST_CTAS_PER_SM = 4;
-constexpr size_t ST_STAGE_BYTES = (size_t)ST_TILE * 27 * sizeof(float);
-constexpr size_t ST_SMEM = ST_STAGES * ST_STAGE_BYTES + 64;
+constexpr int ST_STAGES = 2;     // 2 stages x 27.6 KB (fp32) / 14.3 KB (bf16)
+constexpr int ST_BF16_STRIDE = 28;  // bf16 coefficients per node (27 taps + 1 zero)
+
+template <typename CT> struct St27Coef;
+template <> struct St27Coef<float> {
+    static constexpr int stride = 27;
+    static constexpr int ctas_per_sm = 4;  // 2 x 27.6 KB each: 32 warps per SM
+};
+template <> struct St27Coef<__nv_bfloat16> {
+    static constexpr int stride = ST_BF16_STRIDE;
+    static constexpr int ctas_per_sm = 6;  // 2 x 14.3 KB each: 48 warps per SM
+};
+template <typename CT> __host__ __device__ constexpr size_t st27_stage_bytes() { return (size_t)ST_TILE * St27Coef<CT>::stride * sizeof(CT); }
+template <typename CT> __host__ __device__ constexpr size_t st27_smem() { return ST_STAGES * st27_stage_bytes<CT>() + 64; }
 
 __host__ __device__ inline int64_t st27_padded_nodes(int64_t n) { return (n + 3) / 4 * 4; }
 
-template <int MODE>
-__global__ void __launch_bounds__(ST_TILE) k_st27_apply(St27Grid g, const float* __restrict__ S, const float* w,
+// the 27 coefficients of this thread's node from the staged tile
+__device__ __forceinline__ void st27_load_coefs(const float* c, float (&v)[27])
+{
+#pragma unroll
+    for (int k = 0; k < 27; ++k) v[k] = c[k];
+}
+
+__device__ __forceinline__ void st27_load_coefs(const __nv_bfloat16* c, float (&v)[27])
+{
+    const uint2* w = reinterpret_cast<const uint2*>(c);  // 56 bytes per node: 7 aligned 8-byte words
+#pragma unroll
+    for (int q = 0; q < 7; ++q) {
+        const uint2 u = w[q];
+        const uint32_t h[2] = {u.x, u.y};
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const int k0 = q * 4 + e * 2;
+            if (k0 < 27) v[k0] = __uint_as_float(h[e] << 16);
+            if (k0 + 1 < 27) v[k0 + 1] = __uint_as_float(h[e] & 0xFFFF0000u);
+        }
+    }
+}
+
+template <int MODE, typename CT>
+__global__ void __launch_bounds__(ST_TILE) k_st27_apply(St27Grid g, const CT* __restrict__ S, const float* w,
                                                          const float* __restrict__ r, const float* __restrict__ dinv,
                                                          float omega, float* w_out, float* out, int* status)
 {
+    constexpr int STRIDE = St27Coef<CT>::stride;
+    constexpr size_t STAGE = st27_stage_bytes<CT>();
     extern __shared__ __align__(16) unsigned char smem[];
     pdl_enter();
-    float* ring = reinterpret_cast<float*>(smem);
-    uint64_t* full = reinterpret_cast<uint64_t*>(smem + ST_STAGES * ST_STAGE_BYTES);
+    CT* ring = reinterpret_cast<CT*>(smem);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + ST_STAGES * STAGE);
     const int64_t ntiles = (g.n + ST_TILE - 1) / ST_TILE;
     const int64_t npad = st27_padded_nodes(g.n);
     // copy of tile `tile` into stage s: its nodes rounded up to 4 (the padded tail of S)
     auto issue = [&](int64_t tile, int s) {
         const int64_t i0 = tile * ST_TILE;
         const int64_t cnt = npad - i0 < ST_TILE ? npad - i0 : ST_TILE;
-        const uint32_t bytes = (uint32_t)(cnt * 27 * sizeof(float));
+        const uint32_t bytes = (uint32_t)(cnt * STRIDE * sizeof(CT));
         mbar_arrive_expect_tx(&full[s], bytes);
-        bulk_g2s(ring + (size_t)s * ST_TILE * 27, S + i0 * 27, bytes, &full[s]);
+        bulk_g2s(ring + (size_t)s * ST_TILE * STRIDE, S + i0 * STRIDE, bytes, &full[s]);
     };
     if (threadIdx.x == 0) {
         for (int s = 0; s < ST_STAGES; ++s) mbar_init(&full[s], 1);
@@ -122,7 +162,8 @@ __global__ void __launch_bounds__(ST_TILE) k_st27_apply(St27Grid g, const float*
         if (!__syncthreads_and(mbar_wait_bounded(&full[s], (uint32_t)(it / ST_STAGES) & 1u))) break;
         const int64_t i = tile * ST_TILE + threadIdx.x;
         if (i < g.n) {
-            const float* c = ring + (size_t)s * ST_TILE * 27 + threadIdx.x * 27;
+            float c[27];
+            st27_load_coefs(ring + (size_t)s * ST_TILE * STRIDE + threadIdx.x * STRIDE, c);
             int x, y, z;
             st27_coords(g, i, x, y, z);
             const bool okx[3] = {x > 0, true, x < g.nx - 1};
@@ -166,11 +207,53 @@ __global__ void __launch_bounds__(ST_TILE) k_st27_apply(St27Grid g, const float*
     }
 }
 
+// S (fp32, 27 per node) -> Sb (bf16, 28 per node, the 28th zero), round to nearest even
+__global__ void k_st27_to_bf16(int64_t npad, const float* __restrict__ S, __nv_bfloat16* __restrict__ Sb)
+{
+    pdl_enter();
+    const int64_t total = npad * ST_BF16_STRIDE;
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t i = e / ST_BF16_STRIDE;
+        const int k = (int)(e - i * ST_BF16_STRIDE);
+        Sb[e] = __float2bfloat16_rn(k < 27 ? S[i * 27 + k] : 0.f);
+    }
+}
+
 static int st27_grid(int64_t n) { return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(n, 256), kSmCount * 8)); }
 
-static int st27_apply_grid(int64_t n)
+template <typename CT> static int st27_apply_grid(int64_t n)
 {
-    return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(n, ST_TILE), (int64_t)sm_count() * ST_CTAS_PER_SM));
+    return (int)std::max<int64_t>(
+        1, std::min<int64_t>(ceil_div<int64_t>(n, ST_TILE), (int64_t)sm_count() * St27Coef<CT>::ctas_per_sm));
+}
+
+template <typename CT>
+static int st27_apply_t(int mode, const St27Grid& g, const CT* S, const float* w, const float* r, const float* dinv,
+                        float omega, float* w_out, float* out, int* status, cudaStream_t stream)
+{
+    const int grid = st27_apply_grid<CT>(g.n);
+    constexpr size_t smem = st27_smem<CT>();
+    static bool attr_set = false;  // one-time per process and coefficient type
+    if (!attr_set) {
+        GB_CHECK_CUDA(cudaFuncSetAttribute(k_st27_apply<0, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        GB_CHECK_CUDA(cudaFuncSetAttribute(k_st27_apply<1, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        GB_CHECK_CUDA(cudaFuncSetAttribute(k_st27_apply<2, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr_set = true;
+    }
+    if (mode == 0) {
+        GB_CHECK_CUDA(launch_pdl(k_st27_apply<0, CT>, grid, ST_TILE, smem, stream, g, S, w, r, dinv, omega, w_out, out,
+                                 status));
+    } else if (mode == 1) {
+        GB_CHECK_CUDA(launch_pdl(k_st27_apply<1, CT>, grid, ST_TILE, smem, stream, g, S, w, r, dinv, omega, w_out, out,
+                                 status));
+    } else if (mode == 2) {
+        GB_CHECK_CUDA(launch_pdl(k_st27_apply<2, CT>, grid, ST_TILE, smem, stream, g, S, w, r, dinv, omega, w_out, out,
+                                 status));
+    } else {
+        gb::set_error("st27_apply: mode must be 0, 1 or 2");
+        return GB_ERR_INVALID;
+    }
+    return GB_OK;
 }
 
 }  // namespace gb
@@ -208,26 +291,38 @@ GB_API int gb_st27_apply(int mode, int nx, int ny, int nz, const float* S, const
     GB_REQUIRE(out != w && out != r && out != w_out, "st27_apply: out must not alias an input");
     const St27Grid g{nx, ny, nz, (int64_t)nx * ny * nz};
     GB_REQUIRE(g.n < (int64_t(1) << 31), "st27_apply: grid too large");
-    const int grid = st27_apply_grid(g.n);
-    static bool attr_set = false;  // one-time per process
-    if (!attr_set) {
-        GB_CHECK_CUDA(cudaFuncSetAttribute(k_st27_apply<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ST_SMEM));
-        GB_CHECK_CUDA(cudaFuncSetAttribute(k_st27_apply<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ST_SMEM));
-        GB_CHECK_CUDA(cudaFuncSetAttribute(k_st27_apply<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ST_SMEM));
-        attr_set = true;
-    }
-    if (mode == 0) {
-        GB_CHECK_CUDA(launch_pdl(k_st27_apply<0>, grid, ST_TILE, ST_SMEM, stream, g, S, w, r, dinv, omega, w_out, out,
-                                 status));
-    } else if (mode == 1) {
-        GB_CHECK_CUDA(launch_pdl(k_st27_apply<1>, grid, ST_TILE, ST_SMEM, stream, g, S, w, r, dinv, omega, w_out, out,
-                                 status));
-    } else if (mode == 2) {
-        GB_CHECK_CUDA(launch_pdl(k_st27_apply<2>, grid, ST_TILE, ST_SMEM, stream, g, S, w, r, dinv, omega, w_out, out,
-                                 status));
-    } else {
-        gb::set_error("st27_apply: mode must be 0, 1 or 2");
-        return GB_ERR_INVALID;
-    }
+    return st27_apply_t<float>(mode, g, S, w, r, dinv, omega, w_out, out, status, stream);
+}
+
+GB_API size_t gb_st27_bytes_bf16(int nx, int ny, int nz)
+{
+    return (size_t)ST_BF16_STRIDE * st27_padded_nodes((int64_t)nx * ny * nz) * sizeof(__nv_bfloat16);
+}
+
+// bf16 copy of the node-major coefficients S (gb_st27_bytes_bf16; 16-byte aligned).
+GB_API int gb_st27_to_bf16(int nx, int ny, int nz, const float* S, void* Sb, cudaStream_t stream)
+{
+    GB_REQUIRE(nx >= 1 && ny >= 1 && nz >= 1 && S && Sb, "st27_to_bf16: bad arguments");
+    GB_REQUIRE((uintptr_t)Sb % 16 == 0, "st27_to_bf16: Sb must be 16-byte aligned");
+    const int64_t npad = st27_padded_nodes((int64_t)nx * ny * nz);
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(npad * ST_BF16_STRIDE, 256),
+                                                                 kSmCount * 8));
+    GB_CHECK_CUDA(launch_pdl(k_st27_to_bf16, grid, 256, 0, stream, npad, S, static_cast<__nv_bfloat16*>(Sb)));
     return GB_OK;
+}
+
+// gb_st27_apply with the bf16 coefficient copy (products accumulate in fp32).
+GB_API int gb_st27_apply_bf16(int mode, int nx, int ny, int nz, const void* Sb, const float* w, const float* r,
+                              const float* dinv, float omega, float* w_out, float* out, int* status,
+                              cudaStream_t stream)
+{
+    GB_REQUIRE(nx >= 1 && ny >= 1 && nz >= 1 && Sb && r && out && status, "st27_apply_bf16: bad arguments");
+    GB_REQUIRE((uintptr_t)Sb % 16 == 0, "st27_apply_bf16: Sb must be 16-byte aligned");
+    GB_REQUIRE(mode == 1 ? (dinv && w_out) : (w != nullptr && (mode == 0 || dinv != nullptr)),
+               "st27_apply_bf16: missing operand for mode");
+    GB_REQUIRE(out != w && out != r && out != w_out, "st27_apply_bf16: out must not alias an input");
+    const St27Grid g{nx, ny, nz, (int64_t)nx * ny * nz};
+    GB_REQUIRE(g.n < (int64_t(1) << 31), "st27_apply_bf16: grid too large");
+    return st27_apply_t<__nv_bfloat16>(mode, g, static_cast<const __nv_bfloat16*>(Sb), w, r, dinv, omega, w_out, out,
+                                       status, stream);
 }

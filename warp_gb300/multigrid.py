@@ -54,10 +54,11 @@ class MultigridPreconditioner:
         coarsest_nodes: stop coarsening at or below this many nodes.
         stencil: apply the level operators in 27-point stencil form (else the CSR kernels; 1x1 only).
         poisson: Poisson ratio of the elasticity levels (3x3).
-        fine_values: scalar type of the fine level's matrix values inside the V-cycle (CSR levels):
-            ``torch.bfloat16`` keeps a bf16 copy for the cycle's residual and smoothing passes, about
-            half their matrix traffic; the flexible solver's own product keeps the fp32 matrix, so
-            its tolerance and the FP64 refinement are unaffected (the cycle only has to be a good
+        fine_values: scalar type of the fine level's matrix values inside the V-cycle:
+            ``torch.bfloat16`` keeps a bf16 copy (of the CSR values, or of the 27-point stencil
+            coefficients) for the cycle's residual and smoothing passes, about half their matrix
+            traffic, with fp32 accumulation; the flexible solver's own product keeps the fp32 matrix,
+            so its tolerance and the FP64 refinement are unaffected (the cycle only has to be a good
             approximate inverse).
 
     Vectors of a 3x3 hierarchy hold 3 interleaved components per node; masks are per node.
@@ -152,6 +153,11 @@ class MultigridPreconditioner:
         for li, bad in enumerate(st_status.tolist()):
             if bad:
                 levels[li].S = None  # entries outside the 27-neighbourhood: keep the CSR kernels
+        for li, lv in enumerate(levels):
+            lv.Sb = None
+            if li == 0 and lv.S is not None and fine_values == torch.bfloat16:
+                lv.Sb = A.empty(int(L.gb_st27_bytes_bf16(*lv.dims)) // 2, torch.bfloat16)
+                N.check(L.gb_st27_to_bf16(*lv.dims, A.ptr(lv.S), A.ptr(lv.Sb), stream), "st27_to_bf16")
         # coarsest level: dense inverse (set-up only; a few hundred unknowns)
         last = levels[-1]
         dense = last.A.numpy_dense()
@@ -216,13 +222,11 @@ class MultigridPreconditioner:
         if li == 0 and self.smoother is not None:
             self.smoother.launch(stream, r, w)
             if lv.S is not None:
-                N.check(L.gb_st27_apply(0, *lv.dims, A.ptr(lv.S), w, r, None, lv.omega, None, t, A.ptr(self.status),
-                                        stream), "residual")
+                self._st27(lv, 0, w, r, None, None, t, stream)  # residual
             else:
                 self._csr_residual(lv, w, r, t, stream)
         elif lv.S is not None:
-            N.check(L.gb_st27_apply(1, *lv.dims, A.ptr(lv.S), None, r, A.ptr(lv.dinv), lv.omega, w, t,
-                                    A.ptr(self.status), stream), "jacobi0+residual")
+            self._st27(lv, 1, None, r, A.ptr(lv.dinv), w, t, stream)  # first Jacobi step + residual
         else:
             N.check(L.gb_mg_jacobi0(lv.n * self.bdim, lv.omega, A.ptr(lv.dinv), r, w, stream), "jacobi0")
             self._csr_residual(lv, w, r, t, stream)
@@ -236,12 +240,21 @@ class MultigridPreconditioner:
                 "prolong")
         # post-smoothing fused with its residual: z = w + omega D^-1 (r - A w)
         if lv.S is not None:
-            N.check(L.gb_st27_apply(2, *lv.dims, A.ptr(lv.S), w, r, A.ptr(lv.dinv), lv.omega, None, z,
-                                    A.ptr(self.status), stream), "smooth")
+            self._st27(lv, 2, w, r, A.ptr(lv.dinv), None, z, stream)  # smoothing step + residual
         else:
             N.check(L.gb_bsr_jacobi_smooth(self.bdim, lv.n, lv.nnz, lv.nnz, A.ptr(Am.offsets), A.ptr(Am.columns),
                                            A.ptr(lv.vals), lv.vals_dtype, r, w, A.ptr(lv.dinv), lv.omega, z,
                                            A.ptr(self.status), stream), "smooth")
+
+    def _st27(self, lv, mode: int, w, r: int, dinv, w_out, out: int, stream) -> None:
+        """One stencil pass of level lv (fp32 coefficients, or their bf16 copy on the fine level)."""
+        L = N.lib()
+        if lv.Sb is not None:
+            N.check(L.gb_st27_apply_bf16(mode, *lv.dims, A.ptr(lv.Sb), w, r, dinv, lv.omega, w_out, out,
+                                         A.ptr(self.status), stream), "st27_apply_bf16")
+        else:
+            N.check(L.gb_st27_apply(mode, *lv.dims, A.ptr(lv.S), w, r, dinv, lv.omega, w_out, out, A.ptr(self.status),
+                                    stream), "st27_apply")
 
     def _csr_residual(self, lv, w: int, r: int, t: int, stream) -> None:
         Am = lv.A
