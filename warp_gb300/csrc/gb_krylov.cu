@@ -10,8 +10,9 @@
 // Here one iteration is three kernels: (1) SpMV Ap = A p fused with p.Ap, (2) x/r update fused
 // with z = D^-1 r and the r.r / r.z reductions, (3) p = z + beta p.  Each reduction is a single
 // pass: CTAs publish partials and the last CTA to finish sums them in a fixed order (so results
-// are deterministic) and computes the next scalar (alpha, beta, the loop condition).  Nothing
-// spins: there is no inter-CTA waiting anywhere in the solve.
+// are deterministic; double-float across warps and CTAs, grid_reduce_df) and computes the next
+// scalar (alpha, beta, the loop condition).  Nothing in these kernels waits on another CTA; the
+// persistent CG below does, at grid barriers of a cooperative launch.
 //
 // Solver scalars live in device memory; the loop condition is evaluated on the device and drives
 // a cudaGraphCondTypeWhile node, so a whole solve is one graph launch with no host round trip.
@@ -138,7 +139,7 @@ __global__ __launch_bounds__(SPMV_THREADS) void k_cg_init(const SolveArgs* __res
                                            smem, &a.S->status, epi);
     }
     float v[3] = {epi.bb, epi.rr, epi.rz};
-    grid_reduce<3>(v, a.partials, &a.S->counters[0], s_red,
+    grid_reduce_df<3>(v, a.partials, &a.S->counters[0], s_red,
                    [&](const double (&t)[3]) { cg_init_finish(a, t, h, has_cond); });
 }
 
@@ -170,7 +171,7 @@ __global__ __launch_bounds__(SPMV_THREADS) void k_cg_spmv(const SolveArgs* __res
     spmv_run<BR, BR, VT, float, float>(nrow, sh, a.offsets, a.row_counts, a.columns, (const VT*)a.values, a.p, smem,
                                         &S->status, epi);
     float v[1] = {epi.pAp};
-    grid_reduce<1>(v, a.partials, &S->counters[1], s_red, [&](const double (&t)[1]) {
+    grid_reduce_df<1>(v, a.partials, &S->counters[1], s_red, [&](const double (&t)[1]) {
         S->pAp = t[0];
         double alpha = 0.0;
         if (S->rr > S->atol_sq) {
@@ -235,7 +236,7 @@ __global__ __launch_bounds__(VEC_THREADS) void k_cg_update(const SolveArgs* __re
         rz += ri * zi;
     }
     float v[2] = {rr, rz};
-    grid_reduce<2>(v, a.partials, &S->counters[2], s_red, [&](const double (&t)[2]) {
+    grid_reduce_df<2>(v, a.partials, &S->counters[2], s_red, [&](const double (&t)[2]) {
         const double rz_old = S->rz;
         S->rr = t[0];
         S->rz = t[1];
@@ -373,29 +374,8 @@ __device__ __forceinline__ bool cg_grid_barrier(KrylovScalars* S, volatile int* 
     return *s_ok != 0;
 }
 
-// Sums inside the persistent CG run in double-float (unevaluated hi + lo pairs of fp32, ~44 bits;
-// gb_df32.cuh): GB300's FP64 pipe is a small fraction of its FP32 rate and its latency sat on the
-// critical path between the grid barriers.  A butterfly of df32 adds leaves every lane with the same
-// value (two_sum is exact, so a + b and b + a agree bit for bit).
-__device__ __forceinline__ df32 warp_sum_df(df32 d)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const df32 other(__shfl_xor_sync(0xffffffffu, d.hi, o), __shfl_xor_sync(0xffffffffu, d.lo, o));
-        d = d + other;
-    }
-    return d;
-}
-
-__device__ __forceinline__ bool df_gt(const df32& a, const df32& b) { return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo); }
-
-__device__ __forceinline__ df32 df_from_double(double v)
-{
-    const float h = (float)v;
-    return df32(h, (float)(v - (double)h));
-}
-
-__device__ __forceinline__ double df_to_double(const df32& d) { return (double)d.hi + (double)d.lo; }
+// Sums inside the persistent CG run in double-float (gb_df32.cuh): GB300's FP64 pipe is a small
+// fraction of its FP32 rate and its latency sat on the critical path between the grid barriers.
 
 // Sum of NV per-thread fp32 values over the 512 consumer threads (fp32 within a warp, double-float
 // across warps); the result is valid in thread 32.
@@ -880,7 +860,7 @@ __global__ __launch_bounds__(SPMV_THREADS) void k_bi_init(const SolveArgs* __res
                                            smem, &a.S->status, epi);
     }
     float v[2] = {epi.bb, epi.rr};
-    grid_reduce<2>(v, a.partials, &a.S->counters[0], s_red, [&](const double (&t)[2]) {
+    grid_reduce_df<2>(v, a.partials, &a.S->counters[0], s_red, [&](const double (&t)[2]) {
         KrylovScalars* S = a.S;
         const double at = fmax(a.tol * sqrt(t[0]), a.atol);
         S->bb = t[0];
@@ -928,7 +908,7 @@ __global__ __launch_bounds__(SPMV_THREADS) void k_bi_spmv_v(const SolveArgs* __r
     spmv_run<BR, BR, VT, float, float>(nrow, sh, a.offsets, a.row_counts, a.columns, (const VT*)a.values, a.y, smem,
                                         &S->status, epi);
     float v[1] = {epi.r0v};
-    grid_reduce<1>(v, a.partials, &S->counters[1], s_red, [&](const double (&t)[1]) {
+    grid_reduce_df<1>(v, a.partials, &S->counters[1], s_red, [&](const double (&t)[1]) {
         S->r0v = t[0];
         double alpha = 0.0;
         if (S->rr > S->atol_sq) {
@@ -961,7 +941,7 @@ __global__ __launch_bounds__(VEC_THREADS) void k_bi_update1(const SolveArgs* __r
         rr += ri * ri;
     }
     float v[1] = {rr};
-    grid_reduce<1>(v, a.partials, &S->counters[2], s_red, [&](const double (&t)[1]) { S->rr = t[0]; });
+    grid_reduce_df<1>(v, a.partials, &S->counters[2], s_red, [&](const double (&t)[1]) { S->rr = t[0]; });
 }
 
 // t = A z ; st, tt (right: r.t, t.t ; left: z.Mt, Mt.Mt) -> omega
@@ -1002,7 +982,7 @@ __global__ __launch_bounds__(SPMV_THREADS) void k_bi_spmv_t(const SolveArgs* __r
     spmv_run<BR, BR, VT, float, float>(nrow, sh, a.offsets, a.row_counts, a.columns, (const VT*)a.values, a.z, smem,
                                         &S->status, epi);
     float v[2] = {epi.st, epi.tt};
-    grid_reduce<2>(v, a.partials, &S->counters[3], s_red, [&](const double (&t)[2]) {
+    grid_reduce_df<2>(v, a.partials, &S->counters[3], s_red, [&](const double (&t)[2]) {
         S->st = t[0];
         S->tt = t[1];
         double omega = 0.0;
@@ -1037,7 +1017,7 @@ __global__ __launch_bounds__(VEC_THREADS) void k_bi_update2(const SolveArgs* __r
         rho += a.r0[i] * ri;
     }
     float v[2] = {rr, rho};
-    grid_reduce<2>(v, a.partials, &S->counters[4], s_red, [&](const double (&t)[2]) {
+    grid_reduce_df<2>(v, a.partials, &S->counters[4], s_red, [&](const double (&t)[2]) {
         S->rr = t[0];
         const bool active = t[0] > S->atol_sq;
         double beta = 0.0, beta_omega = 0.0;
@@ -1099,7 +1079,7 @@ __global__ __launch_bounds__(VEC_THREADS) void k_fcg_dir(const SolveArgs* __rest
         zap += zi * a.Ap[i];
     }
     float v[2] = {zr, zap};
-    grid_reduce<2>(v, a.partials, &S->counters[5], s_red, [&](const double (&t)[2]) {
+    grid_reduce_df<2>(v, a.partials, &S->counters[5], s_red, [&](const double (&t)[2]) {
         S->rz = t[0];
         double beta = 0.0;
         if (S->iter > 0 && S->pAp != 0.0) beta = -t[1] / S->pAp;

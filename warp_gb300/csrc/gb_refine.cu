@@ -94,7 +94,7 @@ __global__ __launch_bounds__(SPMV_THREADS) void k_resid_df(int nrow, SpmvShape s
     EpiResid<BR, df32> epi{b, r64, r32};
     spmv_run<BR, BR, VT, float2, df32>(nrow, sh, offsets, row_counts, columns, values, x2, smem, status, epi);
     float v[2] = {epi.rr, epi.bb};
-    grid_reduce<2>(v, partials, counter, s_red, [&](const double (&t)[2]) {
+    grid_reduce_df<2>(v, partials, counter, s_red, [&](const double (&t)[2]) {
         norms[0] = t[0];
         norms[1] = t[1];
     });
@@ -114,7 +114,7 @@ __global__ __launch_bounds__(SPMV_THREADS) void k_resid64(int nrow, SpmvShape sh
     EpiResid64<BR> epi{b, r64, r32};
     spmv_run<BR, BR, VT, double, double>(nrow, sh, offsets, row_counts, columns, values, x, smem, status, epi);
     float v[2] = {epi.rr, epi.bb};
-    grid_reduce<2>(v, partials, counter, s_red, [&](const double (&t)[2]) {
+    grid_reduce_df<2>(v, partials, counter, s_red, [&](const double (&t)[2]) {
         norms[0] = t[0];
         norms[1] = t[1];
     });
