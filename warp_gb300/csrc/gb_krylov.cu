@@ -1072,8 +1072,21 @@ __global__ __launch_bounds__(VEC_THREADS) void k_fcg_dir(const SolveArgs* __rest
     KrylovScalars* S = a.S;
     if (!S->cond) return;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     float zr = 0.f, zap = 0.f;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
+    int64_t done = 0;
+    if ((((uintptr_t)a.z | (uintptr_t)a.r | (uintptr_t)a.Ap) & 15) == 0) {
+        const int64_t n4 = a.n >> 2;
+        for (int64_t i = tid; i < n4; i += stride) {
+            const float4 zv = reinterpret_cast<const float4*>(a.z)[i];
+            const float4 rv = reinterpret_cast<const float4*>(a.r)[i];
+            const float4 av = reinterpret_cast<const float4*>(a.Ap)[i];
+            zr += zv.x * rv.x + zv.y * rv.y + zv.z * rv.z + zv.w * rv.w;
+            zap += zv.x * av.x + zv.y * av.y + zv.z * av.z + zv.w * av.w;
+        }
+        done = n4 << 2;
+    }
+    for (int64_t i = done + tid; i < a.n; i += stride) {
         const float zi = a.z[i];
         zr += zi * a.r[i];
         zap += zi * a.Ap[i];
@@ -1101,8 +1114,19 @@ __global__ __launch_bounds__(VEC_THREADS) void k_fcg_p(const SolveArgs* __restri
     if (!S->cond) return;
     const float beta = (float)S->beta;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride)
-        a.p[i] = a.z[i] + beta * a.p[i];
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t done = 0;
+    if ((((uintptr_t)a.z | (uintptr_t)a.p) & 15) == 0) {
+        const int64_t n4 = a.n >> 2;
+        for (int64_t i = tid; i < n4; i += stride) {
+            const float4 zv = reinterpret_cast<const float4*>(a.z)[i];
+            float4 pv = reinterpret_cast<float4*>(a.p)[i];
+            pv.x = zv.x + beta * pv.x; pv.y = zv.y + beta * pv.y; pv.z = zv.z + beta * pv.z; pv.w = zv.w + beta * pv.w;
+            reinterpret_cast<float4*>(a.p)[i] = pv;
+        }
+        done = n4 << 2;
+    }
+    for (int64_t i = done + tid; i < a.n; i += stride) a.p[i] = a.z[i] + beta * a.p[i];
 }
 
 __global__ void k_store_args(SolveArgs* dst, SolveArgs src, int reset_status)

@@ -25,6 +25,8 @@ V-cycle into its CUDA graph.
 
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 import torch
 
@@ -169,17 +171,44 @@ class MultigridPreconditioner:
         torch.cuda.current_stream().synchronize()
 
     def _auto_omega(self, lv, iters: int = 30) -> float:
-        """4 / (3 rho(D^-1 A)) with rho from power iteration on the level (set-up only)."""
-        g = torch.Generator(device="cuda").manual_seed(7)
-        x = torch.rand(lv.n * self.bdim, device="cuda", generator=g) + 0.5
-        y = torch.empty_like(x)
+        """4 / (3 rho(D^-1 A)) with rho from power iteration on the level (set-up only).  Runs on the
+        library's own kernels (SpMV, dot products, axpby), so the set-up launches no torch reduction
+        (those are compiled for this GPU on first use, which took seconds on a fresh process)."""
+        L = N.lib()
+        stream = A.stream()
+        m = lv.n * self.bdim
+        rng = np.random.default_rng(7)
+        x = A.from_numpy((rng.random(m) + 0.5).astype(np.float32))
+        y = A.empty(m, torch.float32)
+        z = A.empty(m, torch.float32)
+        ws = A.zeros(int(L.gb_dots_workspace_bytes()), torch.uint8)
+        out = A.zeros(4, torch.float64)
+        host = torch.zeros(4, dtype=torch.float64, pin_memory=True)
+
+        def norms(*vs) -> list[float]:
+            ptrs = (ctypes.c_void_p * 4)(*[v.data_ptr() for v in vs])
+            N.check(L.gb_dots(N.GB_F32, m, len(vs), ptrs, ptrs, out.data_ptr(), ws.data_ptr(), stream), "dots")
+            host[: len(vs)].copy_(out[: len(vs)], non_blocking=True)
+            torch.cuda.current_stream().synchronize()
+            return [float(v) ** 0.5 for v in host[: len(vs)].tolist()]
+
+        # a <- D^-1 A b with b = a, rescaled to unit norm every 8 steps (8 steps grow it by rho^8, far inside
+        # fp32 range for these operators, rho ~ 2-5); three buffers so that no kernel reads and writes the
+        # same vector; rho = |a| / |b| at the last step.  5 host reads per level.
+        a, b, c = x, y, z
+        nrm = norms(a)[0]
         rho = 1.0
-        for _ in range(iters):
-            x /= torch.linalg.vector_norm(x)
-            sparse.bsr_mv(lv.A, x, y)
-            y *= lv.dinv
-            rho = float(torch.linalg.vector_norm(y))
-            x, y = y, x
+        for it in range(iters):
+            scale = 1.0 / max(nrm, 1e-30) if it % 8 == 0 else 1.0
+            N.check(L.gb_axpby(N.GB_F32, m, scale, a.data_ptr(), 0.0, a.data_ptr(), b.data_ptr(), stream), "scale")
+            sparse.bsr_mv(lv.A, b, c)
+            N.check(L.gb_diag_mv(N.GB_F32, m, lv.dinv.data_ptr(), c.data_ptr(), None, a.data_ptr(), 1.0, 0.0,
+                                 stream), "dinv")
+            if it == iters - 1:
+                na, nb = norms(a, b)
+                rho = na / max(nb, 1e-30)
+            elif (it + 1) % 8 == 0:
+                nrm = norms(a)[0]
         return 4.0 / (3.0 * max(rho, 1e-30))
 
     @property
