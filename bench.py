@@ -760,6 +760,10 @@ def main():
     l32solver = linear.RefinedSolver(A, M=l32, method="fcg", inner_tol=args.inner_tol)
     l32ms, l32infos, _, _ = timed(l32solver, system.b, max(3, args.steps // 4))
     del l32solver, l32
+    # ... and with the flexible solver's product on the CSR matrix instead of the fine level's stencil form
+    lcsr = linear.RefinedSolver(A, M=lmg, method="fcg", inner_tol=args.inner_tol, stencil_product=False)
+    lcsr_ms, lcsr_infos, _, _ = timed(lcsr, system.b, max(3, args.steps // 4))
+    del lcsr
 
     # ---- the learned smoother's layers (tensor-core roofline) ----------------------------------
     sm = lmg.smoother
@@ -978,7 +982,8 @@ def main():
                         "outer_iterations": statistics.median(outer),
                         "rel_residual": max(i["rel_residual"] for i in linfos), "fallbacks": lsolver.fallbacks,
                         "setup_ms": setup_ms, "speedup_vs_jacobi_cg": jms / ms, "vcycle_fine_values": VCYCLE_FINE,
-                        "fp32_vcycle_ms": l32ms,
+                        "fp32_vcycle_ms": l32ms, "stencil_product": lsolver.inner.stencil_product,
+                        "csr_product_ms": lcsr_ms,
                         "fp32_vcycle_inner_iterations": statistics.median([i["inner_iterations"] for i in l32infos]),
                         **oracle_check(lsolver.last_x)},
         "jacobi_cg": {"ms": jms, "inner_iterations": statistics.median([i["inner_iterations"] for i in jinfos]),

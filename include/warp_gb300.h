@@ -205,6 +205,10 @@ int gb_dirichlet_project(int bdim, int nrow, const int* offsets, const int* colu
  * r.z <= 0) stops the loop with GB_DEV_STAGNATION so the caller can fall back to Jacobi-CG. */
 typedef int (*gb_precond_fn)(void* user, gb_stream_t stream, const float* r, float* z);
 int gb_krylov_set_precond(void* handle, gb_precond_fn fn, void* user, int stag_window, double stag_factor);
+/* Flexible solver with 1x1 blocks: take the product of every iteration from the 27-point stencil form S of
+ * the same matrix on an nx x ny x nz node grid (gb_st27_build; the caller keeps S alive); S = NULL returns
+ * to the CSR product. */
+int gb_krylov_set_stencil(void* handle, int nx, int ny, int nz, const float* S);
 /* z_out = z + omega * dinv * (r - A z) (fused Jacobi smoothing step; z_out may not alias z; fp32 or bf16
  * values). */
 int gb_bsr_jacobi_smooth(int bdim, int nrow, int64_t nnz, int64_t ncap, const int* offsets, const int* columns,

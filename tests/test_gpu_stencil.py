@@ -231,3 +231,57 @@ def test_bf16_fine_stencil_fcg_converges(cuda, learned_smoother):
         assert int(mg.status.item()) == 0
         its[fv] = it
     assert its[torch.bfloat16] <= its[torch.float32] + 1, its
+
+
+@pytest.mark.parametrize("learned_smoother", [False, True])
+def test_fcg_stencil_product_matches_csr_product(cuda, learned_smoother):
+    """The flexible solver's product on the fine level's stencil form (k_fcg_st27_ap) against the CSR
+    product: same iteration count within one, and the refined solve reaches 1e-8 with the FP64 residual
+    recomputed on the host."""
+    import os
+
+    from warp_gb300 import learned, multigrid
+    from warp_gb300.optim import linear
+
+    s = _system((20, 18, 22), seed=13)
+    n, off, col, val = _csr(s.A)
+    mg = multigrid.MultigridPreconditioner(s.A, s.geo, s.coef)
+    if learned_smoother:
+        w = os.path.join(os.path.dirname(__file__), "..", "warp_gb300", "data", "smoother_q1_diffusion.npz")
+        mg.smoother = learned.LearnedSmoother(learned.ConvNet.load(w), mg, s.coef)
+    its = {}
+    for st in (False, True):
+        x = torch.zeros_like(s.b)
+        solver = linear.FCG(s.A, s.b, x, tol=1e-6, atol=0.0, maxiter=300, M=mg, check_every=1,
+                            stencil="auto" if st else None)
+        assert solver.stencil_product == st
+        it, res, atol = solver()
+        assert res <= atol
+        its[st] = it
+        r = s.b.cpu().numpy().astype(np.float64) - _matvec(off, col, val, x.cpu().numpy().astype(np.float64))
+        assert np.linalg.norm(r) <= 32e-6 * np.linalg.norm(s.b.cpu().numpy()), st
+    assert abs(its[True] - its[False]) <= 1, its
+    for sp in (False, True):
+        rs = linear.RefinedSolver(s.A, M=mg, method="fcg", inner_tol=1e-5, stencil_product=sp)
+        assert rs.inner.stencil_product == sp
+        x64, info = rs.solve(s.b, tol=1e-8)
+        assert info["converged"] and rs.fallbacks == 0
+        bh = s.b.cpu().numpy().astype(np.float64)
+        r = bh - _matvec(off, col, val, x64.cpu().numpy())
+        assert np.linalg.norm(r) <= 2e-8 * np.linalg.norm(bh)
+
+
+def test_fcg_stencil_rejects_mismatched_grid(cuda):
+    from warp_gb300 import _native as N
+    from warp_gb300 import multigrid
+    from warp_gb300.optim import linear
+
+    s = _system((8, 8, 8), seed=2)
+    mg = multigrid.MultigridPreconditioner(s.A, s.geo, s.coef)
+    S = mg.levels[0].S
+    assert S is not None and len(mg.levels) > 1
+    x = torch.zeros_like(s.b)
+    solver = linear.FCG(s.A, s.b, x, tol=1e-6, maxiter=50, M=mg)
+    assert N.lib().gb_krylov_set_stencil(solver._native, 9, 9, 10, S.data_ptr()) != 0  # 810 nodes, not 729
+    assert N.lib().gb_krylov_set_stencil(solver._native, 9, 9, 9, S.data_ptr()) == 0
+    assert N.lib().gb_krylov_set_stencil(solver._native, 0, 0, 0, None) == 0

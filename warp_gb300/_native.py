@@ -71,6 +71,7 @@ _SIGNATURES = {
     "gb_update_solution": (_c_int, [_c_i64, _vp, _vp, _vp, _c_dbl, _vp]),
     "gb_krylov_set_precond": (_c_int, [_vp, _vp, _vp, _c_int, _c_dbl]),
     "gb_krylov_set_persistent": (_c_int, [_vp, _c_int, _vp]),
+    "gb_krylov_set_stencil": (_c_int, [_vp, _c_int, _c_int, _c_int, _vp]),
     "gb_bsr_jacobi_smooth": (_c_int, [_c_int, _c_int, _c_i64, _c_i64, _vp, _vp, _vp, _c_int, _vp, _vp, _vp,
                                       ctypes.c_float, _vp, _vp, _vp]),
     "gb_mg_restrict": (_c_int, [_c_int] * 6 + [_vp, _vp, _vp, _vp, _vp]),

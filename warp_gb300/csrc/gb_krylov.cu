@@ -21,6 +21,7 @@
 #include "gb_common.cuh"
 #include "gb_df32.cuh"
 #include "gb_spmv.cuh"
+#include "gb_st27.cuh"
 
 #include <new>
 
@@ -820,6 +821,94 @@ __global__ __launch_bounds__(SPMV_THREADS, 2) void k_cg_loop(const SolveArgs* __
     __syncthreads();
 }
 
+// Flexible-CG product on the 27-point stencil form of A (the fine level of the multigrid carrier
+// holds it): Ap = A p with p.Ap and alpha -- the k_cg_spmv step reading 108 B of coefficients and
+// 12 B of vectors per node instead of the CSR's 8 B per nonzero.  The staging is k_st27_apply's
+// (gb_stencil.cu): per 256-node tile one bulk copy into a 2-stage ring, four CTAs per SM.
+__global__ void __launch_bounds__(ST_TILE) k_fcg_st27_ap(const SolveArgs* __restrict__ args, St27Grid g,
+                                                         const float* __restrict__ Sc)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double s_red[32];
+    pdl_enter();
+    const SolveArgs a = *args;
+    KrylovScalars* S = a.S;
+    if (!S->cond) return;
+    constexpr size_t STAGE = st27_stage_bytes<float>();
+    float* ring = reinterpret_cast<float*>(smem);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + ST_STAGES * STAGE);
+    const int64_t ntiles = (g.n + ST_TILE - 1) / ST_TILE;
+    const int64_t npad = st27_padded_nodes(g.n);
+    auto issue = [&](int64_t tile, int s) {
+        const int64_t i0 = tile * ST_TILE;
+        const int64_t cnt = npad - i0 < ST_TILE ? npad - i0 : ST_TILE;
+        const uint32_t bytes = (uint32_t)(cnt * 27 * sizeof(float));
+        mbar_arrive_expect_tx(&full[s], bytes);
+        bulk_g2s(ring + (size_t)s * ST_TILE * 27, Sc + i0 * 27, bytes, &full[s]);
+    };
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < ST_STAGES; ++s) mbar_init(&full[s], 1);
+        fence_mbar_init();
+        for (int s = 0; s < ST_STAGES; ++s)
+            if (blockIdx.x + (int64_t)s * gridDim.x < ntiles) issue(blockIdx.x + (int64_t)s * gridDim.x, s);
+    }
+    __syncthreads();
+    const int64_t yz = (int64_t)g.ny * g.nz;
+    float pAp = 0.f;
+    int it = 0;
+    int64_t tile = blockIdx.x;
+    for (; tile < ntiles; tile += gridDim.x, ++it) {
+        const int s = it % ST_STAGES;
+        if (!__syncthreads_and(mbar_wait_bounded(&full[s], (uint32_t)(it / ST_STAGES) & 1u))) break;
+        const int64_t i = tile * ST_TILE + threadIdx.x;
+        if (i < g.n) {
+            float c[27];
+            st27_load_coefs(ring + (size_t)s * ST_TILE * 27 + threadIdx.x * 27, c);
+            int x, y, z;
+            st27_coords(g, i, x, y, z);
+            const bool okx[3] = {x > 0, true, x < g.nx - 1};
+            const bool oky[3] = {y > 0, true, y < g.ny - 1};
+            const bool okz[3] = {z > 0, true, z < g.nz - 1};
+            float acc = 0.f;
+#pragma unroll
+            for (int k = 0; k < 27; ++k) {
+                const int dx = k / 9 - 1, dy = (k / 3) % 3 - 1, dz = k % 3 - 1;
+                if (okx[dx + 1] && oky[dy + 1] && okz[dz + 1])
+                    acc = fmaf(c[k], __ldg(a.p + i + dx * yz + (int64_t)dy * g.nz + dz), acc);
+            }
+            a.Ap[i] = acc;
+            pAp += a.p[i] * acc;
+        }
+        __syncthreads();  // stage s is read: refill it
+        if (threadIdx.x == 0 && tile + (int64_t)ST_STAGES * gridDim.x < ntiles)
+            issue(tile + (int64_t)ST_STAGES * gridDim.x, s);
+    }
+    if (tile < ntiles) {
+        // a wait gave up: drain the copies still in flight (bounded) before shared memory goes away
+        if (threadIdx.x == 0) {
+            for (int q = 0; q < ST_STAGES; ++q) {
+                const int64_t tq = tile + (int64_t)q * gridDim.x;
+                if (tq < ntiles) mbar_wait_bounded(&full[(it + q) % ST_STAGES], (uint32_t)((it + q) / ST_STAGES) & 1u);
+            }
+            atomicOr(&S->status, GB_DEV_WAIT_TIMEOUT);
+        }
+        __syncthreads();
+    }
+    float v[1] = {pAp};
+    grid_reduce_df<1>(v, a.partials, &S->counters[1], s_red, [&](const double (&t)[1]) {
+        S->pAp = t[0];
+        double alpha = 0.0;
+        if (S->rr > S->atol_sq) {
+            alpha = S->rz / t[0];
+            if (!finite(alpha)) {
+                S->status |= GB_DEV_BREAKDOWN;
+                alpha = 0.0;
+            }
+        }
+        S->alpha = alpha;
+    });
+}
+
 // ---------------------------------------------------------------------------------------------
 // BiCGSTAB (right preconditioning by default, left with left_precond; M = D^-1 or identity)
 // ---------------------------------------------------------------------------------------------
@@ -1159,6 +1248,9 @@ struct Solver {
     void* precond_user = nullptr;
     int loop_grid = 0;   // CTAs of the persistent CG launch (0: the device cannot hold the SpMV grid at once)
     int persistent = 1;  // CG: run iterations as one cooperative launch when loop_grid > 0
+    const float* st_S = nullptr;  // flexible solver: 27-point stencil form of A for its product (or null)
+    St27Grid st_g = {};
+    int st_grid = 0;
 };
 
 static bool use_loop(const Solver* s) { return s->kind == KRYLOV_CG && s->persistent && s->loop_grid > 0; }
@@ -1260,7 +1352,12 @@ static int launch_iter_t(Solver* s, cudaStream_t st, cudaGraphConditionalHandle 
         }
         GB_CHECK_CUDA(launch_pdl(k_fcg_dir, s->vec_grid, VEC_THREADS, 0, st, s->d_args, h, has_cond));
         GB_CHECK_CUDA(launch_pdl(k_fcg_p, s->vec_grid, VEC_THREADS, 0, st, s->d_args));
-        GB_CHECK_CUDA(launch_pdl(k_cg_spmv<BR, VT>, s->spmv_grid, SPMV_THREADS, s->spmv_smem, st, s->d_args, s->nrow, s->sh));
+        if (s->st_S)
+            GB_CHECK_CUDA(launch_pdl(k_fcg_st27_ap, s->st_grid, ST_TILE, st27_smem<float>(), st, s->d_args, s->st_g,
+                                     s->st_S));
+        else
+            GB_CHECK_CUDA(launch_pdl(k_cg_spmv<BR, VT>, s->spmv_grid, SPMV_THREADS, s->spmv_smem, st, s->d_args,
+                                     s->nrow, s->sh));
         GB_CHECK_CUDA(launch_pdl(k_cg_update, s->vec_grid, VEC_THREADS, 0, st, s->d_args, h, has_cond));
     } else if (s->kind == KRYLOV_CG && use_loop(s)) {
         return launch_loop(s, st, 1);
@@ -1651,5 +1748,37 @@ GB_API int gb_krylov_set_persistent(void* handle, int enable, int* active_out)
     s->exec_while = s->exec_init = s->exec_chunk = nullptr;
     s->chunk_iters = 0;
     if (active_out) *active_out = use_loop(s) ? 1 : 0;
+    return GB_OK;
+}
+
+// Flexible solver with 1x1 blocks on an nx x ny x nz node grid: use the 27-point stencil form S of A
+// (node-major fp32 coefficients, gb_st27_build / gb_st27_bytes, 16-byte aligned; the caller keeps it
+// alive and equal to A) for the product of every iteration; S = null returns to the CSR product.
+// Drops any cached graphs.
+GB_API int gb_krylov_set_stencil(void* handle, int nx, int ny, int nz, const float* S)
+{
+    Solver* s = static_cast<Solver*>(handle);
+    GB_REQUIRE(s && s->kind == KRYLOV_FCG, "krylov_set_stencil: flexible solver handle required");
+    if (S) {
+        GB_REQUIRE(s->br == 1, "krylov_set_stencil: 1x1 blocks required");
+        GB_REQUIRE(nx >= 1 && ny >= 1 && nz >= 1 && (int64_t)nx * ny * nz == (int64_t)s->nrow,
+                   "krylov_set_stencil: grid %dx%dx%d does not match %d rows", nx, ny, nz, s->nrow);
+        GB_REQUIRE((uintptr_t)S % 16 == 0, "krylov_set_stencil: S must be 16-byte aligned");
+        static bool attr_set = false;
+        if (!attr_set) {
+            GB_CHECK_CUDA(cudaFuncSetAttribute(k_fcg_st27_ap, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)st27_smem<float>()));
+            attr_set = true;
+        }
+        s->st_g = St27Grid{nx, ny, nz, (int64_t)nx * ny * nz};
+        s->st_grid = (int)std::max<int64_t>(
+            1, std::min<int64_t>(ceil_div<int64_t>(s->st_g.n, ST_TILE), (int64_t)sm_count() * St27Coef<float>::ctas_per_sm));
+    }
+    s->st_S = S;
+    if (s->exec_while) cudaGraphExecDestroy(s->exec_while);
+    if (s->exec_init) cudaGraphExecDestroy(s->exec_init);
+    if (s->exec_chunk) cudaGraphExecDestroy(s->exec_chunk);
+    s->exec_while = s->exec_init = s->exec_chunk = nullptr;
+    s->chunk_iters = 0;
     return GB_OK;
 }

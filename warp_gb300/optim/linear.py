@@ -800,6 +800,18 @@ class BiCGSTAB(LinearSolverState):
         return it, math.sqrt(rr), atol_v
 
 
+def _fine_stencil(M, Aop):
+    """(dims, S) of a multigrid preconditioner's fine level when it is Aop's matrix in stencil form."""
+    levels = getattr(M, "levels", None)
+    bsr = getattr(Aop, "_bsr", None)
+    if not levels or bsr is None:
+        return None
+    lv = levels[0]
+    if getattr(lv, "S", None) is None or lv.A is not bsr or bsr.block_shape != (1, 1) or len(lv.dims) != 3:
+        return None
+    return lv.dims, lv.S
+
+
 class FCG(LinearSolverState):
     """Flexible CG, FCG(1) (Notay's truncated variant): each new direction z = M(r) is
     A-orthogonalised against the previous direction only, so M may change from one application to
@@ -814,7 +826,12 @@ class FCG(LinearSolverState):
     _kind = N.KRYLOV_FCG
 
     def __init__(self, A_, b, x, tol=None, atol=None, maxiter=0, M=None, callback=None, check_every=10,
-                 use_cuda_graph=True, stagnation_window: int = 25, stagnation_factor: float = 0.9):
+                 use_cuda_graph=True, stagnation_window: int = 25, stagnation_factor: float = 0.9,
+                 stencil=None):
+        """``stencil``: optional ``(dims, S)`` -- the 27-point stencil form (``gb_st27_build``, fp32) of the
+        same 1x1 matrix on a node grid of ``dims``; the product of every iteration then reads it
+        (120 B per node) instead of the CSR form.  ``stencil="auto"`` takes it from a
+        ``MultigridPreconditioner`` M whose fine level is this matrix in stencil form."""
         if M is None or not hasattr(M, "launch"):
             raise ValueError("FCG needs a preconditioner object with launch(stream, r_ptr, z_ptr)")
         self._precond_obj = M
@@ -824,6 +841,14 @@ class FCG(LinearSolverState):
             raise ValueError("FCG needs a BSR operator with 1x1/3x3 fp32 blocks and fp32 vectors")
         self._M = None
         self._install_precond(M)
+        if stencil == "auto":
+            stencil = _fine_stencil(M, self._A)
+        self.stencil_product = stencil is not None
+        if stencil is not None:
+            dims, S = stencil
+            self._stencil_keep = S
+            N.check(N.lib().gb_krylov_set_stencil(self._native, int(dims[0]), int(dims[1]), int(dims[2]), A.ptr(S)),
+                    "krylov_set_stencil")
 
     def _install_precond(self, M):
         import traceback
@@ -944,12 +969,15 @@ class RefinedSolver:
     ||b - A x|| / ||b|| in FP64.  The inner tolerance adapts: the first step uses ``inner_tol``,
     later steps ask only for the reduction still missing (x 1/4 margin), never below
     ``inner_tol``.  ``inner_values`` (e.g. a bfloat16 copy) replaces the matrix values in the
-    inner loop only.
+    inner loop only.  ``persistent``: the inner CG as one persistent cooperative launch (``CG``).
+    ``stencil_product``: with ``method="fcg"`` and a multigrid preconditioner whose fine level holds
+    this matrix in 27-point stencil form, the flexible solver's product reads the stencil form.
     """
 
     def __init__(self, Am: sparse.BsrMatrix, M: LinearOperator | None = None, method: str = "cg",
                  inner_tol: float = 1e-5, inner_maxiter: int = 0, inner_values: torch.Tensor | None = None,
-                 residual: str = "df32", use_cuda_graph: bool = True, persistent: bool = True):
+                 residual: str = "df32", use_cuda_graph: bool = True, persistent: bool = True,
+                 stencil_product: bool = True):
         self.A = Am
         self.M = M
         self.n = Am.nrow * Am.block_shape[0]
@@ -973,7 +1001,7 @@ class RefinedSolver:
                                                                                    use_cuda_graph=False)
         if method == "fcg":
             self.inner = FCG(self._inner_A, self._r32, self._d, tol=self.inner_tol, atol=0.0,
-                             maxiter=self.inner_maxiter, M=M, **loop)
+                             maxiter=self.inner_maxiter, M=M, stencil="auto" if stencil_product else None, **loop)
             # Jacobi-CG: the fallback when the flexible solve stagnates
             self._jacobi_M = preconditioner(self._inner_A, "diag")
             self._jacobi = CG(self._inner_A, self._r32, self._d, tol=self.inner_tol, atol=0.0,
