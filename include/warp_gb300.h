@@ -238,6 +238,12 @@ int gb_st27_apply(int mode, int nx, int ny, int nz, const float* S, const float*
                   float omega, float* w_out, float* out, int* status, gb_stream_t stream);
 /* bf16 copy of S (28 values per node, the last zero; gb_st27_bytes_bf16, 16-byte aligned) and the same
  * three passes reading it, with fp32 accumulation. */
+/* r = b - A x on the stencil form S of a 1x1 matrix, x as interleaved (hi, lo) fp32 pairs, double-float
+ * arithmetic: gb_residual_df's outputs (r64 / r32 may be null; norms = ||r||^2, ||b||^2) and workspace
+ * (gb_residual_f64_workspace_bytes; its first 256 bytes an arrival counter, zero before the first call). */
+int gb_residual_df_st27(int nx, int ny, int nz, const float* S, const void* x2, const float* b, double* r64,
+                        float* r32, double* norms, void* workspace, size_t workspace_bytes, int* status,
+                        gb_stream_t stream);
 size_t gb_st27_bytes_bf16(int nx, int ny, int nz);
 int gb_st27_to_bf16(int nx, int ny, int nz, const float* S, void* Sb, gb_stream_t stream);
 int gb_st27_apply_bf16(int mode, int nx, int ny, int nz, const void* Sb, const float* w, const float* r,

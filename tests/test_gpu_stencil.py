@@ -285,3 +285,51 @@ def test_fcg_stencil_rejects_mismatched_grid(cuda):
     assert N.lib().gb_krylov_set_stencil(solver._native, 9, 9, 10, S.data_ptr()) != 0  # 810 nodes, not 729
     assert N.lib().gb_krylov_set_stencil(solver._native, 9, 9, 9, S.data_ptr()) == 0
     assert N.lib().gb_krylov_set_stencil(solver._native, 0, 0, 0, None) == 0
+
+
+def test_residual_df_on_stencil_matches_fp64(cuda):
+    """gb_residual_df_st27 against the FP64 oracle product on the same fp32 values (the double-float
+    tolerance of gb_residual_df) and against gb_residual_df on the CSR form."""
+    from warp_gb300 import _native as N
+
+    s = _system((14, 12, 16), seed=21)
+    dims = (15, 13, 17)
+    n, off, col, val = _csr(s.A)
+    L = N.lib()
+    S = torch.empty(int(L.gb_st27_bytes(*dims)) // 4, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    N.check(L.gb_st27_build(*dims, s.A.offsets.data_ptr(), s.A.columns.data_ptr(), s.A.values.data_ptr(),
+                            S.data_ptr(), status.data_ptr(), 0))
+    rng = np.random.default_rng(8)
+    x64 = rng.standard_normal(n)
+    b = rng.standard_normal(n).astype(np.float32)
+    hi = x64.astype(np.float32)
+    lo = (x64 - hi.astype(np.float64)).astype(np.float32)
+    x2 = torch.from_numpy(np.stack([hi, lo], 1).reshape(-1).copy()).cuda()
+    bd = torch.from_numpy(b).cuda()
+    ws = torch.zeros(int(L.gb_residual_f64_workspace_bytes(1, n, len(val), N.GB_F32)), dtype=torch.uint8, device="cuda")
+    out = {}
+    for kind in ("st27", "csr"):
+        r64 = torch.zeros(n, dtype=torch.float64, device="cuda")
+        r32 = torch.zeros(n, dtype=torch.float32, device="cuda")
+        norms = torch.zeros(2, dtype=torch.float64, device="cuda")
+        if kind == "st27":
+            N.check(L.gb_residual_df_st27(*dims, S.data_ptr(), x2.data_ptr(), bd.data_ptr(), r64.data_ptr(),
+                                          r32.data_ptr(), norms.data_ptr(), ws.data_ptr(), ws.numel(),
+                                          status.data_ptr(), 0))
+        else:
+            N.check(L.gb_residual_df(1, n, len(val), s.A.capacity, s.A.offsets.data_ptr(), None,
+                                     s.A.columns.data_ptr(), s.A.values.data_ptr(), N.GB_F32, x2.data_ptr(),
+                                     bd.data_ptr(), r64.data_ptr(), r32.data_ptr(), norms.data_ptr(), ws.data_ptr(),
+                                     ws.numel(), status.data_ptr(), 0))
+        torch.cuda.synchronize()
+        out[kind] = (r64.cpu().numpy(), r32.cpu().numpy(), norms.cpu().numpy())
+    assert int(status.item()) == 0
+    exact = b.astype(np.float64) - _matvec(off, col, val, x64)
+    scale = _matvec(off, col, np.abs(val), np.abs(x64)) + np.abs(b)
+    for kind, (r64, r32, norms) in out.items():
+        assert np.all(np.abs(r64 - exact) <= 1e-11 * scale), kind
+        np.testing.assert_allclose(r32, exact.astype(np.float32), rtol=2e-7, atol=1e-12 * scale.max())
+        np.testing.assert_allclose(norms[0], np.dot(r32.astype(np.float64), r32), rtol=1e-5)
+        np.testing.assert_allclose(norms[1], np.dot(b.astype(np.float64), b), rtol=1e-5)
+    np.testing.assert_allclose(out["st27"][2], out["csr"][2], rtol=1e-6)

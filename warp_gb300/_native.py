@@ -83,6 +83,7 @@ _SIGNATURES = {
     "gb_st27_build": (_c_int, [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gb_st27_apply": (_c_int, [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, ctypes.c_float, _vp, _vp, _vp, _vp]),
     "gb_st27_bytes_bf16": (_c_sz, [_c_int, _c_int, _c_int]),
+    "gb_residual_df_st27": (_c_int, [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _c_sz, _vp, _vp]),
     "gb_st27_to_bf16": (_c_int, [_c_int, _c_int, _c_int, _vp, _vp, _vp]),
     "gb_st27_apply_bf16": (_c_int, [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, ctypes.c_float, _vp, _vp, _vp,
                                     _vp]),

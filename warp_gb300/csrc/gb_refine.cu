@@ -176,7 +176,7 @@ GB_API size_t gb_residual_f64_workspace_bytes(int block_dim, int nrow, int64_t n
 //   mode 0: x2 = interleaved (hi, lo) fp32 split of x, double-float arithmetic (fast path);
 //   mode 1: x = fp64 array, FP64 arithmetic (verification path).
 // Writes r64 and/or r32 (either may be null) and norms[0] = ||r||^2, norms[1] = ||b||^2 (device
-// doubles; accumulated per thread in fp32 and across threads in fp64).  The workspace's first 256
+// doubles; accumulated per thread in fp32 and across threads in double-float).  The workspace's first 256
 // bytes hold the arrival counter: zero before the first call, left zero by the kernel.
 GB_API int gb_residual_f64(int block_dim, int nrow, int64_t nnz, int64_t ncap, const int* offsets,
                            const int* row_counts, const int* columns, const void* values, int val_dtype,

@@ -33,6 +33,7 @@
 #include "gb_common.cuh"
 #include "gb_spmv.cuh"  // sm_count()
 #include "gb_st27.cuh"
+#include "gb_df32.cuh"
 
 namespace gb {
 
@@ -149,6 +150,91 @@ __global__ void __launch_bounds__(ST_TILE) k_st27_apply(St27Grid g, const CT* __
         }
         __syncthreads();
     }
+}
+
+// The refinement's true residual on the stencil form: r = b - A x with x given as (hi, lo) fp32
+// pairs and double-float products and sums (the arithmetic of gb_refine.cu's k_resid_df), r32 = the
+// residual rounded to fp32 (and r64 in FP64, if asked), norms = ||r||^2, ||b||^2.  Staging as
+// k_st27_apply.
+__global__ void __launch_bounds__(ST_TILE) k_st27_resid_df(St27Grid g, const float* __restrict__ S,
+                                                           const float2* __restrict__ x2, const float* __restrict__ b,
+                                                           double* r64, float* r32, double* norms, double* partials,
+                                                           unsigned int* counter, int* status)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ double s_red[64];
+    pdl_enter();
+    constexpr size_t STAGE = st27_stage_bytes<float>();
+    float* ring = reinterpret_cast<float*>(smem);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + ST_STAGES * STAGE);
+    const int64_t ntiles = (g.n + ST_TILE - 1) / ST_TILE;
+    const int64_t npad = st27_padded_nodes(g.n);
+    auto issue = [&](int64_t tile, int s) {
+        const int64_t i0 = tile * ST_TILE;
+        const int64_t cnt = npad - i0 < ST_TILE ? npad - i0 : ST_TILE;
+        const uint32_t bytes = (uint32_t)(cnt * 27 * sizeof(float));
+        mbar_arrive_expect_tx(&full[s], bytes);
+        bulk_g2s(ring + (size_t)s * ST_TILE * 27, S + i0 * 27, bytes, &full[s]);
+    };
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < ST_STAGES; ++s) mbar_init(&full[s], 1);
+        fence_mbar_init();
+        for (int s = 0; s < ST_STAGES; ++s)
+            if (blockIdx.x + (int64_t)s * gridDim.x < ntiles) issue(blockIdx.x + (int64_t)s * gridDim.x, s);
+    }
+    __syncthreads();
+    const int64_t yz = (int64_t)g.ny * g.nz;
+    float rr = 0.f, bb = 0.f;
+    int it = 0;
+    int64_t tile = blockIdx.x;
+    for (; tile < ntiles; tile += gridDim.x, ++it) {
+        const int s = it % ST_STAGES;
+        if (!__syncthreads_and(mbar_wait_bounded(&full[s], (uint32_t)(it / ST_STAGES) & 1u))) break;
+        const int64_t i = tile * ST_TILE + threadIdx.x;
+        if (i < g.n) {
+            float c[27];
+            st27_load_coefs(ring + (size_t)s * ST_TILE * 27 + threadIdx.x * 27, c);
+            int x, y, z;
+            st27_coords(g, i, x, y, z);
+            const bool okx[3] = {x > 0, true, x < g.nx - 1};
+            const bool oky[3] = {y > 0, true, y < g.ny - 1};
+            const bool okz[3] = {z > 0, true, z < g.nz - 1};
+            df32 acc;
+#pragma unroll
+            for (int k = 0; k < 27; ++k) {
+                const int dx = k / 9 - 1, dy = (k / 3) % 3 - 1, dz = k % 3 - 1;
+                if (okx[dx + 1] && oky[dy + 1] && okz[dz + 1]) {
+                    const float2 xv = __ldg(x2 + i + dx * yz + (int64_t)dy * g.nz + dz);
+                    acc += df32(c[k], 0.f) * df32(xv.x, xv.y);
+                }
+            }
+            const float bi = b[i];
+            const df32 ri = df32(bi, 0.f) + (-acc);
+            const float r = ri.hi + ri.lo;
+            if (r64) r64[i] = (double)ri.hi + (double)ri.lo;
+            if (r32) r32[i] = r;
+            rr += r * r;
+            bb += bi * bi;
+        }
+        __syncthreads();  // stage s is read: refill it
+        if (threadIdx.x == 0 && tile + (int64_t)ST_STAGES * gridDim.x < ntiles)
+            issue(tile + (int64_t)ST_STAGES * gridDim.x, s);
+    }
+    if (tile < ntiles) {
+        if (threadIdx.x == 0) {
+            for (int q = 0; q < ST_STAGES; ++q) {
+                const int64_t tq = tile + (int64_t)q * gridDim.x;
+                if (tq < ntiles) mbar_wait_bounded(&full[(it + q) % ST_STAGES], (uint32_t)((it + q) / ST_STAGES) & 1u);
+            }
+            atomicOr(status, GB_DEV_WAIT_TIMEOUT);
+        }
+        __syncthreads();
+    }
+    float v[2] = {rr, bb};
+    grid_reduce_df<2>(v, partials, counter, s_red, [&](const double (&t)[2]) {
+        norms[0] = t[0];
+        norms[1] = t[1];
+    });
 }
 
 // S (fp32, 27 per node) -> Sb (bf16, 28 per node, the 28th zero), round to nearest even
@@ -269,4 +355,32 @@ GB_API int gb_st27_apply_bf16(int mode, int nx, int ny, int nz, const void* Sb, 
     GB_REQUIRE(g.n < (int64_t(1) << 31), "st27_apply_bf16: grid too large");
     return st27_apply_t<__nv_bfloat16>(mode, g, static_cast<const __nv_bfloat16*>(Sb), w, r, dinv, omega, w_out, out,
                                        status, stream);
+}
+
+// r = b - A x on the stencil form S (fp32, gb_st27_build) of a 1x1 matrix on an nx x ny x nz node
+// grid, x given as interleaved (hi, lo) fp32 pairs, double-float arithmetic: the stencil counterpart of
+// gb_residual_df (same outputs; the workspace of gb_residual_f64_workspace_bytes, first 256 bytes the
+// arrival counter, zero before the first call and left zero).
+GB_API int gb_residual_df_st27(int nx, int ny, int nz, const float* S, const void* x2, const float* b, double* r64,
+                               float* r32, double* norms, void* workspace, size_t workspace_bytes, int* status,
+                               cudaStream_t stream)
+{
+    GB_REQUIRE(nx >= 1 && ny >= 1 && nz >= 1 && S && x2 && b && norms && workspace && status,
+               "residual_df_st27: null argument");
+    GB_REQUIRE((uintptr_t)S % 16 == 0, "residual_df_st27: S must be 16-byte aligned");
+    const St27Grid g{nx, ny, nz, (int64_t)nx * ny * nz};
+    GB_REQUIRE(g.n < (int64_t(1) << 31), "residual_df_st27: grid too large");
+    const int grid = st27_apply_grid<float>(g.n);
+    GB_REQUIRE(workspace_bytes >= 256 + sizeof(double) * 2 * (size_t)grid, "residual_df_st27: workspace too small");
+    static bool attr_set = false;
+    if (!attr_set) {
+        GB_CHECK_CUDA(cudaFuncSetAttribute(k_st27_resid_df, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)st27_smem<float>()));
+        attr_set = true;
+    }
+    unsigned int* counter = static_cast<unsigned int*>(workspace);
+    double* partials = reinterpret_cast<double*>(static_cast<unsigned char*>(workspace) + 256);
+    GB_CHECK_CUDA(launch_pdl(k_st27_resid_df, grid, ST_TILE, st27_smem<float>(), stream, g, S,
+                             static_cast<const float2*>(x2), b, r64, r32, norms, partials, counter, status));
+    return GB_OK;
 }

@@ -970,8 +970,9 @@ class RefinedSolver:
     later steps ask only for the reduction still missing (x 1/4 margin), never below
     ``inner_tol``.  ``inner_values`` (e.g. a bfloat16 copy) replaces the matrix values in the
     inner loop only.  ``persistent``: the inner CG as one persistent cooperative launch (``CG``).
-    ``stencil_product``: with ``method="fcg"`` and a multigrid preconditioner whose fine level holds
-    this matrix in 27-point stencil form, the flexible solver's product reads the stencil form.
+    ``stencil_product``: with a multigrid preconditioner whose fine level holds this matrix in 27-point
+    stencil form, the true residual (and, with ``method="fcg"``, the flexible solver's product) reads
+    the stencil form.
     """
 
     def __init__(self, Am: sparse.BsrMatrix, M: LinearOperator | None = None, method: str = "cg",
@@ -1024,6 +1025,9 @@ class RefinedSolver:
         self._host = torch.zeros(2, dtype=torch.float64, pin_memory=True)
         self._x_backup = None
         self.kernel_launches = 0
+        # the true residual on the multigrid fine level's stencil form of the same matrix, when it has one
+        self._res_stencil = (_fine_stencil(M, aslinearoperator(Am)) if stencil_product and residual == "df32"
+                             else None)
 
     def residual(self, x64: torch.Tensor, b: torch.Tensor, sync: bool = True):
         """True residual (written as the fp32 right-hand side of the next correction solve)."""
@@ -1034,6 +1038,11 @@ class RefinedSolver:
                                       A.ptr(Am.columns), A.ptr(Am.values), A.gb_dtype(Am.values.dtype), A.ptr(x64),
                                       A.ptr(b), None, A.ptr(self._r32), A.ptr(self._norms), self._res_ws.data_ptr(),
                                       self._res_ws.numel(), A.ptr(self._status), A.stream()), "residual_f64")
+        elif self._res_stencil is not None:
+            dims, S = self._res_stencil
+            N.check(L.gb_residual_df_st27(*dims, A.ptr(S), A.ptr(self._x2), A.ptr(b), None, A.ptr(self._r32),
+                                          A.ptr(self._norms), self._res_ws.data_ptr(), self._res_ws.numel(),
+                                          A.ptr(self._status), A.stream()), "residual_df_st27")
         else:
             N.check(L.gb_residual_df(Am.block_shape[0], Am.nrow, Am.nnz, Am.capacity, A.ptr(Am.offsets), None,
                                      A.ptr(Am.columns), A.ptr(Am.values), A.gb_dtype(Am.values.dtype),
