@@ -960,7 +960,9 @@ def main():
         "config": {"workload": WORKLOAD, "solver": "learned_fcg_refined", "n_dofs": n, "nnz": nnz,
                    "parallelism": f"replicas{ws}", "l2": "inputs > L2 (matrix 204 MB vs 129 MB L2), no flush",
                    "inner_tol": args.inner_tol, "weights": os.path.relpath(args.weights, ROOT),
-                   "mg_levels": lmg.describe(), "vcycle_fine_values": VCYCLE_FINE},
+                   "mg_levels": lmg.describe(), "vcycle_fine_values": VCYCLE_FINE,
+                   "fcg_product": "27-point stencil form of A (fp32)" if lsolver.inner.stencil_product else "CSR",
+                   "jacobi_cg": "persistent cooperative launch" if jsolver.inner.persistent_active else "three kernels"},
         "roofline": {"bound": "hbm", "kernel": "k_bsr_mv<1,1,float>", "achieved": mv_gbs, "peak": hbm_peak,
                      "unit": "GB/s", "frac": mv_gbs / hbm_peak, "peak_kind": peak_kind,
                      "algorithmic_bytes": mv_bytes, "traffic": traffic, "launch_us": mv_s * 1e6,
