@@ -31,8 +31,8 @@
 // A work item is one output x-plane of a column of TC_SUB = 2 windows (252 output rows); a CTA walks
 // x through a contiguous range of items, so each input x-plane block (both planes, rows
 // [q0 - sy, q0 + sy + 126 + 128)) is copied once with 1-D bulk copies into a ring of slots.  Warp
-// roles: a copy warp, one MMA-issuing warp per window (3 dy MMAs per input plane on the window's
-// chunk ring), and two groups of four epilogue warps per window (one warp per TMEM lane quarter;
+// roles: a copy warp, two MMA-issuing warps per window (alternate input planes; 3 dy MMAs per input
+// plane on the window's chunk ring), and two groups of four epilogue warps per window (one warp per TMEM lane quarter;
 // the groups take alternate output planes) that read a finished chunk with tcgen05.ld, sum the dz
 // taps, apply ReLU and store bf16 rows of interior voxels -- or, for the last layer, write
 // w[v] = omega dinv[v] r[v] + (mask[v] ? 0 : out[v][0]) in fp32 (the Jacobi step fused; for vec3
@@ -52,7 +52,8 @@ constexpr int TC_SUB = 2;                  // windows per work item (252 output 
 constexpr int TC_CHUNK = 48;               // TMEM columns of one (window, output plane): 3 dz x 16 co
 constexpr int TC_RING = 5;                 // output planes in flight per window (chunk ring)
 constexpr int TC_N = 3 * TC_CHUNK;         // 144 = 3 dx x 3 dz x 16 co (UMMA N of a full MMA)
-constexpr int TC_ISSUERS = TC_SUB;         // one MMA-issuing warp per window
+constexpr int TC_ISSUE_PAR = 2;            // MMA-issuing threads per window: alternate input planes
+constexpr int TC_ISSUERS = TC_SUB * TC_ISSUE_PAR;
 constexpr int TC_EPI_PAR = 2;              // epilogue groups per window: items drained alternately
 constexpr int TC_EPI_GROUPS = TC_SUB * TC_EPI_PAR;  // groups of 4 warps (one per TMEM lane quarter)
 constexpr int TC_EPI_WARP0 = 1 + TC_ISSUERS;  // warp 0 copies, warps 1..TC_ISSUERS issue MMAs, then the epilogue
@@ -227,10 +228,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
     if (threadIdx.x == 0) {
         for (int s = 0; s < NS; ++s) {
             mbar_init(&full[s], 1);
-            mbar_init(&empty[s], TC_ISSUERS);
+            mbar_init(&empty[s], TC_SUB);  // an input plane is read by one issuer per window
         }
         for (int a = 0; a < TC_RING; ++a) {
-            mbar_init(&accfull[a], TC_ISSUERS);
+            mbar_init(&accfull[a], TC_ISSUERS);  // per window: the last contribution of each issuer
             mbar_init(&accempty[a], 4 * TC_SUB);  // the 4 warps of each window's group draining the plane
         }
         mbar_init(done, TC_ISSUERS);
@@ -303,9 +304,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
             }
         }
     } else if (warp <= TC_ISSUERS) {
-        // ---------- MMA warps: warp 1 + j issues window j's 3 dy MMAs for every input plane -----------
+        // ---------- MMA warps: warp 1 + u issues, for window u % TC_SUB, the 3 dy MMAs of the input
+        // planes of parity u / TC_SUB (counted from the run's first input plane) ---------------------
+        // Two threads accumulate into the same window's chunks (the tensor pipe executes one SM's
+        // MMAs in order).  Output plane P receives input planes P - 1, P + 1 from one issuer and P
+        // from the other, so each issuer commits accfull[P] after its last contribution to P: at
+        // input P (its own parity) and at input P + 1 (the other parity) -- TC_ISSUERS arrivals
+        // per plane.  An issuer waits for a chunk to be drained before it first writes it; the chunk
+        // of plane xi was first written by the other issuer (input xi - 1), so the issuer of input xi
+        // waits on planes xi and xi + 1 (the wait on an already completed phase returns at once).
         if (lane == 0) {
-            const int j = warp - 1;
+            const int u = warp - 1;
+            const int j = u % TC_SUB, par = u / TC_SUB;
             const uint32_t wbase = smem_u32(wsm);
             const uint32_t rbase = smem_u32(ring);
             const uint32_t dwin = tmem + (uint32_t)j * TC_WIN_COLS;
@@ -317,15 +327,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
                 const int x0 = (int)(k % c.nx) + 1;
                 const int64_t run_end = min(k_end, (int64_t)(o + 1) * c.nx);
                 const int x1 = (int)((run_end - 1) % c.nx) + 1;
-                for (int xi = x0 - 1; xi <= x1 + 1; ++xi) {
+                for (int xi = x0 - 1 + par; xi <= x1 + 1; xi += TC_ISSUE_PAR) {
                     const int q = q0 + (xi - x0 + 1);
-                    // output planes this input feeds inside the run, and whether the last of them is
-                    // touched for the first time (its chunk must have been drained and zeroed)
+                    // output planes this input feeds inside the run; the chunks of planes lo..hi must
+                    // be free before this thread's first write to each
                     const int lo = max(x0, xi - 1), hi = min(x1, xi + 1);
-                    const bool fresh = (hi == xi + 1) || (xi == x0 - 1);
                     ok = tc_wait(&full[q % NS], (q / NS) & 1, s_abort);
-                    if (ok && fresh) {
-                        const int sh = it0 + (hi - x0);
+                    for (int pl = max(lo, xi); ok && pl <= hi; ++pl) {
+                        const int sh = it0 + (pl - x0);
                         ok = tc_wait(&accempty[sh % TC_RING], (sh / TC_RING) & 1, s_abort);
                     }
                     if (!ok) {
@@ -348,8 +357,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
                             tc_mma(dwin, adesc, umma_desc(b0 + (uint32_t)(n1 * TC_CHUNK * 16), TC_WB_KHALF, 128),
                                    tc_idesc((np - n1) * TC_CHUNK), 1u);
                     }
-                    tc_commit(&empty[q % NS]);  // the block is not read again
-                    if (xi - 1 >= x0) tc_commit(&accfull[(it0 + (xi - 1 - x0)) % TC_RING]);  // plane xi - 1 done
+                    tc_commit(&empty[q % NS]);  // the block is not read again by this thread
+                    // this thread's last contributions: plane xi - 1 (other parity) and plane xi (own)
+                    if (xi - 1 >= x0 && xi - 1 <= x1) tc_commit(&accfull[(it0 + (xi - 1 - x0)) % TC_RING]);
+                    if (xi >= x0 && xi <= x1) tc_commit(&accfull[(it0 + (xi - x0)) % TC_RING]);
                 }
                 it0 += (int)(run_end - k);
                 q0 += (int)(run_end - k) + 2;
