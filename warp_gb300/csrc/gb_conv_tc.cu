@@ -36,7 +36,8 @@
 // the groups take alternate output planes) that read a finished chunk with tcgen05.ld, sum the dz
 // taps, apply ReLU and store bf16 rows of interior voxels -- or, for the last layer, write
 // w[v] = omega dinv[v] r[v] + (mask[v] ? 0 : out[v][0]) in fp32 (the Jacobi step fused; for vec3
-// fields the node's three dofs from output channels 0..2) -- then zero the chunk with tcgen05.st.
+// fields the node's three dofs from output channels 0..2).  A chunk is zeroed with tcgen05.st and
+// handed back to the issuers as soon as its values are in registers, before the exchange and stores.
 // Every wait is bounded (globaltimer); a timeout sets GB_DEV_WAIT_TIMEOUT, the CTA drains its own
 // copies and MMAs (bounded) and frees its TMEM before returning.
 #include "gb_bulk.cuh"
@@ -432,6 +433,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
                     zp[q] = tc_ld1(taddr + 32 + q);
                 }
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                // the values are in registers: zero the chunk for the plane TC_RING items later and give
+                // it back to the MMA issuers before the exchange and the stores
+#pragma unroll
+                for (int h = 0; h < 3; ++h) tc_st16_zero(taddr + (uint32_t)(16 * h));
+                asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive1(&accempty[a]);
 #pragma unroll
                 for (int q = 0; q < NOUT; ++q) {
                     if (lane == 31) xb[(quarter * 2 + 0) * 16 + q] = zm[q];
@@ -458,6 +467,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
                 tc_ld16(taddr + 16, z0);
                 tc_ld16(taddr + 32, zp);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                // the values are in registers: zero the chunk for the plane TC_RING items later and give
+                // it back to the MMA issuers before the exchange and the stores
+#pragma unroll
+                for (int h = 0; h < 3; ++h) tc_st16_zero(taddr + (uint32_t)(16 * h));
+                asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+                tc_fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive1(&accempty[a]);
                 float4* lo_dst = reinterpret_cast<float4*>(xb + (quarter * 2 + 0) * 16);
                 float4* hi_dst = reinterpret_cast<float4*>(xb + (quarter * 2 + 1) * 16);
                 if (lane == 31) {
@@ -505,14 +522,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) k_conv3_tc(const TcConv c)
                     *reinterpret_cast<uint4*>(c.out + (c.plane_rows + pr) * 16) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
                 }
             }
-            // the chunk starts the plane TC_RING items later at zero
-#pragma unroll
-            for (int h = 0; h < 3; ++h) tc_st16_zero(taddr + (uint32_t)(16 * h));
-            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
             xp ^= 1;
-            tc_fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive1(&accempty[a]);
         }
     }
 
