@@ -550,12 +550,12 @@ __global__ void k_features_planar(int ncomp, int nx, int ny, int nz, int64_t pla
                                   const float* __restrict__ mask, unsigned char* __restrict__ out)
 {
     pdl_enter();
-    const int64_t n = (int64_t)nx * ny * nz;
-    const int64_t sy = nz + 2, sx = (int64_t)(ny + 2) * sy;
-    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
-        const int x = (int)(v / ((int64_t)ny * nz));
-        const int y = (int)((v / nz) % ny);
-        const int z = (int)(v % nz);
+    // 3-D launch: 32 z-consecutive nodes x 8 y-rows per block, one x-plane per grid z index
+    const int z = (int)(blockIdx.x * blockDim.x + threadIdx.x), y = (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int x = (int)blockIdx.z;
+    if (z < nz && y < ny) {
+        const int64_t sy = nz + 2, sx = (int64_t)(ny + 2) * sy;
+        const int64_t v = ((int64_t)x * ny + y) * nz + z;
         const int64_t p = (x + 1) * sx + (y + 1) * sy + (z + 1);
         float f[16];
         net_node_features(ncomp, v, r, dinv, chat, mask, f);
@@ -589,9 +589,10 @@ GB_API int gb_net_features_planar(int ncomp, int nx, int ny, int nz, const float
     GB_REQUIRE(ncomp == 1 || ncomp == 3, "net_features_planar: ncomp must be 1 or 3");
     if (n <= 0) return GB_OK;
     GB_REQUIRE((uintptr_t)out % 16 == 0, "net_features_planar: output must be 16-byte aligned");
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div<int64_t>(n, 256), kSmCount * 16));
-    GB_CHECK_CUDA(launch_pdl(k_features_planar, grid, 256, 0, stream, ncomp, nx, ny, nz, planar_rows(nx, ny, nz), r,
-                             dinv, chat, mask, static_cast<unsigned char*>(out)));
+    GB_REQUIRE(nx <= 65535, "net_features_planar: grid too long in x");
+    const dim3 grid((unsigned)ceil_div(nz, 32), (unsigned)ceil_div(ny, 8), (unsigned)nx);
+    GB_CHECK_CUDA(launch_pdl(k_features_planar, grid, dim3(32, 8, 1), 0, stream, ncomp, nx, ny, nz,
+                             planar_rows(nx, ny, nz), r, dinv, chat, mask, static_cast<unsigned char*>(out)));
     return GB_OK;
 }
 

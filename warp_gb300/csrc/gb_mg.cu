@@ -32,12 +32,11 @@ __global__ void k_restrict_fw(NodeGrid fg, NodeGrid cg, const float* __restrict_
                               const float* __restrict__ cmask, float* __restrict__ rc)
 {
     pdl_enter();
-    const int64_t n = (int64_t)cg.nx * cg.ny * cg.nz;
-    const int64_t I = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (I >= n) return;
-    const int X = (int)(I / ((int64_t)cg.ny * cg.nz));
-    const int Y = (int)((I / cg.nz) % cg.ny);
-    const int Z = (int)(I % cg.nz);
+    // 3-D launch (tgrid3): no index division
+    const int Z = (int)(blockIdx.x * blockDim.x + threadIdx.x), Y = (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int X = (int)blockIdx.z;
+    if (Z >= cg.nz || Y >= cg.ny) return;
+    const int64_t I = nidx(cg, X, Y, Z);
     const bool cmasked = cmask && __ldg(cmask + I) != 0.f;
     float s[C];
 #pragma unroll
@@ -81,13 +80,12 @@ __global__ void k_prolong_add(NodeGrid fg, NodeGrid cg, const float* __restrict_
                               float scale, float* __restrict__ z)
 {
     pdl_enter();
-    const int64_t n = (int64_t)fg.nx * fg.ny * fg.nz;
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+    // 3-D launch (tgrid3): no index division
+    const int zz = (int)(blockIdx.x * blockDim.x + threadIdx.x), y = (int)(blockIdx.y * blockDim.y + threadIdx.y);
+    const int x = (int)blockIdx.z;
+    if (zz >= fg.nz || y >= fg.ny) return;
+    const int64_t i = nidx(fg, x, y, zz);
     const bool masked = fmask && __ldg(fmask + i) != 0.f;
-    const int x = (int)(i / ((int64_t)fg.ny * fg.nz));
-    const int y = (int)((i / fg.nz) % fg.ny);
-    const int zz = (int)(i % fg.nz);
     const int xs[2] = {x >> 1, min((x + 1) >> 1, cg.nx - 1)};
     const int ys[2] = {y >> 1, min((y + 1) >> 1, cg.ny - 1)};
     const int zs[2] = {zz >> 1, min((zz + 1) >> 1, cg.nz - 1)};
@@ -145,6 +143,12 @@ __global__ void k_coarsen_cells(int fx, int fy, int fz, const float* __restrict_
 
 static int grid1(int64_t n) { return (int)std::max<int64_t>(1, ceil_div<int64_t>(n, 256)); }
 
+// 3-D launch over an nx x ny x nz node grid: 32 z-consecutive nodes x 8 y-rows per block, one x-plane
+// per grid z index (coalesced along z, no division for the coordinates)
+constexpr int TG3_Z = 32, TG3_Y = 8;
+static dim3 tgrid3(const NodeGrid& g) { return dim3(ceil_div(g.nz, TG3_Z), ceil_div(g.ny, TG3_Y), g.nx); }
+static dim3 tblock3() { return dim3(TG3_Z, TG3_Y, 1); }
+
 }  // namespace gb
 
 using namespace gb;
@@ -157,11 +161,11 @@ GB_API int gb_mg_restrict_c(int ncomp, int fnx, int fny, int fnz, int cnx, int c
     GB_REQUIRE(cnx == (fnx + 1) / 2 && cny == (fny + 1) / 2 && cnz == (fnz + 1) / 2, "mg_restrict: grid mismatch");
     GB_REQUIRE(ncomp == 1 || ncomp == 3, "mg_restrict: 1 or 3 components");
     NodeGrid fg{fnx, fny, fnz}, cg{cnx, cny, cnz};
-    const int grid = grid1((int64_t)cnx * cny * cnz);
+    GB_REQUIRE(cnx <= 65535, "mg_restrict: grid too long in x");
     if (ncomp == 1)
-        GB_CHECK_CUDA(launch_pdl(k_restrict_fw<1>, grid, 256, 0, stream, fg, cg, r, fmask, cmask, rc));
+        GB_CHECK_CUDA(launch_pdl(k_restrict_fw<1>, tgrid3(cg), tblock3(), 0, stream, fg, cg, r, fmask, cmask, rc));
     else
-        GB_CHECK_CUDA(launch_pdl(k_restrict_fw<3>, grid, 256, 0, stream, fg, cg, r, fmask, cmask, rc));
+        GB_CHECK_CUDA(launch_pdl(k_restrict_fw<3>, tgrid3(cg), tblock3(), 0, stream, fg, cg, r, fmask, cmask, rc));
     return GB_OK;
 }
 
@@ -171,11 +175,11 @@ GB_API int gb_mg_prolong_add_c(int ncomp, int fnx, int fny, int fnz, int cnx, in
     GB_REQUIRE(cnx == (fnx + 1) / 2 && cny == (fny + 1) / 2 && cnz == (fnz + 1) / 2, "mg_prolong: grid mismatch");
     GB_REQUIRE(ncomp == 1 || ncomp == 3, "mg_prolong: 1 or 3 components");
     NodeGrid fg{fnx, fny, fnz}, cg{cnx, cny, cnz};
-    const int grid = grid1((int64_t)fnx * fny * fnz);
+    GB_REQUIRE(fnx <= 65535, "mg_prolong: grid too long in x");
     if (ncomp == 1)
-        GB_CHECK_CUDA(launch_pdl(k_prolong_add<1>, grid, 256, 0, stream, fg, cg, zc, fmask, scale, z));
+        GB_CHECK_CUDA(launch_pdl(k_prolong_add<1>, tgrid3(fg), tblock3(), 0, stream, fg, cg, zc, fmask, scale, z));
     else
-        GB_CHECK_CUDA(launch_pdl(k_prolong_add<3>, grid, 256, 0, stream, fg, cg, zc, fmask, scale, z));
+        GB_CHECK_CUDA(launch_pdl(k_prolong_add<3>, tgrid3(fg), tblock3(), 0, stream, fg, cg, zc, fmask, scale, z));
     return GB_OK;
 }
 
