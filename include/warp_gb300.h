@@ -281,6 +281,15 @@ int gb_net_features_planar(int ncomp, int nx, int ny, int nz, const float* r, co
                            const float* mask, void* out, gb_stream_t stream);
 int gb_conv3_fwd_tc(int nx, int ny, int nz, int last, const void* in, const void* Wt, void* out, float* w,
                     const float* r, const float* dinv, const float* mask, float omega, int* status, gb_stream_t stream);
+/* The whole network (features, nlayers - 1 ReLU layers, the last layer into w as last = ncomp) in one
+ * cooperative launch: act[l] is layer l's planar input (act[0] the features), flags holds
+ * gb_convnet_tc_items() uint32 counters and epoch 2 uint32, all zero before the first launch and shared only
+ * by consecutive launches of the same nlayers on one stream.  GB_ERR_UNSUPPORTED (nothing launched) when the
+ * device cannot hold every CTA at once. */
+int64_t gb_convnet_tc_items(int nx, int ny, int nz);
+int gb_convnet_fwd_tc(int nx, int ny, int nz, int ncomp, int nlayers, void* const* act, const void* const* Wt,
+                      float* w, const float* r, const float* dinv, const float* chat, const float* mask, float omega,
+                      unsigned int* flags, unsigned int* epoch, int* status, gb_stream_t stream);
 
 /* Multi-column dot / axpy for GMRES's Gram-Schmidt steps (warp/_src/optim/linear.py:1653-1916 computes
  * them with TiledDot over the basis and _gmres_arnoldi_axpy_kernel): out[c] = V[c] . w (rows of V ldv

@@ -383,3 +383,61 @@ def test_vec3_training_gradient_matches_a_directional_difference(cuda):
     err = float((w16 - w32).norm() / w32.norm())
     assert err < 2e-2, err
     assert int(f.mg.status.item()) == 0
+
+
+@pytest.mark.parametrize("cells,vec3", [((8, 8, 8), False), ((40, 40, 40), False), ((31, 18, 47), False),
+                                        ((96, 96, 96), False), ((16, 16, 16), True)])
+def test_whole_network_launch_matches_layer_launches(cuda, cells, vec3):
+    """One cooperative launch of the features and the four layers writes, bit for bit, what the features
+    kernel and four layer launches write: over several launches sharing the counters (a new residual
+    each time) and inside a CUDA graph replayed twice."""
+    from warp_gb300 import learned, multigrid, problems
+
+    if vec3:
+        s = problems.elasticity(cells, sigma=1.0, corr_length=0.3, seed=4)
+    else:
+        s = problems.diffusion(cells, sigma=1.5, corr_length=0.2, seed=6)
+    net = learned.ConvNet(seed=3, ncomp=3 if vec3 else 1)
+    net.W[3] = (torch.randn(net.W[3].numel(), generator=torch.Generator().manual_seed(4)) * 0.05).cuda()
+    mg = multigrid.MultigridPreconditioner(s.A, s.geo, s.coef, **({"faces": ("x-",)} if vec3 else {}))
+    layered = learned.LearnedSmoother(net, mg, s.coef, launches=5)
+    whole = learned.LearnedSmoother(net, mg, s.coef, launches=1)
+    two = learned.LearnedSmoother(net, mg, s.coef, launches=2)
+    assert whole.whole_network and whole.kernels_per_apply == 1 and layered.kernels_per_apply == 5
+    assert two.whole_network and two.kernels_per_apply == 2
+    n = layered.n * (3 if vec3 else 1)
+    gen = torch.Generator(device="cuda").manual_seed(1)
+    for trial in range(3):
+        r = torch.randn(n, device="cuda", generator=gen)
+        w_ref = torch.full_like(r, float("nan"))
+        w = torch.full_like(r, float("nan"))
+        w2 = torch.full_like(r, float("nan"))
+        layered.launch(STREAM(), r.data_ptr(), w_ref.data_ptr())
+        whole.launch(STREAM(), r.data_ptr(), w.data_ptr())
+        two.launch(STREAM(), r.data_ptr(), w2.data_ptr())
+        torch.cuda.synchronize()
+        assert int(mg.status.item()) == 0
+        assert torch.isfinite(w_ref).all()
+        assert torch.equal(w, w_ref), f"launch {trial}: max diff {float((w - w_ref).abs().max())}"
+        assert torch.equal(w2, w_ref), f"launch {trial}: max diff {float((w2 - w_ref).abs().max())}"
+    assert int(whole.epoch[0].item()) == 3 and int(whole.epoch[1].item()) == 0
+    assert int(two.epoch[0].item()) == 3
+    # graph capture: the counters live on the device, so replays keep advancing the epoch
+    r = torch.randn(n, device="cuda", generator=gen)
+    w_ref = torch.empty_like(r)
+    layered.launch(STREAM(), r.data_ptr(), w_ref.data_ptr())
+    w = torch.full_like(r, float("nan"))
+    s_cap = torch.cuda.Stream()
+    s_cap.wait_stream(torch.cuda.current_stream())
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.stream(s_cap):
+        with torch.cuda.graph(g, stream=s_cap):
+            whole.launch(s_cap.cuda_stream, r.data_ptr(), w.data_ptr())
+    torch.cuda.current_stream().wait_stream(s_cap)
+    for _ in range(2):
+        w.fill_(float("nan"))
+        g.replay()
+        torch.cuda.synchronize()
+        assert torch.equal(w, w_ref)
+    assert int(whole.epoch[0].item()) == 5
+    assert int(mg.status.item()) == 0

@@ -108,6 +108,8 @@ _SIGNATURES = {
     "gb_conv3_planar_rows": (_c_i64, [_c_int] * 3),
     "gb_net_features_planar": (_c_int, [_c_int] * 4 + [_vp, _vp, _vp, _vp, _vp, _vp]),
     "gb_conv3_fwd_tc": (_c_int, [_c_int] * 4 + [_vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_float, _vp, _vp]),
+    "gb_convnet_tc_items": (_c_i64, [_c_int] * 3),
+    "gb_convnet_fwd_tc": (_c_int, [_c_int] * 5 + [_vp] * 7 + [ctypes.c_float, _vp, _vp, _vp, _vp]),
     "gb_batched_pcg_workspace_bytes": (_c_sz, [_c_i64]),
     "gb_batched_pcg": (_c_int, [_c_int, _vp, _vp, _c_i64, _vp, _vp, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _c_int, _c_int,
                                 _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_sz, _vp, _vp]),

@@ -192,9 +192,13 @@ class LearnedSmoother:
     """The inference smoother plugged into ``MultigridPreconditioner.smoother``.
 
     tcgen05 implicit-GEMM layers on the planar padded layout (features + 4 layers, the last one fused
-    with the Jacobi step: 5 launches)."""
+    with the Jacobi step).  ``launches``: 5 -- the features kernel and one launch per layer; 2 -- the
+    features kernel, then the four layers in one cooperative launch whose CTAs wait on per-item
+    completion counters instead of kernel boundaries; 1 -- the features computed inside that launch
+    too.  All three write the same values, bit for bit."""
 
-    def __init__(self, net: ConvNet, mg: multigrid.MultigridPreconditioner, coef, backend: str = "tc"):
+    def __init__(self, net: ConvNet, mg: multigrid.MultigridPreconditioner, coef, backend: str = "tc",
+                 launches: int = 2):
         bdim = getattr(mg, "bdim", 1)
         if bdim != net.ncomp:
             raise ValueError(f"learned smoother: a network for {net.ncomp}-component fields on a {bdim}x{bdim} "
@@ -217,10 +221,34 @@ class LearnedSmoother:
         self.Wt = net.bf16_weights(last_cout=16)
         rows = planar_rows(self.dims)
         self.buf = [A.zeros(2 * rows * 8, torch.bfloat16), A.zeros(2 * rows * 8, torch.bfloat16)]
+        if launches not in (1, 2, 5):
+            raise ValueError("launches must be 1, 2 or 5")
         self.kernels_per_apply = 5
+        self.whole_network = launches < 5 and 2 <= len(self.Wt) <= 4
+        self._features_in_network = launches == 1
+        if self.whole_network:
+            L = N.lib()
+            nl = len(self.Wt)
+            # one planar buffer per layer input: no layer overwrites what another CTA may still stage
+            self.buf += [A.zeros(2 * rows * 8, torch.bfloat16) for _ in range(nl - 2)]
+            self.flags = A.zeros(int(L.gb_convnet_tc_items(*self.dims)), torch.int32)
+            self.epoch = A.zeros(2, torch.int32)
+            self._act = (ctypes.c_void_p * nl)(*[A.ptr(b) for b in self.buf[:nl]])
+            self._wt = (ctypes.c_void_p * nl)(*[A.ptr(t) for t in self.Wt])
+            self.kernels_per_apply = 1 if self._features_in_network else 2
 
     def launch(self, stream, r: int, w: int) -> None:
         L = N.lib()
+        if self.whole_network:
+            if not self._features_in_network:
+                N.check(L.gb_net_features_planar(self.ncomp, *self.dims, r, A.ptr(self.dinv), A.ptr(self.chat),
+                                                 A.ptr(self.mask), A.ptr(self.buf[0]), stream), "features")
+            chat = None if not self._features_in_network else A.ptr(self.chat)
+            N.check(L.gb_convnet_fwd_tc(*self.dims, self.ncomp, len(self.Wt), self._act, self._wt, w, r,
+                                        A.ptr(self.dinv), chat, A.ptr(self.mask), self.omega,
+                                        A.ptr(self.flags), A.ptr(self.epoch), A.ptr(self.status), stream),
+                    "convnet tc")
+            return
         N.check(L.gb_net_features_planar(self.ncomp, *self.dims, r, A.ptr(self.dinv), A.ptr(self.chat),
                                          A.ptr(self.mask), A.ptr(self.buf[0]), stream), "features")
         src, dst = self.buf[0], self.buf[1]

@@ -1023,6 +1023,7 @@ class RefinedSolver:
         self._norms = A.zeros(2, torch.float64)
         self._status = A.zeros(1, torch.int32)
         self._host = torch.zeros(2, dtype=torch.float64, pin_memory=True)
+        self._step_host = torch.zeros(2, dtype=torch.int32, pin_memory=True)
         self._x_backup = None
         self.kernel_launches = 0
         # the true residual on the multigrid fine level's stencil form of the same matrix, when it has one
@@ -1084,31 +1085,45 @@ class RefinedSolver:
             self.inner._tol = min(max(self.inner_tol, need), 0.5)
             self._d.zero_()
             self.inner._run_fused(Aop, self._r32, self._d, self.inner._M, x_is_zero=True)
-            it = int(self.inner._dev_iter.item())
+            # queue x += d and the new residual behind the correction solve, and read its iteration
+            # count and status together with the residual norms (one host synchronisation per step)
+            self._step_host[0:1].copy_(self.inner._dev_iter.reshape(1), non_blocking=True)
+            self._step_host[1:2].copy_(self.inner._dev_status.reshape(1), non_blocking=True)
+            N.check(L.gb_update_solution(self.n, A.ptr(x64), A.ptr(self._x2), A.ptr(self._d), 1.0, A.stream()),
+                    "update_solution")
+            self.kernel_launches += 1
+            self.residual(x64, b, sync=False)
+            self._host.copy_(self._norms, non_blocking=True)
+            torch.cuda.current_stream().synchronize()
+            it, status = (int(v) for v in self._step_host.tolist())
+            rnorm = math.sqrt(float(self._host[0]))
             if self.inner.persistent_active:
                 # argument store, init and the persistent loop (one launch per host-checked chunk)
                 self.kernel_launches += 3 if self.inner._check_every == 0 else 2 + it
             else:
                 per_it = 3 if self.method != "fcg" else 4 + getattr(self.inner._precond_obj, "kernels_per_apply", 0)
                 self.kernel_launches += 2 + per_it * it  # argument store, init, kernels per iteration
-            if self.method == "fcg":
-                status = int(self.inner._dev_status.item())
-                if status & (N.DEV_STAGNATION | N.DEV_BREAKDOWN | N.DEV_NONFINITE):
-                    # the flexible solve stalled: finish this correction with plain Jacobi-CG
-                    self.fallbacks += 1
-                    self._jacobi._tol = self.inner._tol
-                    self._jacobi._run_fused(Aop, self._r32, self._d, self._jacobi_M, x_is_zero=False)
-                    jt = int(self._jacobi._dev_iter.item())
-                    it += jt
-                    if self._jacobi.persistent_active:
-                        self.kernel_launches += 3 if self._jacobi._check_every == 0 else 2 + jt
-                    else:
-                        self.kernel_launches += 2 + 3 * jt
-            N.check(L.gb_update_solution(self.n, A.ptr(x64), A.ptr(self._x2), A.ptr(self._d), 1.0, A.stream()),
-                    "update_solution")
-            self.kernel_launches += 1
+            if self.method == "fcg" and status & (N.DEV_STAGNATION | N.DEV_BREAKDOWN | N.DEV_NONFINITE):
+                # the flexible solve stalled: take its correction back, recompute the residual it was
+                # solving for (the queued residual overwrote it) and finish the correction with plain
+                # Jacobi-CG, starting from the flexible solve's d
+                N.check(L.gb_update_solution(self.n, A.ptr(x64), A.ptr(self._x2), A.ptr(self._d), -1.0, A.stream()),
+                        "undo_solution")
+                self.residual(x64, b, sync=False)
+                self.fallbacks += 1
+                self._jacobi._tol = self.inner._tol
+                self._jacobi._run_fused(Aop, self._r32, self._d, self._jacobi_M, x_is_zero=False)
+                jt = int(self._jacobi._dev_iter.item())
+                it += jt
+                if self._jacobi.persistent_active:
+                    self.kernel_launches += 3 if self._jacobi._check_every == 0 else 2 + jt
+                else:
+                    self.kernel_launches += 2 + 3 * jt
+                N.check(L.gb_update_solution(self.n, A.ptr(x64), A.ptr(self._x2), A.ptr(self._d), 1.0, A.stream()),
+                        "update_solution")
+                self.kernel_launches += 2
+                rnorm, _ = self.residual(x64, b)
             inner_iters += it
-            rnorm, _ = self.residual(x64, b)
             outer += 1
             history.append(rnorm / bnorm)
             if callback is not None:
