@@ -558,6 +558,20 @@ def run_profile(args):
         assert int(st.item()) == 0
         print("profile run done", flush=True)
         return 0
+    if args.profile == "convnet":  # 3 applications of the learned smoother (features + one network launch)
+        from warp_gb300 import learned, multigrid
+
+        system = problems.diffusion(tuple(args.res), sigma=1.5, corr_length=0.1, seed=0)
+        mg = multigrid.MultigridPreconditioner(system.A, system.geo, system.coef)
+        sm = learned.LearnedSmoother(learned.ConvNet.load(learned.DEFAULT_WEIGHTS), mg, system.coef)
+        r = torch.randn(system.A.nrow, device="cuda") * (1 - mg.levels[0].mask)
+        w = torch.empty_like(r)
+        for _ in range(3):
+            sm.launch(torch.cuda.current_stream().cuda_stream, r.data_ptr(), w.data_ptr())
+        torch.cuda.synchronize()
+        assert int(mg.status.item()) == 0
+        print("profile run done", flush=True)
+        return 0
     if args.profile == "vcycle":  # 3 eager V-cycles (stencil-form levels) on the 97^3 node grid
         from warp_gb300 import multigrid, problems
 
@@ -652,13 +666,14 @@ def main():
     p.add_argument("--elasticity-large-res", type=int, default=128,
                    help="cells per axis of the large elasticity extra (0 skips it)")
     p.add_argument("--weights", default=os.path.join(ROOT, "warp_gb300", "data", "smoother_q1_diffusion.npz"))
-    p.add_argument("--profile", choices=["spmv", "cg", "jacobi_solve", "solve", "conv", "batched", "vcycle",
+    p.add_argument("--profile", choices=["spmv", "cg", "jacobi_solve", "solve", "conv", "convnet", "batched", "vcycle",
                                          "assembly"],
                    default=None,
                    help="run a fixed kernel sequence for an ncu capture and exit (prints no bench line): "
                         "spmv = 8 bsr_mv launches, cg = 30 eager (non-graph) Jacobi-CG iterations, "
                         "jacobi_solve = one refined Jacobi-CG solve, solve = two learned-FCG solves (eager launches), "
-                        "conv = 3 launches of one tcgen05 conv layer on the node grid, batched = two launches of "
+                        "conv = 3 launches of one tcgen05 conv layer on the node grid, convnet = 3 applications of "
+                        "the learned smoother (features kernel + whole-network launch), batched = two launches of "
                         "the batched CG on 512 uneven systems, vcycle = 3 eager multigrid V-cycles (stencil levels), "
                         "assembly = one 96^3 fem.integrate per construction (direct, triplets, row compress)")
     args = p.parse_args()
@@ -974,7 +989,7 @@ def main():
                            "d2h_bytes_per_step": d2h, "timing": "host wall clock, synchronised"},
         "gpu_launches": gpu_launches,
         "clocks": clocks,
-        "roofline_conv": {"bound": "tensor", "kernel": "k_conv3_tc<false> (one 16->16 hidden layer, 97^3 nodes)",
+        "roofline_conv": {"bound": "tensor", "kernel": "k_conv3_tc<0, false> (one 16->16 hidden layer, 97^3 nodes)",
                           "achieved": conv_tflops, "peak": tensor_peak, "unit": "TFLOP/s",
                           "frac": conv_tflops / tensor_peak, "peak_kind": tensor_peak_kind,
                           "algorithmic_flop": conv_flop, "launch_us": conv_ms * 1e3,

@@ -357,65 +357,70 @@ __global__ void __launch_bounds__(NET ? TC_NET_THREADS : TC_THREADS, 1) k_conv3_
         // items): its lanes read up to 32 (plane, column) counters from plane x on at once (one round
         // trip), the planes before the first unfinished one are then ready, and a proxy fence orders the
         // acquired stores before the bulk copies.
-        int q = 0;  // sequence number of the next block; its slot is q % NS
-        bool ok = true;
-        const int span = (int)(((int64_t)c.sy + 2 + TC_SUB * TC_OUT - 1) / (TC_SUB * TC_OUT));  // columns
-        for (int l = 0; l < NL && ok; ++l) {
-            const unsigned int need = flag_base + 8u * (unsigned int)(l + feat);
-            const bool wait_flags = fused && (l + feat) > 0;
-            for (int64_t k = k_begin; k < k_end && ok;) {
-                const int o = (int)(k / c.nx);
-                const int x0 = (int)(k % c.nx) + 1;
-                const int64_t run_end = min(k_end, (int64_t)(o + 1) * c.nx);
-                const int x1 = (int)((run_end - 1) % c.nx) + 1;
-                int ready = 0;  // planes up to this one are finished (this layer's input, this run)
-                for (int xb = x0 - 1; xb <= x1 + 1; ++xb, ++q) {
-                    const int s = q % NS;
-                    int wok = 1;
-                    if (lane == 0 && ((q >= NS && !tc_wait(&empty[s], ((q / NS) - 1) & 1, s_abort)) || *s_abort)) wok = 0;
-                    if (!__shfl_sync(0xffffffffu, wok, 0)) {
-                        if (lane == 0) *s_abort = 1;
-                        ok = false;
-                        break;
-                    }
-                    if (wait_flags && xb >= 1 && xb <= c.nx && xb > ready) {
-                        const int cmin = max(0, o - span), cmax = min(c.ncols - 1, o + span);
-                        const int ncl = cmax - cmin + 1;  // <= TC_POLL (checked on the host)
-                        const int npl = max(1, min(min(c.nx, x1 + 1) - xb + 1, TC_POLL / ncl));
-                        const int pe = lane / ncl, ce = lane - pe * ncl;  // this lane's (plane, column)
-                        const bool mine = pe < npl;
-                        const unsigned int* fp = c.flags + (int64_t)(cmin + ce) * c.nx + (xb - 1 + pe);
-                        const uint64_t t0 = globaltimer_ns();
-                        int first_bad;  // first plane (offset from xb) not finished yet
-                        for (;;) {
-                            const bool bad = mine && (int)(ld_acquire_u32_gpu(fp) - need) < 0;
-                            first_bad = (int)__reduce_min_sync(0xffffffffu, (unsigned)(bad ? pe : npl));
-                            if (first_bad > 0) break;
-                            int stop = 0;
-                            if (lane == 0 && (*s_abort || globaltimer_ns() - t0 > kWaitLimitNs)) stop = 1;
-                            if (__shfl_sync(0xffffffffu, stop, 0)) break;
-                        }
-                        if (first_bad == 0) {
+        // a single-layer launch needs lane 0 only (no counters to read)
+        if (NET || lane == 0) {
+            constexpr unsigned kLanes = NET ? 0xffffffffu : 1u;
+            int q = 0;  // sequence number of the next block; its slot is q % NS
+            bool ok = true;
+            const int span = (int)(((int64_t)c.sy + 2 + TC_SUB * TC_OUT - 1) / (TC_SUB * TC_OUT));  // columns
+            for (int l = 0; l < NL && ok; ++l) {
+                const unsigned int need = flag_base + 8u * (unsigned int)(l + feat);
+                const bool wait_flags = fused && (l + feat) > 0;
+                for (int64_t k = k_begin; k < k_end && ok;) {
+                    const int o = (int)(k / c.nx);
+                    const int x0 = (int)(k % c.nx) + 1;
+                    const int64_t run_end = min(k_end, (int64_t)(o + 1) * c.nx);
+                    const int x1 = (int)((run_end - 1) % c.nx) + 1;
+                    int ready = 0;  // planes up to this one are finished (this layer's input, this run)
+                    for (int xb = x0 - 1; xb <= x1 + 1; ++xb, ++q) {
+                        const int s = q % NS;
+                        int wok = 1;
+                        if (lane == 0 && ((q >= NS && !tc_wait(&empty[s], ((q / NS) - 1) & 1, s_abort)) || *s_abort))
+                            wok = 0;
+                        if (!__shfl_sync(kLanes, wok, 0)) {
                             if (lane == 0) *s_abort = 1;
                             ok = false;
                             break;
                         }
-                        ready = xb + first_bad - 1;
-                        __syncwarp();
-                        asm volatile("fence.proxy.async.global;" ::: "memory");
+                        if (wait_flags && xb >= 1 && xb <= c.nx && xb > ready) {
+                            const int cmin = max(0, o - span), cmax = min(c.ncols - 1, o + span);
+                            const int ncl = cmax - cmin + 1;  // <= TC_POLL (checked on the host)
+                            const int npl = max(1, min(min(c.nx, x1 + 1) - xb + 1, TC_POLL / ncl));
+                            const int pe = lane / ncl, ce = lane - pe * ncl;  // this lane's (plane, column)
+                            const bool mine = pe < npl;
+                            const unsigned int* fp = c.flags + (int64_t)(cmin + ce) * c.nx + (xb - 1 + pe);
+                            const uint64_t t0 = globaltimer_ns();
+                            int first_bad;  // first plane (offset from xb) not finished yet
+                            for (;;) {
+                                const bool bad = mine && (int)(ld_acquire_u32_gpu(fp) - need) < 0;
+                                first_bad = (int)__reduce_min_sync(0xffffffffu, (unsigned)(bad ? pe : npl));
+                                if (first_bad > 0) break;
+                                int stop = 0;
+                                if (lane == 0 && (*s_abort || globaltimer_ns() - t0 > kWaitLimitNs)) stop = 1;
+                                if (__shfl_sync(0xffffffffu, stop, 0)) break;
+                            }
+                            if (first_bad == 0) {
+                                if (lane == 0) *s_abort = 1;
+                                ok = false;
+                                break;
+                            }
+                            ready = xb + first_bad - 1;
+                            __syncwarp();
+                            asm volatile("fence.proxy.async.global;" ::: "memory");
+                        }
+                        if (lane == 0) {
+                            const int64_t row = (int64_t)xb * c.sx + (int64_t)o * (TC_SUB * TC_OUT);
+                            unsigned char* dst = ring + (size_t)s * c.block_bytes;
+                            mbar_arrive_expect_tx(&full[s], c.block_bytes);
+    #pragma unroll
+                            for (int h = 0; h < 2; ++h)
+                                bulk_g2s(dst + h * c.rows_bytes, c.in[l] + ((int64_t)h * c.plane_rows + row) * 16,
+                                         c.rows_bytes, &full[s]);
+                            *s_issued = q + 1;
+                        }
                     }
-                    if (lane == 0) {
-                        const int64_t row = (int64_t)xb * c.sx + (int64_t)o * (TC_SUB * TC_OUT);
-                        unsigned char* dst = ring + (size_t)s * c.block_bytes;
-                        mbar_arrive_expect_tx(&full[s], c.block_bytes);
-#pragma unroll
-                        for (int h = 0; h < 2; ++h)
-                            bulk_g2s(dst + h * c.rows_bytes, c.in[l] + ((int64_t)h * c.plane_rows + row) * 16,
-                                     c.rows_bytes, &full[s]);
-                        *s_issued = q + 1;
-                    }
+                    k = run_end;
                 }
-                k = run_end;
             }
         }
     } else if (warp <= TC_ISSUERS) {
@@ -572,7 +577,7 @@ __global__ void __launch_bounds__(NET ? TC_NET_THREADS : TC_THREADS, 1) k_conv3_
         }
         int xp = 0;  // exchange buffer parity
         for (int it = par; it < NL * nit; it += TC_EPI_PAR) {
-            const int l = it / nit;
+            const int l = NET ? it / nit : 0;
             const int64_t k = k_begin + (it - l * nit);
             const bool last_layer = NOUT > 0 && (!NET || l == NL - 1);
             const int a = it % TC_RING;
@@ -844,11 +849,10 @@ static int tc_set_smem_attr()
     // one-time per process: the largest dynamic shared memory any variant may use
     static bool attr_set = false;
     if (!attr_set) {
-        GB_CHECK_CUDA(cudaFuncSetAttribute(k_conv3_tc<0, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_LIMIT));
-        GB_CHECK_CUDA(cudaFuncSetAttribute(k_conv3_tc<1, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_LIMIT));
-        GB_CHECK_CUDA(cudaFuncSetAttribute(k_conv3_tc<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_LIMIT));
-        GB_CHECK_CUDA(cudaFuncSetAttribute(k_conv3_tc<1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_LIMIT));
-        GB_CHECK_CUDA(cudaFuncSetAttribute(k_conv3_tc<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_LIMIT));
+        void (*const kernels[])(const TcConv) = {k_conv3_tc<0, false>, k_conv3_tc<1, false>, k_conv3_tc<3, false>,
+                                                 k_conv3_tc<1, true>, k_conv3_tc<3, true>};
+        for (auto kern : kernels)
+            GB_CHECK_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM_LIMIT));
         attr_set = true;
     }
     return GB_OK;
