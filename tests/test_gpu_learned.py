@@ -441,3 +441,33 @@ def test_whole_network_launch_matches_layer_launches(cuda, cells, vec3):
         assert torch.equal(w, w_ref)
     assert int(whole.epoch[0].item()) == 5
     assert int(mg.status.item()) == 0
+
+
+def test_whole_network_launch_times_out_when_counters_never_reach(cuda):
+    """A dependency that is never met ends the whole-network launch through its bounded waits: the status
+    word gets DEV_WAIT_TIMEOUT and the call returns; the next launch with fresh counters is right again."""
+    import warp_gb300._native as N
+    from warp_gb300 import learned, multigrid, problems
+
+    s = problems.diffusion((16, 16, 16), sigma=1.5, corr_length=0.2, seed=6)
+    net = learned.ConvNet(seed=3)
+    net.W[3] = (torch.randn(net.W[3].numel(), generator=torch.Generator().manual_seed(4)) * 0.05).cuda()
+    mg = multigrid.MultigridPreconditioner(s.A, s.geo, s.coef)
+    layered = learned.LearnedSmoother(net, mg, s.coef, launches=5)
+    two = learned.LearnedSmoother(net, mg, s.coef, launches=2)
+    r = torch.randn(layered.n, device="cuda", generator=torch.Generator(device="cuda").manual_seed(2))
+    w_ref, w = torch.empty_like(r), torch.empty_like(r)
+    layered.launch(STREAM(), r.data_ptr(), w_ref.data_ptr())
+    torch.cuda.synchronize()
+    assert int(mg.status.item()) == 0
+    two.flags.fill_(-4096)  # far below every stage's expected count: layer 1 can never be staged
+    two.launch(STREAM(), r.data_ptr(), w.data_ptr())
+    torch.cuda.synchronize()
+    assert int(mg.status.item()) & N.DEV_WAIT_TIMEOUT
+    mg.status.zero_()
+    two.flags.zero_()
+    two.epoch.zero_()
+    two.launch(STREAM(), r.data_ptr(), w.data_ptr())
+    torch.cuda.synchronize()
+    assert int(mg.status.item()) == 0
+    assert torch.equal(w, w_ref)
