@@ -41,7 +41,7 @@
 // The two issuers of a window take turns in block order (a shared-memory sequence word), so a plane's
 // three contributions are summed in the same order in every launch: results are bitwise reproducible.
 //
-// Whole-network launch (gb_convnet_fwd_tc, NET = true): one cooperative launch runs the features and
+// Whole-network launch (gb_convnet_fwd_tc, NET = true): one cooperative launch runs (optionally) the features and
 // all four layers; each CTA walks its items layer after layer, and layer l reads activations that
 // other CTAs wrote in layer l - 1.  Per-item counters in global memory carry the dependency: a counter
 // warp raises an item's counter by 8 once the item's 8 epilogue warps have stored a hidden layer
