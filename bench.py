@@ -97,6 +97,11 @@ class ClockSampler:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
                  "-lms", "50"], stdout=self.f, stderr=subprocess.DEVNULL)
+            # nvidia-smi's start-up (driver attach, first query) must not overlap the timed region: wait
+            # for its first sample (at most 5 s)
+            t_end = time.time() + 5.0
+            while time.time() < t_end and self.proc.poll() is None and os.path.getsize(self.path) == 0:
+                time.sleep(0.01)
         except Exception:
             self.proc = None
         return self

@@ -23,7 +23,7 @@ def test_vector_transfers_equal_scalar_transfers_per_component(cuda):
     from warp_gb300 import multigrid
 
     s = _elasticity(8)
-    mg = multigrid.MultigridPreconditioner(s.A, s.geo, s.coef, faces=FACES)
+    mg = multigrid.MultigridPreconditioner(s.A, s.geo, s.coef, faces=FACES, coarsest_nodes=400)  # two levels
     f, c = mg.levels[0], mg.levels[1]
     L = N.lib()
     st = torch.cuda.current_stream().cuda_stream
@@ -52,7 +52,7 @@ def test_elasticity_hierarchy_and_symmetric_vcycle(cuda):
     from warp_gb300 import multigrid
 
     s = _elasticity(16, seed=2)
-    mg = multigrid.MultigridPreconditioner(s.A, s.geo, s.coef, faces=FACES)
+    mg = multigrid.MultigridPreconditioner(s.A, s.geo, s.coef, faces=FACES, coarsest_nodes=400)  # three levels
     assert mg.bdim == 3 and mg.n == s.A.nrow * 3
     assert [lv.dims for lv in mg.levels] == [(17,) * 3, (9,) * 3, (5,) * 3]
     assert all(lv.A.block_shape == (3, 3) for lv in mg.levels)

@@ -115,3 +115,21 @@ def test_refined_fcg_reaches_fp64_tolerance_and_falls_back(cuda):
     bad = linear.RefinedSolver(s.A, M=Bad(), method="fcg", inner_tol=1e-5)
     x64b, infob = bad.solve(s.b, tol=1e-8)
     assert infob["converged"] and bad.fallbacks >= 1
+
+
+def test_default_coarsest_level_holds_at_most_2200_unknowns(cuda):
+    """The default hierarchy stops at the first level with at most 2200 unknowns (13^3 nodes for 1x1,
+    9^3 nodes for 3x3 blocks) and holds that level's exact inverse."""
+    from warp_gb300 import multigrid, problems
+
+    s = _system((24, 24, 24), sigma=1.5, seed=4)
+    mg = multigrid.MultigridPreconditioner(s.A, s.geo, s.coef)
+    assert [lv.dims for lv in mg.levels] == [(25,) * 3, (13,) * 3]
+    e = problems.elasticity((16, 16, 16), sigma=1.0, corr_length=0.3, seed=1)
+    mge = multigrid.MultigridPreconditioner(e.A, e.geo, e.coef, faces=("x-",))
+    assert [lv.dims for lv in mge.levels] == [(17,) * 3, (9,) * 3]
+    for m in (mg, mge):
+        last = m.levels[-1]
+        dense = last.A.numpy_dense()
+        inv = last.inv.cpu().numpy().astype(np.float64).reshape(dense.shape)
+        assert np.abs(inv @ dense - np.eye(dense.shape[0])).max() < 1e-4

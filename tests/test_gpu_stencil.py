@@ -126,7 +126,7 @@ def test_vcycle_and_fcg_stencil_match_csr(cuda, learned_smoother):
     s = _system((16, 16, 16), seed=7)
     mgs = {}
     for st in (False, True):
-        mg = multigrid.MultigridPreconditioner(s.A, s.geo, s.coef, stencil=st)
+        mg = multigrid.MultigridPreconditioner(s.A, s.geo, s.coef, stencil=st, coarsest_nodes=400)  # 3 levels
         if learned_smoother:
             w = os.path.join(os.path.dirname(__file__), "..", "warp_gb300", "data", "smoother_q1_diffusion.npz")
             mg.smoother = learned.LearnedSmoother(learned.ConvNet.load(w), mg, s.coef)
@@ -277,7 +277,7 @@ def test_fcg_stencil_rejects_mismatched_grid(cuda):
     from warp_gb300.optim import linear
 
     s = _system((8, 8, 8), seed=2)
-    mg = multigrid.MultigridPreconditioner(s.A, s.geo, s.coef)
+    mg = multigrid.MultigridPreconditioner(s.A, s.geo, s.coef, coarsest_nodes=400)
     S = mg.levels[0].S
     assert S is not None and len(mg.levels) > 1
     x = torch.zeros_like(s.b)

@@ -293,7 +293,8 @@ class _Field:
     def __init__(self, system, net: ConvNet):
         self.sys = system
         faces = ("x-",) if system.A.block_shape == (3, 3) else ("x-", "x+", "y-", "y+", "z-", "z+")
-        self.mg = multigrid.MultigridPreconditioner(system.A, system.geo, system.coef, faces=faces)
+        # the hierarchy the shipped weights were trained in (coarsest grid <= 400 nodes)
+        self.mg = multigrid.MultigridPreconditioner(system.A, system.geo, system.coef, faces=faces, coarsest_nodes=400)
         self.bdim = self.mg.bdim
         self.sm = TrainingSmoother(net, self.mg, system.coef)
         n = self.mg.n
