@@ -133,3 +133,24 @@ def test_default_coarsest_level_holds_at_most_2200_unknowns(cuda):
         dense = last.A.numpy_dense()
         inv = last.inv.cpu().numpy().astype(np.float64).reshape(dense.shape)
         assert np.abs(inv @ dense - np.eye(dense.shape[0])).max() < 1e-4
+
+
+def test_refined_solve_from_zero_edge_cases(cuda):
+    """Starting from x = 0 the refined solve reads the initial norms together with the first step's: a zero
+    right-hand side returns x = 0 after no outer step, max_outer = 0 reports the initial residual, and a
+    given starting iterate still goes through the synchronous first residual."""
+    from warp_gb300 import multigrid
+    from warp_gb300.optim import linear
+
+    s = _system((16, 16, 16), sigma=1.0, seed=9)
+    mg = multigrid.MultigridPreconditioner(s.A, s.geo, s.coef)
+    solver = linear.RefinedSolver(s.A, M=mg, method="fcg", inner_tol=1e-5)
+    x, info = solver.solve(torch.zeros_like(s.b), tol=1e-8)
+    assert info["outer"] == 0 and info["inner_iterations"] == 0 and info["converged"]
+    assert float(x.abs().max()) == 0.0 and info["history"] == [0.0]
+    x, info = solver.solve(s.b, tol=1e-8, max_outer=0)
+    assert info["outer"] == 0 and info["rel_residual"] == 1.0 and not info["converged"]
+    x, info = solver.solve(s.b, tol=1e-8)
+    assert info["converged"] and info["history"][0] == 1.0 and info["rel_residual"] <= 1e-8
+    x2, info2 = solver.solve(s.b, x64=x.clone(), tol=1e-8)
+    assert info2["converged"] and info2["outer"] == 0

@@ -1024,6 +1024,7 @@ class RefinedSolver:
         self._status = A.zeros(1, torch.int32)
         self._host = torch.zeros(2, dtype=torch.float64, pin_memory=True)
         self._step_host = torch.zeros(2, dtype=torch.int32, pin_memory=True)
+        self._host0 = torch.zeros(2, dtype=torch.float64, pin_memory=True)
         self._x_backup = None
         self.kernel_launches = 0
         # the true residual on the multigrid fine level's stencil form of the same matrix, when it has one
@@ -1064,24 +1065,30 @@ class RefinedSolver:
         if b.dtype != torch.float32:
             raise TypeError("right-hand side must be float32 (the system's scalar type)")
         L = N.lib()
+        history = []
+        inner_iters = 0
+        outer = 0
+        Aop = self.inner._A
+        diverged = False
         if x64 is None:
+            # x = 0: the residual is b, so the first correction solve needs no host read first; the
+            # initial norms come back with the first step's
             x64 = A.zeros(self.n, torch.float64)
             self._x2.zero_()
+            self.residual(x64, b, sync=False)
+            self._host0.copy_(self._norms, non_blocking=True)
+            rnorm = bnorm = None
+            guard = None
         else:
             x64 = A.as_tensor(x64).reshape(-1)
             N.check(L.gb_update_solution(self.n, A.ptr(x64), A.ptr(self._x2), None, 0.0, A.stream()), "update")
             self.kernel_launches += 1
-        history = []
-        inner_iters = 0
-        rnorm, bnorm = self.residual(x64, b)
-        history.append(rnorm / bnorm if bnorm > 0 else 0.0)
-        outer = 0
-        Aop = self.inner._A
-        guard = _DivergenceGuard(rnorm, bnorm)
-        diverged = False
-        while bnorm > 0 and rnorm > tol * bnorm and outer < max_outer:
+            rnorm, bnorm = self.residual(x64, b)
+            history.append(rnorm / bnorm if bnorm > 0 else 0.0)
+            guard = _DivergenceGuard(rnorm, bnorm)
+        while (bnorm is None or (bnorm > 0 and rnorm > tol * bnorm)) and outer < max_outer:
             # ask the correction solve only for the reduction still missing (never below inner_tol)
-            need = 0.25 * tol * bnorm / rnorm
+            need = 0.25 * tol * (1.0 if bnorm is None else bnorm / rnorm)
             self.inner._tol = min(max(self.inner_tol, need), 0.5)
             self._d.zero_()
             self.inner._run_fused(Aop, self._r32, self._d, self.inner._M, x_is_zero=True)
@@ -1096,6 +1103,15 @@ class RefinedSolver:
             self._host.copy_(self._norms, non_blocking=True)
             torch.cuda.current_stream().synchronize()
             it, status = (int(v) for v in self._step_host.tolist())
+            if bnorm is None:
+                r0, bnorm = (math.sqrt(v) for v in self._host0.tolist())
+                history.append(r0 / bnorm if bnorm > 0 else 0.0)
+                guard = _DivergenceGuard(r0, bnorm)
+                if bnorm == 0:  # b = 0: x = 0 is the solution (the correction solve had nothing to do)
+                    x64.zero_()
+                    self._x2.zero_()
+                    rnorm = 0.0
+                    break
             rnorm = math.sqrt(float(self._host[0]))
             if self.inner.persistent_active:
                 # argument store, init and the persistent loop (one launch per host-checked chunk)
@@ -1151,6 +1167,10 @@ class RefinedSolver:
                 break
             if it == 0:
                 break
+        if bnorm is None:  # max_outer = 0: only the initial residual was queued
+            torch.cuda.current_stream().synchronize()
+            rnorm, bnorm = (math.sqrt(v) for v in self._host0.tolist())
+            history.append(rnorm / bnorm if bnorm > 0 else 0.0)
         return x64, dict(outer=outer, inner_iterations=inner_iters, rel_residual=history[-1], history=history,
                          converged=bool(rnorm <= tol * bnorm), diverged=diverged)
 
