@@ -154,3 +154,27 @@ def test_refined_solve_from_zero_edge_cases(cuda):
     assert info["converged"] and info["history"][0] == 1.0 and info["rel_residual"] <= 1e-8
     x2, info2 = solver.solve(s.b, x64=x.clone(), tol=1e-8)
     assert info2["converged"] and info2["outer"] == 0
+
+
+@pytest.mark.parametrize("m,n", [(37, 300), (700, 2197), (5, 4096)])
+def test_dense_mv_matches_fp64(cuda, m, n):
+    """gb_dense_mv (the coarsest level's inverse product): one warp per row for short rows, one CTA per row
+    for long ones; z = alpha A x + beta y within fp32 summation error, and bitwise the same on a repeat."""
+    import warp_gb300._native as N
+
+    g = torch.Generator(device="cuda").manual_seed(m + n)
+    Am = torch.randn(m, n, device="cuda", generator=g)
+    x = torch.randn(n, device="cuda", generator=g)
+    y = torch.randn(m, device="cuda", generator=g)
+    z = torch.empty(m, device="cuda")
+    st = torch.cuda.current_stream().cuda_stream
+    for alpha, beta in ((1.0, 0.0), (0.5, -2.0)):
+        N.check(N.lib().gb_dense_mv(N.GB_F32, m, n, Am.data_ptr(), x.data_ptr(), y.data_ptr(), z.data_ptr(),
+                                    alpha, beta, st))
+        z1 = z.clone()
+        N.check(N.lib().gb_dense_mv(N.GB_F32, m, n, Am.data_ptr(), x.data_ptr(), y.data_ptr(), z.data_ptr(),
+                                    alpha, beta, st))
+        ref = alpha * (Am.double() @ x.double()) + beta * y.double()
+        bound = 1e-5 * (Am.double().abs() @ x.double().abs()) * abs(alpha) + 1e-6 * y.double().abs() * abs(beta)
+        assert bool(((z.double() - ref).abs() <= bound + 1e-7).all())
+        assert torch.equal(z, z1)

@@ -93,6 +93,42 @@ __global__ void k_dense_mv(int m, int n, const T* __restrict__ A, const T* __res
     }
 }
 
+// The same product for long rows (the multigrid's coarsest inverse, a few thousand columns): one CTA of
+// DMV_THREADS per row, so that thousands of rows keep enough loads in flight to stream the matrix;
+// per-thread partials in order, then a fixed-order reduction (deterministic).
+constexpr int DMV_THREADS = 128;
+template <typename T>
+__global__ void __launch_bounds__(DMV_THREADS) k_dense_mv_rows(int n, const T* __restrict__ A, const T* __restrict__ x,
+                                                              const T* y, T* z, T alpha, T beta)
+{
+    pdl_enter();
+    __shared__ T s_part[DMV_THREADS / 32];
+    const int row = blockIdx.x;
+    const T* __restrict__ a = A + (size_t)row * n;
+    T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
+    int c = threadIdx.x;
+    if (alpha != T(0)) {
+        for (; c + 3 * DMV_THREADS < n; c += 4 * DMV_THREADS) {
+            s0 += a[c] * x[c];
+            s1 += a[c + DMV_THREADS] * x[c + DMV_THREADS];
+            s2 += a[c + 2 * DMV_THREADS] * x[c + 2 * DMV_THREADS];
+            s3 += a[c + 3 * DMV_THREADS] * x[c + 3 * DMV_THREADS];
+        }
+        for (; c < n; c += DMV_THREADS) s0 += a[c] * x[c];
+    }
+    T s = warp_sum((s0 + s1) + (s2 + s3));
+    if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        T t = s_part[0];
+#pragma unroll
+        for (int w = 1; w < DMV_THREADS / 32; ++w) t += s_part[w];
+        T v = alpha * t;
+        if (beta != T(0)) v += beta * y[row];
+        z[row] = v;
+    }
+}
+
 // Multi-column dot products out[k] = sum_i x_k[i] y_k[i] (k < ncols <= 4), accumulated in fp64,
 // single-pass deterministic grid reduction.
 struct DotPtrs {
@@ -196,6 +232,20 @@ GB_API int gb_dense_mv(int dtype, int m, int n, const void* A, const void* x, co
                        double beta, cudaStream_t stream)
 {
     if (m <= 0) return GB_OK;
+    if (n >= 4 * DMV_THREADS) {  // long rows: one CTA per row
+        if (dtype == GB_F32)
+            GB_CHECK_CUDA(launch_pdl(k_dense_mv_rows<float>, m, DMV_THREADS, 0, stream, n, (const float*)A,
+                                     (const float*)x, (const float*)y, (float*)z, (float)alpha, (float)beta));
+        else if (dtype == GB_F64)
+            GB_CHECK_CUDA(launch_pdl(k_dense_mv_rows<double>, m, DMV_THREADS, 0, stream, n, (const double*)A,
+                                     (const double*)x, (const double*)y, (double*)z, alpha, beta));
+        else {
+            gb::set_error("dense_mv: unsupported dtype");
+            return GB_ERR_UNSUPPORTED;
+        }
+        GB_CHECK_CUDA(cudaGetLastError());
+        return GB_OK;
+    }
     const int grid = ceil_div(m, 8);
     if (dtype == GB_F32)
         GB_CHECK_CUDA(launch_pdl(k_dense_mv<float>, grid, 256, 0, stream, m, n, (const float*)A, (const float*)x,
