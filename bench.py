@@ -640,7 +640,8 @@ def run_profile(args):
         from warp_gb300 import learned, multigrid
 
         net = learned.ConvNet.load(args.weights)
-        mg = multigrid.MultigridPreconditioner(A, system.geo, system.coef, fine_values=_fine_values())
+        mg = multigrid.MultigridPreconditioner(A, system.geo, system.coef, fine_values=_fine_values(),
+                                               omega=net.cycle_omega or "auto")
         mg.smoother = learned.LearnedSmoother(net, mg, system.coef, backend="tc")
         # eager launches (host check per iteration) so that every kernel of the solve is listed
         solver = linear.RefinedSolver(A, M=mg, method="fcg", inner_tol=args.inner_tol, use_cuda_graph=False)
@@ -749,7 +750,9 @@ def main():
         torch.cuda.synchronize()
         s0 = time.perf_counter()
         net = learned.ConvNet.load(args.weights)
-        lmg = multigrid.MultigridPreconditioner(A, system.geo, system.coef, fine_values=_fine_values())
+        # the hierarchy in the damping the network was trained with (no per-level estimate to discard)
+        lmg = multigrid.MultigridPreconditioner(A, system.geo, system.coef, fine_values=_fine_values(),
+                                                omega=net.cycle_omega or "auto")
         lmg.smoother = learned.LearnedSmoother(net, lmg, system.coef, backend="tc")
         lsolver = linear.RefinedSolver(A, M=lmg, method="fcg", inner_tol=args.inner_tol)
         torch.cuda.synchronize()
@@ -775,7 +778,7 @@ def main():
     fcg_ms, finfos, _, _ = timed(fsolver, system.b, args.steps)
 
     # ---- the learned solve with fp32 fine-level coefficients in the V-cycle, for comparison -----
-    l32 = multigrid.MultigridPreconditioner(A, system.geo, system.coef)
+    l32 = multigrid.MultigridPreconditioner(A, system.geo, system.coef, omega=net.cycle_omega or "auto")
     l32.smoother = learned.LearnedSmoother(net, l32, system.coef, backend="tc")
     l32solver = linear.RefinedSolver(A, M=l32, method="fcg", inner_tol=args.inner_tol)
     l32ms, l32infos, _, _ = timed(l32solver, system.b, max(3, args.steps // 4))

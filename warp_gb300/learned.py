@@ -74,12 +74,16 @@ class ConvNet:
         self.mean_log = 0.0
         self.inv_std = 1.0 / SIGMA_DEFAULT
         self.omega = 0.6
+        # Jacobi damping of the V-cycle the network is trained in and then serves: a number for every
+        # level, or None for the hierarchy's own per-level estimate ("auto")
+        self.cycle_omega = 0.6 if ncomp == 1 else None
 
     # --- persistence -------------------------------------------------------------------------
     def save(self, path: str, **meta) -> None:
         arrs = {f"W{i}": w.detach().cpu().numpy() for i, w in enumerate(self.W)}
         np.savez(path, mean_log=self.mean_log, inv_std=self.inv_std, omega=self.omega, steps=self.step_count,
-                 ncomp=self.ncomp, **arrs, **{k: np.asarray(v) for k, v in meta.items()})
+                 ncomp=self.ncomp, cycle_omega=np.nan if self.cycle_omega is None else self.cycle_omega, **arrs,
+                 **{k: np.asarray(v) for k, v in meta.items()})
 
     @classmethod
     def load(cls, path: str = DEFAULT_WEIGHTS, device="cuda") -> "ConvNet":
@@ -88,6 +92,9 @@ class ConvNet:
         for i in range(len(net.layers)):
             net.W[i] = torch.from_numpy(np.asarray(d[f"W{i}"], np.float32)).to(device)
         net.mean_log, net.inv_std, net.omega = float(d["mean_log"]), float(d["inv_std"]), float(d["omega"])
+        if "cycle_omega" in d:  # (files written before the field: the constructor's default for ncomp)
+            v = float(d["cycle_omega"])
+            net.cycle_omega = None if math.isnan(v) else v
         net.step_count = int(d["steps"])
         return net
 
@@ -213,6 +220,10 @@ class LearnedSmoother:
         self.mg = mg
         self.dims = lv.dims
         self.n = lv.n
+        if net.cycle_omega is not None:
+            # the network serves the cycle it was trained in: its Jacobi damping on every level
+            for level in mg.levels:
+                level.omega = float(net.cycle_omega)
         self.omega = float(lv.omega)
         self.mask, self.dinv = lv.mask, lv.dinv
         self.status = mg.status
@@ -293,8 +304,9 @@ class _Field:
     def __init__(self, system, net: ConvNet):
         self.sys = system
         faces = ("x-",) if system.A.block_shape == (3, 3) else ("x-", "x+", "y-", "y+", "z-", "z+")
-        # the hierarchy the shipped weights were trained in (coarsest grid <= 400 nodes)
-        self.mg = multigrid.MultigridPreconditioner(system.A, system.geo, system.coef, faces=faces, coarsest_nodes=400)
+        # the hierarchy the shipped weights were trained in (coarsest grid <= 400 nodes, the network's damping)
+        self.mg = multigrid.MultigridPreconditioner(system.A, system.geo, system.coef, faces=faces, coarsest_nodes=400,
+                                                    omega="auto" if net.cycle_omega is None else net.cycle_omega)
         self.bdim = self.mg.bdim
         self.sm = TrainingSmoother(net, self.mg, system.coef)
         n = self.mg.n

@@ -87,10 +87,11 @@ class MultigridPreconditioner:
         coef: per-cell diffusion coefficient (1x1), or per-cell Young's modulus (3x3; the Lame parameters
             of every level follow from it and ``poisson``); host array or device tensor.
         faces: Dirichlet faces (default: the whole boundary).
-        omega: Jacobi damping: a number for every level, or "auto" for 4 / (3 rho_l) per level with
-            rho_l = rho(D^-1 A_l) estimated by power iteration at set-up.  Default: 0.6 for 1x1 (the
-            Q1 Laplacian has rho ~ 2), "auto" for 3x3 (point Jacobi on Q1 elasticity has a larger rho,
-            where a fixed 0.6 amplifies the high-frequency error it should damp).
+        omega: Jacobi damping: a number for every level, or "auto" (the default) for 4 / (3 rho_l) per level
+            with rho_l = rho(D^-1 A_l) estimated by power iteration at set-up (about 0.91 on the 96^3
+            lognormal diffusion levels: 10 flexible-CG iterations there against 13 with a fixed 0.6; on Q1
+            elasticity a fixed 0.6 amplifies the high-frequency error it should damp).  A learned smoother
+            attached to the hierarchy sets the damping its network was trained with.
         coarsest_nodes: stop coarsening at or below this many nodes; that level is solved exactly with a
             dense inverse (computed on the host at set-up).  Default: at most 2200 unknowns -- 2200 nodes
             for 1x1 hierarchies (13^3 at 96^3), 733 for 3x3 (9^3 at 128^3): a 19 MB dense product per
@@ -123,7 +124,7 @@ class MultigridPreconditioner:
             raise ValueError("multigrid preconditioner: 3x3 blocks need a Grid3D (vec3 elasticity)")
         self.poisson = float(poisson)
         if omega is None:
-            omega = 0.6 if self.bdim == 1 else "auto"
+            omega = "auto"
         self.omega = omega if omega == "auto" else float(omega)
         self.faces = tuple(faces)
         self.smoother = None  # learned fine-level smoother (set by warp_gb300.learned)
