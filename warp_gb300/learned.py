@@ -301,11 +301,12 @@ class TrainingSmoother:
 class _Field:
     """One training problem: system, hierarchy, fp32 training smoother and scratch vectors."""
 
-    def __init__(self, system, net: ConvNet):
+    def __init__(self, system, net: ConvNet, coarsest_nodes: int = 400):
         self.sys = system
         faces = ("x-",) if system.A.block_shape == (3, 3) else ("x-", "x+", "y-", "y+", "z-", "z+")
-        # the hierarchy the shipped weights were trained in (coarsest grid <= 400 nodes, the network's damping)
-        self.mg = multigrid.MultigridPreconditioner(system.A, system.geo, system.coef, faces=faces, coarsest_nodes=400,
+        # the training hierarchy (the shipped weights: coarsest grid <= 400 nodes) in the network's damping
+        self.mg = multigrid.MultigridPreconditioner(system.A, system.geo, system.coef, faces=faces,
+                                                    coarsest_nodes=coarsest_nodes,
                                                     omega="auto" if net.cycle_omega is None else net.cycle_omega)
         self.bdim = self.mg.bdim
         self.sm = TrainingSmoother(net, self.mg, system.coef)
@@ -329,9 +330,10 @@ def _spmv(Am: sparse.BsrMatrix, x: torch.Tensor, y: torch.Tensor, alpha: float, 
 class SmootherTrainer:
     """GPU training of the learned smoother with the package's own kernels."""
 
-    def __init__(self, net: ConvNet, lr: float = 1e-3):
+    def __init__(self, net: ConvNet, lr: float = 1e-3, coarsest_nodes: int = 400):
         self.net = net
         self.lr = lr
+        self.coarsest_nodes = coarsest_nodes
         self._ws = None
         self._ws_dims = None
         self._gbuf = None
@@ -339,7 +341,7 @@ class SmootherTrainer:
         self._dots_out = A.zeros(4, torch.float64)
 
     def field(self, system) -> _Field:
-        f = _Field(system, self.net)
+        f = _Field(system, self.net, self.coarsest_nodes)
         f.mg.smoother = f.sm
         return f
 

@@ -54,7 +54,7 @@ def make_elasticity_field(res: int, seed: int, sigma: float = learned.SIGMA_DEFA
 def train(fields: int = 2000, res: int = 48, steps_per_field: int = 2, batch: int = 6, lr: float = 2e-3,
           lr_min: float = 1e-4, seed0: int = 10_000, eval_every: int = 250, out: str | None = None, log=print,
           net: learned.ConvNet | None = None, max_minutes: float | None = None,
-          problem: str = "diffusion", fcg_rhs: int = 0) -> learned.ConvNet:
+          problem: str = "diffusion", fcg_rhs: int = 0, coarsest_nodes: int = 400) -> learned.ConvNet:
     if problem not in ("diffusion", "elasticity"):
         raise ValueError("problem: diffusion or elasticity")
     field_of = make_field if problem == "diffusion" else make_elasticity_field
@@ -62,7 +62,7 @@ def train(fields: int = 2000, res: int = 48, steps_per_field: int = 2, batch: in
         net = learned.ConvNet(seed=0, ncomp=1 if problem == "diffusion" else 3)
         if problem == "elasticity":  # E = 1e3 exp(g), g ~ N(0, sigma^2)
             net.mean_log, net.inv_std = math.log(1e3), 1.0 / learned.SIGMA_DEFAULT
-    tr = learned.SmootherTrainer(net, lr=lr)
+    tr = learned.SmootherTrainer(net, lr=lr, coarsest_nodes=coarsest_nodes)
     rng = np.random.default_rng(seed0)
     held = tr.field(field_of(res, seed=seed0 - 1))
     held_pairs = learned.slow_pairs(held, 2, np.random.default_rng(1), smoother=None)
@@ -111,14 +111,24 @@ def main():
     ap.add_argument("--fcg-rhs", type=int, default=0,
                     help="right-hand sides per field whose flexible-CG residuals (current network) join the pairs")
     ap.add_argument("--init", default=None, help="start from these weights instead of a fresh network")
+    ap.add_argument("--cycle-omega", default=None,
+                    help="Jacobi damping of the training (and serving) cycle: a number, or 'auto' for the "
+                         "hierarchy's per-level estimate (default: the network's own, 0.6 for scalar fields)")
+    ap.add_argument("--coarsest-nodes", type=int, default=400, help="coarsest level of the training hierarchy")
     a = ap.parse_args()
     import os
 
     os.makedirs(os.path.dirname(os.path.abspath(a.out)), exist_ok=True)
     net = learned.ConvNet.load(a.init) if a.init else None
+    if a.cycle_omega is not None:
+        if net is None:
+            net = learned.ConvNet(seed=0, ncomp=1 if a.problem == "diffusion" else 3)
+            if a.problem == "elasticity":  # E = 1e3 exp(g), g ~ N(0, sigma^2)
+                net.mean_log, net.inv_std = math.log(1e3), 1.0 / learned.SIGMA_DEFAULT
+        net.cycle_omega = None if a.cycle_omega == "auto" else float(a.cycle_omega)
     train(a.fields, a.res, a.steps_per_field, a.batch, a.lr, eval_every=a.eval_every, out=a.out,
           log=lambda m: print(m, flush=True), max_minutes=a.max_minutes, problem=a.problem, fcg_rhs=a.fcg_rhs,
-          net=net)
+          net=net, coarsest_nodes=a.coarsest_nodes)
 
 
 if __name__ == "__main__":
