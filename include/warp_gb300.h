@@ -225,6 +225,16 @@ int gb_mg_restrict_c(int ncomp, int fnx, int fny, int fnz, int cnx, int cny, int
 int gb_mg_prolong_add_c(int ncomp, int fnx, int fny, int fnz, int cnx, int cny, int cnz, const float* zc,
                         const float* fmask, float scale, float* z, gb_stream_t stream);
 int gb_mg_jacobi0(int64_t n, float omega, const float* dinv, const float* r, float* z, gb_stream_t stream);
+/* Block-Jacobi smoothing of vec3 levels (no reference counterpart): the inverses of the 3x3 diagonal blocks
+ * (9 floats per block row, row-major; identity where a block is missing or singular), the first step
+ * z_i = omega Dinv_i r_i from zero, and the fused step z_out = z + omega Dinv (r - A z). */
+int gb_bsr_block_inverse_diagonal3(int nrow, const int* offsets, const int* row_counts, const int* columns,
+                                   const float* values, float* inv, gb_stream_t stream);
+int gb_mg_block_jacobi0(int64_t nodes, float omega, const float* dinv_blocks, const float* r, float* z,
+                        gb_stream_t stream);
+int gb_bsr_block_jacobi_smooth3(int nrow, int64_t nnz, int64_t ncap, const int* offsets, const int* columns,
+                                const void* values, int val_dtype, const float* r, const float* z,
+                                const float* dinv_blocks, float omega, float* z_out, int* status, gb_stream_t stream);
 int gb_mg_coarsen_cells(int fx, int fy, int fz, const float* a, float* ac, gb_stream_t stream);
 /* 27-point stencil form of a multigrid level's operator (no reference counterpart): node-major
  * coefficients S[i][k], k = 9(dx+1) + 3(dy+1) + (dz+1), i = (x*ny + y)*nz + z (gb_st27_bytes, 16-byte

@@ -182,3 +182,59 @@ def test_trained_3_channel_smoother_solves_elasticity(cuda):
     bd = s.b.cpu().numpy().astype(np.float64)
     assert np.linalg.norm(bd - Ah @ x.cpu().numpy()) / np.linalg.norm(bd) <= 2e-8
     assert int(mg.status.item()) == 0
+
+
+@pytest.mark.parametrize("values", ["fp32", "bf16"])
+def test_block_jacobi_kernels_match_fp64(cuda, values):
+    """Block-Jacobi pieces of the vec3 smoother against float64: the 3x3 diagonal-block inverses, the first
+    step omega Dinv r and the fused step z + omega Dinv (r - A z) (fp32 or bf16 matrix values)."""
+    import warp_gb300._native as N
+
+    s = _elasticity(5, seed=4, sigma=1.0)
+    A = s.A
+    L = N.lib()
+    st = torch.cuda.current_stream().cuda_stream
+    n = A.nrow
+    dense = A.numpy_dense()
+    inv = torch.empty(n * 9, device="cuda")
+    N.check(L.gb_bsr_block_inverse_diagonal3(n, A.offsets.data_ptr(), None, A.columns.data_ptr(),
+                                             A.values.data_ptr(), inv.data_ptr(), st))
+    blocks = np.stack([dense[3 * i:3 * i + 3, 3 * i:3 * i + 3] for i in range(n)])
+    ref_inv = np.linalg.inv(blocks)
+    got_inv = inv.cpu().numpy().astype(np.float64).reshape(n, 3, 3)
+    assert np.abs(got_inv - ref_inv).max() <= 1e-5 * np.abs(ref_inv).max()
+    g = torch.Generator(device="cuda").manual_seed(5)
+    r = torch.randn(3 * n, device="cuda", generator=g)
+    z = torch.randn(3 * n, device="cuda", generator=g)
+    w = torch.empty_like(r)
+    omega = 0.45
+    N.check(L.gb_mg_block_jacobi0(n, omega, inv.data_ptr(), r.data_ptr(), w.data_ptr(), st))
+    rr, zz = r.double().cpu().numpy(), z.double().cpu().numpy()
+    ref_w = omega * np.einsum("nij,nj->ni", got_inv, rr.reshape(n, 3)).reshape(-1)
+    assert np.abs(w.double().cpu().numpy() - ref_w).max() <= 1e-5 * np.abs(ref_w).max()
+    vals = A.values if values == "fp32" else A.values.to(torch.bfloat16)
+    dense_v = dense if values == "fp32" else _bf16_dense(A)
+    out = torch.empty_like(r)
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    N.check(L.gb_bsr_block_jacobi_smooth3(n, A.nnz_sync(), A.nnz_sync(), A.offsets.data_ptr(), A.columns.data_ptr(),
+                                          vals.data_ptr(), N.GB_F32 if values == "fp32" else N.GB_BF16, r.data_ptr(),
+                                          z.data_ptr(), inv.data_ptr(), omega, out.data_ptr(), status.data_ptr(), st))
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    res = rr - dense_v @ zz
+    ref = zz + omega * np.einsum("nij,nj->ni", got_inv, res.reshape(n, 3)).reshape(-1)
+    scale = np.abs(zz).max() + omega * np.abs(got_inv).max() * (np.abs(dense_v) @ np.abs(zz) + np.abs(rr)).max()
+    assert np.abs(out.double().cpu().numpy() - ref).max() <= 1e-5 * scale
+
+
+def _bf16_dense(A):
+    """The dense matrix of A's values rounded to bf16 (the values the bf16 kernels read)."""
+    nnz = A.nnz_sync()
+    off = A.offsets.cpu().numpy()
+    cols = A.columns[:nnz].cpu().numpy()
+    vals = A.values[:nnz].to(torch.bfloat16).double().cpu().numpy().reshape(-1, 3, 3)
+    D = np.zeros((3 * A.nrow, 3 * A.ncol))
+    for i in range(A.nrow):
+        for k in range(off[i], off[i + 1]):
+            D[3 * i:3 * i + 3, 3 * cols[k]:3 * cols[k] + 3] = vals[k]
+    return D

@@ -79,6 +79,10 @@ _SIGNATURES = {
     "gb_mg_prolong_add_c": (_c_int, [_c_int] * 7 + [_vp, _vp, ctypes.c_float, _vp, _vp]),
     "gb_mg_prolong_add": (_c_int, [_c_int] * 6 + [_vp, _vp, ctypes.c_float, _vp, _vp]),
     "gb_mg_jacobi0": (_c_int, [_c_i64, ctypes.c_float, _vp, _vp, _vp, _vp]),
+    "gb_bsr_block_inverse_diagonal3": (_c_int, [_c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "gb_mg_block_jacobi0": (_c_int, [_c_i64, ctypes.c_float, _vp, _vp, _vp, _vp]),
+    "gb_bsr_block_jacobi_smooth3": (_c_int, [_c_int, _c_i64, _c_i64, _vp, _vp, _vp, _c_int, _vp, _vp, _vp,
+                                             ctypes.c_float, _vp, _vp, _vp]),
     "gb_st27_bytes": (_c_sz, [_c_int, _c_int, _c_int]),
     "gb_st27_build": (_c_int, [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gb_st27_apply": (_c_int, [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, ctypes.c_float, _vp, _vp, _vp, _vp]),

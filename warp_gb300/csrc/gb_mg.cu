@@ -123,6 +123,19 @@ __global__ void k_jacobi0(int64_t n, float omega, const float* __restrict__ dinv
         z[i] = omega * dinv[i] * r[i];
 }
 
+// z_i = omega * Dinv_i r_i per node (3x3 blocks, 9 floats per node): the first block-Jacobi step
+__global__ void k_block_jacobi0(int64_t nodes, float omega, const float* __restrict__ dinv, const float* __restrict__ r,
+                                float* __restrict__ z)
+{
+    pdl_enter();
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nodes; i += (int64_t)gridDim.x * blockDim.x) {
+        const float* d = dinv + i * 9;
+        const float r0 = r[3 * i], r1 = r[3 * i + 1], r2 = r[3 * i + 2];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) z[3 * i + c] = omega * (d[3 * c] * r0 + d[3 * c + 1] * r1 + d[3 * c + 2] * r2);
+    }
+}
+
 // cell coefficient of coarse cell (X,Y,Z) = exp(mean log of its 2x2x2 fine cells)
 __global__ void k_coarsen_cells(int fx, int fy, int fz, const float* __restrict__ a, float* __restrict__ ac)
 {
@@ -199,6 +212,16 @@ GB_API int gb_mg_jacobi0(int64_t n, float omega, const float* dinv, const float*
 {
     if (n <= 0) return GB_OK;
     GB_CHECK_CUDA(launch_pdl(k_jacobi0, (int)std::min<int64_t>(grid1(n), kSmCount * 8), 256, 0, stream, n, omega, dinv, r, z));
+    return GB_OK;
+}
+
+GB_API int gb_mg_block_jacobi0(int64_t nodes, float omega, const float* dinv, const float* r, float* z,
+                               cudaStream_t stream)
+{
+    if (nodes <= 0) return GB_OK;
+    GB_REQUIRE(dinv && r && z && r != z, "mg_block_jacobi0: bad arguments");
+    GB_CHECK_CUDA(launch_pdl(k_block_jacobi0, (int)std::min<int64_t>(grid1(nodes), kSmCount * 8), 256, 0, stream, nodes,
+                             omega, dinv, r, z));
     return GB_OK;
 }
 

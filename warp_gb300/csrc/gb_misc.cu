@@ -61,6 +61,49 @@ __global__ void k_bsr_inverse_diag(int nrow, int bdim, const int* __restrict__ o
     }
 }
 
+// Inverse of every 3x3 diagonal block (the block-Jacobi smoother of vec3 multigrid levels), computed
+// in double by the adjugate; a missing or singular block gives the identity.  inv: 9 floats per block
+// row, row-major.
+__global__ void k_bsr_block_inverse_diag3(int nrow, const int* __restrict__ offsets, const int* __restrict__ row_counts,
+                                          const int* __restrict__ columns, const float* __restrict__ values,
+                                          float* __restrict__ inv)
+{
+    const int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= nrow) return;
+    const int beg = offsets[row];
+    const int end = row_counts ? beg + row_counts[row] : offsets[row + 1];
+    int lo = beg, hi = end - 1, found = -1;
+    while (lo <= hi) {
+        const int mid = (lo + hi) >> 1;
+        const int c = columns[mid];
+        if (c == row) {
+            found = mid;
+            break;
+        }
+        if (c < row) lo = mid + 1; else hi = mid - 1;
+    }
+    double m[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+    if (found >= 0)
+        for (int k = 0; k < 9; ++k) m[k] = (double)values[(size_t)found * 9 + k];
+    const double c00 = m[4] * m[8] - m[5] * m[7], c01 = m[5] * m[6] - m[3] * m[8], c02 = m[3] * m[7] - m[4] * m[6];
+    const double det = m[0] * c00 + m[1] * c01 + m[2] * c02;
+    float* o = inv + (size_t)row * 9;
+    if (!(det != 0.0) || !isfinite(det)) {
+        for (int k = 0; k < 9; ++k) o[k] = (k % 4 == 0) ? 1.f : 0.f;
+        return;
+    }
+    const double id = 1.0 / det;
+    o[0] = (float)(c00 * id);
+    o[1] = (float)((m[2] * m[7] - m[1] * m[8]) * id);
+    o[2] = (float)((m[1] * m[5] - m[2] * m[4]) * id);
+    o[3] = (float)(c01 * id);
+    o[4] = (float)((m[0] * m[8] - m[2] * m[6]) * id);
+    o[5] = (float)((m[2] * m[3] - m[0] * m[5]) * id);
+    o[6] = (float)(c02 * id);
+    o[7] = (float)((m[1] * m[6] - m[0] * m[7]) * id);
+    o[8] = (float)((m[0] * m[4] - m[1] * m[3]) * id);
+}
+
 template <typename T>
 __global__ void k_diag_mv(int64_t n, const T* __restrict__ A, const T* __restrict__ x, const T* y, T* z, T alpha,
                           T beta)
@@ -224,6 +267,17 @@ GB_API int gb_diag_mv(int dtype, int64_t n, const void* A, const void* x, const 
         gb::set_error("diag_mv: unsupported dtype");
         return GB_ERR_UNSUPPORTED;
     }
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+GB_API int gb_bsr_block_inverse_diagonal3(int nrow, const int* offsets, const int* row_counts, const int* columns,
+                                          const float* values, float* inv, cudaStream_t stream)
+{
+    GB_REQUIRE(nrow >= 0, "bsr_block_inverse_diagonal3: bad shape");
+    if (nrow == 0) return GB_OK;
+    GB_REQUIRE(offsets && columns && values && inv, "bsr_block_inverse_diagonal3: missing argument");
+    k_bsr_block_inverse_diag3<<<ceil_div(nrow, 128), 128, 0, stream>>>(nrow, offsets, row_counts, columns, values, inv);
     GB_CHECK_CUDA(cudaGetLastError());
     return GB_OK;
 }

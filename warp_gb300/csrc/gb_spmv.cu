@@ -51,6 +51,37 @@ template <int BR> struct EpiSmooth {
     }
 };
 
+// Block-Jacobi step on 3x3 block rows: z_out_i = z_i + omega Dinv_i (r - A z)_i, Dinv_i the inverse of the
+// row's diagonal block (9 floats, row-major); every lane of the row's group holds all 3 sums.
+struct EpiSmoothBlock3 {
+    const float *z, *r, *dinv;
+    float omega;
+    float* z_out;
+    __device__ __forceinline__ void operator()(int row, const float (&acc)[3], int lane_g)
+    {
+        if (lane_g < 3) {
+            const size_t b = (size_t)row * 3;
+            const float* d = dinv + (size_t)row * 9 + 3 * lane_g;
+            const float t0 = r[b] - acc[0], t1 = r[b + 1] - acc[1], t2 = r[b + 2] - acc[2];
+            z_out[b + lane_g] = z[b + lane_g] + omega * (d[0] * t0 + d[1] * t1 + d[2] * t2);
+        }
+    }
+};
+
+template <typename VT>
+__global__ __launch_bounds__(SPMV_THREADS) void k_bsr_block_smooth3(int nrow, SpmvShape sh,
+                                                                    const int* __restrict__ offsets,
+                                                                    const int* __restrict__ columns,
+                                                                    const VT* __restrict__ values, const float* z,
+                                                                    const float* r, const float* dinv, float omega,
+                                                                    float* z_out, int* status)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    pdl_enter();
+    EpiSmoothBlock3 epi{z, r, dinv, omega, z_out};
+    spmv_run<3, 3, VT, float, float>(nrow, sh, offsets, nullptr, columns, values, z, smem, status, epi);
+}
+
 template <int BR, typename VT>
 __global__ __launch_bounds__(SPMV_THREADS) void k_bsr_smooth(int nrow, SpmvShape sh, const int* __restrict__ offsets,
                                                              const int* __restrict__ columns,
@@ -346,6 +377,42 @@ static int launch_smooth(int nrow, int64_t nnz, int64_t ncap, const int* offsets
                              values, z, r, dinv, omega, z_out, status));
     GB_CHECK_CUDA(cudaGetLastError());
     return GB_OK;
+}
+
+template <typename VT>
+static int launch_block_smooth3(int nrow, int64_t nnz, int64_t ncap, const int* offsets, const int* columns,
+                                const VT* values, const float* r, const float* z, const float* dinv, float omega,
+                                float* z_out, int* status, int val_dtype, cudaStream_t stream)
+{
+    const bool aligned = ((uintptr_t)columns % 16 == 0) && ((uintptr_t)values % 16 == 0);
+    SpmvShape sh = default_shape(3, 3, val_dtype, nrow, nnz, ncap, aligned);
+    const size_t smem = spmv_smem_bytes<3, 3, VT>(sh.rows, sh.cap, sh.stages);
+    finalize_shape(sh, nrow, smem, offsets);
+    static size_t attr_bytes = 48 * 1024;  // raised only when a launch needs more
+    if (smem > attr_bytes) {
+        GB_CHECK_CUDA(cudaFuncSetAttribute(k_bsr_block_smooth3<VT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        attr_bytes = smem;
+    }
+    GB_CHECK_CUDA(launch_pdl(k_bsr_block_smooth3<VT>, sh.grid, SPMV_THREADS, smem, stream, nrow, sh, offsets, columns,
+                             values, z, r, dinv, omega, z_out, status));
+    GB_CHECK_CUDA(cudaGetLastError());
+    return GB_OK;
+}
+
+// z_out = z + omega Dinv (r - A z) with Dinv the inverses of A's 3x3 diagonal blocks (gb_bsr_block_inverse_diagonal3).
+GB_API int gb_bsr_block_jacobi_smooth3(int nrow, int64_t nnz, int64_t ncap, const int* offsets, const int* columns,
+                                       const void* values, int val_dtype, const float* r, const float* z,
+                                       const float* dinv_blocks, float omega, float* z_out, int* status,
+                                       cudaStream_t stream)
+{
+    GB_REQUIRE(val_dtype == GB_F32 || val_dtype == GB_BF16, "block_jacobi_smooth3: fp32 or bf16 values");
+    GB_REQUIRE(nrow > 0 && offsets && columns && values && r && z && dinv_blocks && z_out && z_out != z,
+               "block_jacobi_smooth3: bad arguments");
+    if (val_dtype == GB_F32)
+        return launch_block_smooth3<float>(nrow, nnz, ncap, offsets, columns, (const float*)values, r, z, dinv_blocks,
+                                           omega, z_out, status, val_dtype, stream);
+    return launch_block_smooth3<__nv_bfloat16>(nrow, nnz, ncap, offsets, columns, (const __nv_bfloat16*)values, r, z,
+                                               dinv_blocks, omega, z_out, status, val_dtype, stream);
 }
 
 GB_API int gb_bsr_jacobi_smooth(int bdim, int nrow, int64_t nnz, int64_t ncap, const int* offsets, const int* columns,

@@ -106,18 +106,22 @@ class MultigridPreconditioner:
             traffic, with fp32 accumulation; the flexible solver's own product keeps the fp32 matrix,
             so its tolerance and the FP64 refinement are unaffected (the cycle only has to be a good
             approximate inverse).
+        block_jacobi: 3x3 hierarchies smooth with the inverses of the node blocks (block Jacobi; damping
+            from rho(Db^-1 A)) instead of the diagonal entries: 77 -> 64 flexible-CG iterations on the 128^3
+            elasticity configuration.
 
     Vectors of a 3x3 hierarchy hold 3 interleaved components per node; masks are per node.
     """
 
     def __init__(self, Am: sparse.BsrMatrix, geo, coef, faces=("x-", "x+", "y-", "y+", "z-", "z+"), omega=None,
                  coarsest_nodes: int | None = None, max_levels: int = 12, stencil: bool = True, poisson: float = 0.3,
-                 fine_values: torch.dtype = torch.float32):
+                 fine_values: torch.dtype = torch.float32, block_jacobi: bool = True):
         if fine_values not in (torch.float32, torch.bfloat16):
             raise ValueError("fine_values: torch.float32 or torch.bfloat16")
         if Am.block_shape not in ((1, 1), (3, 3)) or Am.scalar_type != torch.float32:
             raise ValueError("multigrid preconditioner: fp32 BSR matrix with 1x1 or 3x3 blocks required")
         self.bdim = Am.block_shape[0]
+        self.block_jacobi = bool(block_jacobi) and self.bdim == 3
         if coarsest_nodes is None:
             coarsest_nodes = 2200 // self.bdim
         if self.bdim == 3 and geo.dimension != 3:
@@ -187,6 +191,13 @@ class MultigridPreconditioner:
                               fields={"u": fem.make_trial(space, bd), "v": fem.make_test(space, bd)}, assembly="nodal")
             fem.project_linear_system(cA, rhs, P)
             cur_geo, cur_A, cur_coef = cgeo, cA, ccoef
+        # 3x3 levels: inverses of the node blocks for the block-Jacobi smoother
+        for lv in levels:
+            lv.dinvb = None
+            if self.block_jacobi:
+                lv.dinvb = A.empty(lv.n * 9, torch.float32)
+                N.check(L.gb_bsr_block_inverse_diagonal3(lv.n, A.ptr(lv.A.offsets), None, A.ptr(lv.A.columns),
+                                                         A.ptr(lv.A.values), A.ptr(lv.dinvb), stream), "block_inverse")
         # damping per level
         for lv in levels:
             lv.omega = self._auto_omega(lv) if self.omega == "auto" else self.omega
@@ -247,8 +258,12 @@ class MultigridPreconditioner:
             scale = 1.0 / max(nrm, 1e-30) if it % 8 == 0 else 1.0
             N.check(L.gb_axpby(N.GB_F32, m, scale, a.data_ptr(), 0.0, a.data_ptr(), b.data_ptr(), stream), "scale")
             sparse.bsr_mv(lv.A, b, c)
-            N.check(L.gb_diag_mv(N.GB_F32, m, lv.dinv.data_ptr(), c.data_ptr(), None, a.data_ptr(), 1.0, 0.0,
-                                 stream), "dinv")
+            if lv.dinvb is not None:
+                N.check(L.gb_mg_block_jacobi0(lv.n, 1.0, lv.dinvb.data_ptr(), c.data_ptr(), a.data_ptr(), stream),
+                        "dinv")
+            else:
+                N.check(L.gb_diag_mv(N.GB_F32, m, lv.dinv.data_ptr(), c.data_ptr(), None, a.data_ptr(), 1.0, 0.0,
+                                     stream), "dinv")
             if it == iters - 1:
                 na, nb = norms(a, b)
                 rho = na / max(nb, 1e-30)
@@ -301,6 +316,9 @@ class MultigridPreconditioner:
                 self._csr_residual(lv, w, r, t, stream)
         elif lv.S is not None:
             self._st27(lv, 1, None, r, A.ptr(lv.dinv), w, t, stream)  # first Jacobi step + residual
+        elif lv.dinvb is not None:
+            N.check(L.gb_mg_block_jacobi0(lv.n, lv.omega, A.ptr(lv.dinvb), r, w, stream), "block_jacobi0")
+            self._csr_residual(lv, w, r, t, stream)
         else:
             N.check(L.gb_mg_jacobi0(lv.n * self.bdim, lv.omega, A.ptr(lv.dinv), r, w, stream), "jacobi0")
             self._csr_residual(lv, w, r, t, stream)
@@ -315,6 +333,10 @@ class MultigridPreconditioner:
         # post-smoothing fused with its residual: z = w + omega D^-1 (r - A w)
         if lv.S is not None:
             self._st27(lv, 2, w, r, A.ptr(lv.dinv), None, z, stream)  # smoothing step + residual
+        elif lv.dinvb is not None:
+            N.check(L.gb_bsr_block_jacobi_smooth3(lv.n, lv.nnz, lv.nnz, A.ptr(Am.offsets), A.ptr(Am.columns),
+                                                  A.ptr(lv.vals), lv.vals_dtype, r, w, A.ptr(lv.dinvb), lv.omega, z,
+                                                  A.ptr(self.status), stream), "block_smooth")
         else:
             N.check(L.gb_bsr_jacobi_smooth(self.bdim, lv.n, lv.nnz, lv.nnz, A.ptr(Am.offsets), A.ptr(Am.columns),
                                            A.ptr(lv.vals), lv.vals_dtype, r, w, A.ptr(lv.dinv), lv.omega, z,
