@@ -660,7 +660,9 @@ def main():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--res", type=int, nargs="+", default=[96, 96, 96])
     p.add_argument("--seed", type=int, default=0)
-    p.add_argument("--inner-tol", type=float, default=1e-5)
+    p.add_argument("--inner-tol", type=float, default=None,
+                   help="inner tolerance of every refined solve (default: the solver's own, 1e-4 for the "
+                        "flexible solves and 1e-5 for the Krylov drop-ins)")
     p.add_argument("--mv-launches", type=int, default=50)
     p.add_argument("--ref-max-iters", type=int, default=5000,
                    help="iteration bound of the reference arm's FP64 Jacobi-PCG solve")
@@ -982,7 +984,8 @@ def main():
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "solver": "learned_fcg_refined", "n_dofs": n, "nnz": nnz,
                    "parallelism": f"replicas{ws}", "l2": "inputs > L2 (matrix 204 MB vs 129 MB L2), no flush",
-                   "inner_tol": args.inner_tol, "weights": os.path.relpath(args.weights, ROOT),
+                   "inner_tol": lsolver.inner_tol, "jacobi_cg_inner_tol": jsolver.inner_tol,
+                   "weights": os.path.relpath(args.weights, ROOT),
                    "mg_levels": lmg.describe(), "vcycle_fine_values": VCYCLE_FINE,
                    "fcg_product": "27-point stencil form of A (fp32)" if lsolver.inner.stencil_product else "CSR",
                    "jacobi_cg": "persistent cooperative launch" if jsolver.inner.persistent_active else "three kernels"},
