@@ -396,6 +396,28 @@ template <int NV> __device__ __forceinline__ void consumer_sum(const float (&v)[
     }
 }
 
+// The same sum of per-thread double-float values (2 floats per warp per value in s_red).
+template <int NV> __device__ __forceinline__ void consumer_sum_df(const df32 (&v)[NV], float* s_red, df32 (&out)[NV])
+{
+    const int cw = (threadIdx.x >> 5) - 1, lane = threadIdx.x & 31;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        const df32 w = warp_sum_df(v[k]);
+        if (lane == 0) {
+            s_red[(cw * NV + k) * 2] = w.hi;
+            s_red[(cw * NV + k) * 2 + 1] = w.lo;
+        }
+    }
+    consumer_sync();
+    if (cw == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            const bool in = lane < SPMV_CONSUMER_WARPS;
+            out[k] = warp_sum_df(df32(in ? s_red[(lane * NV + k) * 2] : 0.f, in ? s_red[(lane * NV + k) * 2 + 1] : 0.f));
+        }
+    }
+}
+
 // Sum of every CTA's double-float partials part[k * gridDim.x + c] over the consumer threads (one or
 // two loads each, warp sums, then a sum of the 16 warp totals), in the same fixed order in every CTA;
 // thread 32 passes the totals to `update` (which changes the shared solver state), and the consumers
@@ -576,8 +598,12 @@ __global__ __launch_bounds__(SPMV_THREADS, 2) void k_cg_loop(const SolveArgs* __
         bool ok = true;
         while (st.cond && (max_iters <= 0 || done < max_iters)) {
             if (threadIdx.x == 32) *(volatile int*)&s_citer = done;
-            // (1) Ap = A p, p.Ap over the tiles this CTA's producer took, up to its sentinel
+            // (1) Ap = A p, p.Ap over the tiles this CTA's producer took, up to its sentinel.  Each thread's
+            // fp32 sum covers the rows one tile gives it (the same in every run, whichever CTA takes the
+            // tile); the tile sums then go into a double-float total, so the schedule changes p.Ap only at
+            // the double-float rounding level
             EpiCgAp<BR, float> epi{a.Ap, a.p};
+            df32 pap_df;
             for (;; ++i) {
                 const int s = i % NS;
                 const uint32_t ph = (uint32_t)(i / NS) & 1u;
@@ -585,6 +611,7 @@ __global__ __launch_bounds__(SPMV_THREADS, 2) void k_cg_loop(const SolveArgs* __
                 const bool tile = full_ok && R.hdr[s].nr >= 0;
                 if (tile) {
                     // the rows of the staged tile (the loop of spmv_run, with coherent gathers of p)
+                    epi.pAp = 0.f;
                     const StageHeader h = R.hdr[s];
                     const unsigned char* stg = R.ring + (size_t)s * R.stage_bytes;
                     const int* s_off = reinterpret_cast<const int*>(stg);
@@ -635,6 +662,7 @@ __global__ __launch_bounds__(SPMV_THREADS, 2) void k_cg_loop(const SolveArgs* __
                         for (int q = 0; q < BR; ++q) acc[q] = group_reduce(acc[q], G);
                         if (active) epi(h.r0 + k, acc, lane_g);
                     }
+                    pap_df += df32(epi.pAp, 0.f);
                 } else if (!full_ok && lane == 0) {
                     *(volatile int*)&s_fail = 1;
                 }
@@ -646,9 +674,9 @@ __global__ __launch_bounds__(SPMV_THREADS, 2) void k_cg_loop(const SolveArgs* __
                 }
             }
             {
-                const float v[1] = {epi.pAp};
+                const df32 v[1] = {pap_df};
                 df32 t[1];
-                consumer_sum<1>(v, s_red, t);
+                consumer_sum_df<1>(v, s_red, t);
                 if (threadIdx.x == 32) partA[blockIdx.x] = make_float2(t[0].hi, t[0].lo);
             }
             // every CTA's producer has made its last take for this iteration: its queue is zeroed for
