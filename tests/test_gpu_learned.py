@@ -279,10 +279,11 @@ def test_trained_network_gains_over_jacobi_smoothing(cuda):
     inf = learned.LearnedSmoother(net, f.mg, test.coef)
     got = np.mean([tr.eval_loss(f, r, e, inf) for r, e in pairs])
     assert got < 0.6 * base, (got, base)
-    # flexible CG with the plain and the learned V-cycle on the held-out right-hand side
+    # flexible CG with the plain and the learned V-cycle on the held-out right-hand side, both in the
+    # hierarchy and damping the network was trained in
     iters = {}
     for name, sm in (("jacobi", None), ("learned", inf)):
-        mg = multigrid.MultigridPreconditioner(test.A, test.geo, test.coef)
+        mg = multigrid.MultigridPreconditioner(test.A, test.geo, test.coef, coarsest_nodes=400, omega=net.cycle_omega)
         mg.smoother = sm if sm is None else learned.LearnedSmoother(net, mg, test.coef)
         x = torch.zeros_like(test.b)
         it, err, atol = linear.fcg(test.A, test.b, x, tol=1e-7, atol=0.0, maxiter=100, M=mg, check_every=1)

@@ -191,3 +191,18 @@ def test_breakdown_inside_the_loop_stops_it(cuda, persistent):
     assert status & N.DEV_BREAKDOWN
     assert not status & N.DEV_WAIT_TIMEOUT
     assert int(it.item()) == 1
+
+
+def test_persistent_solves_are_reproducible(cuda):
+    """Several tiles per CTA, taken from the dynamic queues in a different order each run: repeated solves
+    give the same iterate bit for bit (the schedule only reaches p.Ap at double-float rounding level)."""
+    from warp_gb300 import problems
+
+    sysm = problems.diffusion((48, 48, 48), sigma=1.5, corr_length=0.1, seed=4)
+    A, b = sysm.A, sysm.b.reshape(-1).contiguous()
+    _, x0, it0, _, _, s0 = _solve(A, b, persistent=True)
+    for _ in range(2):
+        st, x1, it1, _, _, s1 = _solve(A, b, persistent=True)
+        assert st.persistent_active and s0 == 0 and s1 == 0
+        assert it1 == it0
+        assert torch.equal(x1, x0)
