@@ -379,8 +379,12 @@ class SmootherTrainer:
         # dL/dz = -2 (r - A z) / den
         scale = (-2.0 * weight / den).to(torch.float32)
         f.gz.mul_(scale)
-        # g_w2 = gz - omega A D^-1 gz
-        torch.mul(lv0.dinv, f.gz, out=f.u)
+        # g_w2 = gz - omega A D^-1 gz (D the fine level's smoothing diagonal: the 3x3 node blocks under
+        # block Jacobi)
+        if getattr(lv0, "dinvb", None) is not None:
+            N.check(L.gb_mg_block_jacobi0(lv0.n, 1.0, A.ptr(lv0.dinvb), A.ptr(f.gz), A.ptr(f.u), stream), "dinvb")
+        else:
+            torch.mul(lv0.dinv, f.gz, out=f.u)
         f.g.copy_(f.gz)
         _spmv(lv0.A, f.u, f.g, -float(lv0.omega), 1.0, stream, st)
         # g_w = g_w2 - A P Vc R g_w2
