@@ -417,14 +417,22 @@ class SmootherTrainer:
         f.mg.smoother = saved
         return float(d[0] / d[1])
 
+    # a batch whose loss exceeds this in magnitude is degenerate (a pair whose error is nearly A-orthogonal
+    # to its residual gives a vanishing denominator, a diverging network a runaway output); its gradient
+    # is dropped instead of applied
+    MAX_BATCH_LOSS = 1e3
+
     def step(self, f: _Field, pairs) -> float:
         self.net.zero_grad()
-        tot = 0.0
         losses = []
         for r, e in pairs:
             losses.append(self.loss_and_grad(f, r, e, 1.0 / len(pairs)))
-        self.net.adam(self.lr)
         tot = float(torch.stack(losses).mean())
+        if math.isfinite(tot) and abs(tot) <= self.MAX_BATCH_LOSS:
+            self.net.adam(self.lr)
+        else:
+            self.skipped_steps = getattr(self, "skipped_steps", 0) + 1
+            self.net.zero_grad()
         return tot
 
 

@@ -87,8 +87,10 @@ def train(fields: int = 2000, res: int = 48, steps_per_field: int = 2, batch: in
         out_of_time = max_minutes is not None and time.time() - t0 > 60.0 * max_minutes
         if (k + 1) % eval_every == 0 or k + 1 == fields or out_of_time:
             got = np.mean([tr.eval_loss(held, r, e, held.sm) for r, e in held_pairs])
-            log(f"fields {k + 1}/{fields}  train loss {np.mean(hist[-eval_every:]):.5f}  held-out {got:.5f} "
-                f"(Jacobi {base:.5f})  {time.time() - t0:.0f}s")
+            kept = [h for h in hist[-eval_every:] if abs(h) <= tr.MAX_BATCH_LOSS]
+            skipped = getattr(tr, "skipped_steps", 0)
+            log(f"fields {k + 1}/{fields}  train loss {np.mean(kept) if kept else float('nan'):.5f}  held-out {got:.5f} "
+                f"(Jacobi {base:.5f})  {time.time() - t0:.0f}s" + (f"  ({skipped} degenerate batches skipped)" if skipped else ""))
             if out:
                 net.save(out, fields=k + 1, res=res, held_out_loss=got, jacobi_loss=base)
         if out_of_time:
