@@ -234,13 +234,15 @@ __device__ __forceinline__ int ld_acquire_cta(volatile int* p)
     return v;
 }
 
-// bounded wait until *seq == want (another issuer's release), or an abort
+// bounded wait until *seq == want (another issuer's release), or an abort; the clock and the abort flag
+// are read once per 32 polls, so that the hand-off is seen within a poll or two
 __device__ __forceinline__ bool tc_wait_seq(volatile int* seq, int want, volatile int* abort_flag)
 {
     if (ld_acquire_cta(seq) == want) return true;
     const uint64_t t0 = globaltimer_ns();
     for (;;) {
-        if (ld_acquire_cta(seq) == want) return true;
+        for (int k = 0; k < 32; ++k)
+            if (ld_acquire_cta(seq) == want) return true;
         if (*abort_flag) return false;
         if (globaltimer_ns() - t0 > kWaitLimitNs) return false;
     }
