@@ -154,6 +154,17 @@ def test_refined_solve_from_zero_edge_cases(cuda):
     assert info["converged"] and info["history"][0] == 1.0 and info["rel_residual"] <= 1e-8
     x2, info2 = solver.solve(s.b, x64=x.clone(), tol=1e-8)
     assert info2["converged"] and info2["outer"] == 0
+    # the x = 0 start hands b itself to the first correction solve; an explicit zero iterate goes through
+    # the product, whose residual b - A 0 rounds to the same b, so both give the same bits
+    for m in (solver, linear.RefinedSolver(s.A, method="cg", inner_tol=1e-5)):
+        xa, ia = m.solve(s.b, tol=1e-8)
+        xb, ib = m.solve(s.b, x64=torch.zeros(s.b.numel(), dtype=torch.float64, device=s.b.device), tol=1e-8)
+        assert ia["converged"] and ia["inner_iterations"] == ib["inner_iterations"]
+        # ||b|| by two reductions: fp32 products summed in fp64 here, exact products in the residual kernel
+        np.testing.assert_allclose(ia["history"], ib["history"], rtol=1e-9)
+        assert torch.equal(xa, xb)
+    with pytest.raises(ValueError, match="b.shape"):
+        solver.solve(s.b[:-1], tol=1e-8)
 
 
 @pytest.mark.parametrize("m,n", [(37, 300), (700, 2197), (5, 4096)])

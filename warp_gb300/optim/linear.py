@@ -1025,6 +1025,7 @@ class RefinedSolver:
         self._res_ws = A.zeros(int(L.gb_residual_f64_workspace_bytes(Am.block_shape[0], Am.nrow, nnz,
                                                                       A.gb_dtype(Am.values.dtype))), torch.uint8)
         self._norms = A.zeros(2, torch.float64)
+        self._dots_ws = A.zeros(int(L.gb_dots_workspace_bytes()), torch.uint8)  # arrival counter starts at 0
         self._status = A.zeros(1, torch.int32)
         self._host = torch.zeros(2, dtype=torch.float64, pin_memory=True)
         self._step_host = torch.zeros(2, dtype=torch.int32, pin_memory=True)
@@ -1068,19 +1069,27 @@ class RefinedSolver:
         b = A.as_tensor(b).reshape(-1)
         if b.dtype != torch.float32:
             raise TypeError("right-hand side must be float32 (the system's scalar type)")
+        if b.numel() != self.n:
+            raise ValueError(f"Incompatible b.shape: expected ({self.n},), got {tuple(b.shape)}")
         L = N.lib()
         history = []
         inner_iters = 0
         outer = 0
         Aop = self.inner._A
         diverged = False
+        rhs = self._r32
         if x64 is None:
-            # x = 0: the residual is b, so the first correction solve needs no host read first; the
+            # x = 0: the residual is b itself, so the first correction solve takes b as its right-hand
+            # side and needs no product and no host read first; only (b.b, b.b) is queued, and the
             # initial norms come back with the first step's
             x64 = A.zeros(self.n, torch.float64)
             self._x2.zero_()
-            self.residual(x64, b, sync=False)
+            xs = (ctypes.c_void_p * 2)(A.ptr(b), A.ptr(b))
+            N.check(L.gb_dots(N.GB_F32, self.n, 2, xs, xs, A.ptr(self._norms), A.ptr(self._dots_ws), A.stream()),
+                    "initial_norms")
+            self.kernel_launches += 1
             self._host0.copy_(self._norms, non_blocking=True)
+            rhs = b
             rnorm = bnorm = None
             guard = None
         else:
@@ -1095,7 +1104,8 @@ class RefinedSolver:
             need = 0.25 * tol * (1.0 if bnorm is None else bnorm / rnorm)
             self.inner._tol = min(max(self.inner_tol, need), 0.5)
             self._d.zero_()
-            self.inner._run_fused(Aop, self._r32, self._d, self.inner._M, x_is_zero=True)
+            self.inner._run_fused(Aop, rhs, self._d, self.inner._M, x_is_zero=True)
+            rhs = self._r32  # the residual queued below is the next step's right-hand side
             # queue x += d and the new residual behind the correction solve, and read its iteration
             # count and status together with the residual norms (one host synchronisation per step)
             self._step_host[0:1].copy_(self.inner._dev_iter.reshape(1), non_blocking=True)
