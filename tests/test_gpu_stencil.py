@@ -235,9 +235,10 @@ def test_bf16_fine_stencil_fcg_converges(cuda, learned_smoother):
 
 @pytest.mark.parametrize("learned_smoother", [False, True])
 def test_fcg_stencil_product_matches_csr_product(cuda, learned_smoother):
-    """The flexible solver's product on the fine level's stencil form (k_fcg_st27_ap) against the CSR
-    product: same iteration count within one, and the refined solve reaches 1e-8 with the FP64 residual
-    recomputed on the host."""
+    """The flexible solver's two-kernel step on the fine level's stencil form (k_fcg_st27_az: A z with
+    z.r, z.Ap_old and z.Az; k_fcg_update: p, Ap, x, r) against the four-kernel step on the CSR product:
+    same iteration count within one, and the refined solve reaches 1e-8 with the FP64 residual recomputed
+    on the host."""
     import os
 
     from warp_gb300 import learned, multigrid

@@ -849,15 +849,20 @@ __global__ __launch_bounds__(SPMV_THREADS, 2) void k_cg_loop(const SolveArgs* __
     __syncthreads();
 }
 
-// Flexible-CG product on the 27-point stencil form of A (the fine level of the multigrid carrier
-// holds it): Ap = A p with p.Ap and alpha -- the k_cg_spmv step reading 108 B of coefficients and
-// 12 B of vectors per node instead of the CSR's 8 B per nonzero.  The staging is k_st27_apply's
-// (gb_stencil.cu): per 256-node tile one bulk copy into a 2-stage ring, four CTAs per SM.
-__global__ void __launch_bounds__(ST_TILE) k_fcg_st27_ap(const SolveArgs* __restrict__ args, St27Grid g,
-                                                         const float* __restrict__ Sc)
+// Flexible-CG step on the 27-point stencil form of A (the fine level of the multigrid carrier holds
+// it), in two kernels instead of four.  With p = z + beta p_old, A p = A z + beta A p_old, so the product
+// runs on z as soon as the preconditioner has written it (Az into v) and forms z.r, z.Ap_old and z.Az in
+// the same pass; from those beta = -(z.Ap_old)/(p_old.Ap_old), p.Ap = z.Az + beta z.Ap_old (A symmetric:
+// p_old.Az = z.Ap_old) and alpha = (z.r)/(p.Ap).  k_fcg_update then forms p, Ap, x and r in one pass.  The
+// product reads 108 B of coefficients and 16 B of vectors per node (the CSR's 8 B per nonzero otherwise);
+// its staging is k_st27_apply's (gb_stencil.cu): per 256-node tile one bulk copy into a 2-stage ring,
+// four CTAs per SM.
+__global__ void __launch_bounds__(ST_TILE) k_fcg_st27_az(const SolveArgs* __restrict__ args, St27Grid g,
+                                                         const float* __restrict__ Sc, cudaGraphConditionalHandle h,
+                                                         int has_cond)
 {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ double s_red[32];
+    __shared__ double s_red[32 * 3];
     pdl_enter();
     const SolveArgs a = *args;
     KrylovScalars* S = a.S;
@@ -881,8 +886,10 @@ __global__ void __launch_bounds__(ST_TILE) k_fcg_st27_ap(const SolveArgs* __rest
             if (blockIdx.x + (int64_t)s * gridDim.x < ntiles) issue(blockIdx.x + (int64_t)s * gridDim.x, s);
     }
     __syncthreads();
+    // before the first step Ap_old holds nothing of this solve: z.Ap_old is neither formed nor used
+    const bool first = S->iter == 0;
     const int64_t yz = (int64_t)g.ny * g.nz;
-    float pAp = 0.f;
+    float zr = 0.f, zap = 0.f, zaz = 0.f;
     int it = 0;
     int64_t tile = blockIdx.x;
     for (; tile < ntiles; tile += gridDim.x, ++it) {
@@ -902,10 +909,13 @@ __global__ void __launch_bounds__(ST_TILE) k_fcg_st27_ap(const SolveArgs* __rest
             for (int k = 0; k < 27; ++k) {
                 const int dx = k / 9 - 1, dy = (k / 3) % 3 - 1, dz = k % 3 - 1;
                 if (okx[dx + 1] && oky[dy + 1] && okz[dz + 1])
-                    acc = fmaf(c[k], __ldg(a.p + i + dx * yz + (int64_t)dy * g.nz + dz), acc);
+                    acc = fmaf(c[k], __ldg(a.z + i + dx * yz + (int64_t)dy * g.nz + dz), acc);
             }
-            a.Ap[i] = acc;
-            pAp += a.p[i] * acc;
+            a.v[i] = acc;
+            const float zi = a.z[i];
+            zaz += zi * acc;
+            zr += zi * a.r[i];
+            if (!first) zap += zi * a.Ap[i];
         }
         __syncthreads();  // stage s is read: refill it
         if (threadIdx.x == 0 && tile + (int64_t)ST_STAGES * gridDim.x < ntiles)
@@ -922,18 +932,104 @@ __global__ void __launch_bounds__(ST_TILE) k_fcg_st27_ap(const SolveArgs* __rest
         }
         __syncthreads();
     }
-    float v[1] = {pAp};
-    grid_reduce_df<1>(v, a.partials, &S->counters[1], s_red, [&](const double (&t)[1]) {
-        S->pAp = t[0];
-        double alpha = 0.0;
-        if (S->rr > S->atol_sq) {
-            alpha = S->rz / t[0];
-            if (!finite(alpha)) {
+    float v[3] = {zr, zap, zaz};
+    grid_reduce_df<3>(v, a.partials, &S->counters[1], s_red, [&](const double (&t)[3]) {
+        S->rz = t[0];
+        double beta = 0.0, alpha = 0.0, pap = t[2];
+        if (!first && S->pAp != 0.0) {
+            beta = -t[1] / S->pAp;
+            pap = t[2] + beta * t[1];
+        }
+        if (!finite(t[0]) || !finite(beta) || t[0] <= 0.0) {
+            // the preconditioned residual is not a descent direction: hand over to the fallback
+            S->status |= (t[0] <= 0.0 && finite(t[0])) ? GB_DEV_STAGNATION : GB_DEV_BREAKDOWN;
+            set_cond(S, 0, h, has_cond);
+            beta = 0.0;
+        } else {
+            alpha = t[0] / pap;
+            if (!finite(alpha) || !(pap > 0.0)) {
                 S->status |= GB_DEV_BREAKDOWN;
+                set_cond(S, 0, h, has_cond);
                 alpha = 0.0;
             }
         }
+        S->beta = beta;
+        S->pAp = pap;
         S->alpha = alpha;
+    });
+}
+
+// p = z + beta p_old, Ap = Az + beta Ap_old (kept for the next step), x += alpha p, r -= alpha Ap; r.r and
+// the loop condition (with the stagnation window of k_cg_update).
+__global__ __launch_bounds__(VEC_THREADS) void k_fcg_update(const SolveArgs* __restrict__ args,
+                                                            cudaGraphConditionalHandle h, int has_cond)
+{
+    pdl_enter();
+    __shared__ double s_red[32];
+    const SolveArgs a = *args;
+    KrylovScalars* S = a.S;
+    if (!S->cond) return;
+    const float alpha = (float)S->alpha, beta = (float)S->beta;
+    const bool first = S->iter == 0;  // p_old and Ap_old are not read before the first step
+    const int64_t n = a.n;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    float rr = 0.f;
+    const bool vec4 = ((((uintptr_t)a.x | (uintptr_t)a.r | (uintptr_t)a.p | (uintptr_t)a.Ap | (uintptr_t)a.z |
+                         (uintptr_t)a.v) & 15) == 0);
+    int64_t done = 0;
+    if (vec4) {
+        const int64_t n4 = n >> 2;
+        for (int64_t i = tid; i < n4; i += stride) {
+            const float4 zv = reinterpret_cast<const float4*>(a.z)[i];
+            const float4 av = reinterpret_cast<const float4*>(a.v)[i];
+            float4 pv = zv, qv = av;
+            if (!first) {
+                const float4 po = reinterpret_cast<const float4*>(a.p)[i];
+                const float4 qo = reinterpret_cast<const float4*>(a.Ap)[i];
+                pv.x = fmaf(beta, po.x, zv.x); pv.y = fmaf(beta, po.y, zv.y);
+                pv.z = fmaf(beta, po.z, zv.z); pv.w = fmaf(beta, po.w, zv.w);
+                qv.x = fmaf(beta, qo.x, av.x); qv.y = fmaf(beta, qo.y, av.y);
+                qv.z = fmaf(beta, qo.z, av.z); qv.w = fmaf(beta, qo.w, av.w);
+            }
+            reinterpret_cast<float4*>(a.p)[i] = pv;
+            reinterpret_cast<float4*>(a.Ap)[i] = qv;
+            float4 xv = reinterpret_cast<float4*>(a.x)[i], rv = reinterpret_cast<float4*>(a.r)[i];
+            xv.x += alpha * pv.x; xv.y += alpha * pv.y; xv.z += alpha * pv.z; xv.w += alpha * pv.w;
+            rv.x -= alpha * qv.x; rv.y -= alpha * qv.y; rv.z -= alpha * qv.z; rv.w -= alpha * qv.w;
+            reinterpret_cast<float4*>(a.x)[i] = xv;
+            reinterpret_cast<float4*>(a.r)[i] = rv;
+            rr += rv.x * rv.x + rv.y * rv.y + rv.z * rv.z + rv.w * rv.w;
+        }
+        done = n4 << 2;
+    }
+    for (int64_t i = done + tid; i < n; i += stride) {
+        const float pi = first ? a.z[i] : fmaf(beta, a.p[i], a.z[i]);
+        const float qi = first ? a.v[i] : fmaf(beta, a.Ap[i], a.v[i]);
+        a.p[i] = pi;
+        a.Ap[i] = qi;
+        a.x[i] += alpha * pi;
+        const float ri = a.r[i] - alpha * qi;
+        a.r[i] = ri;
+        rr += ri * ri;
+    }
+    float v[1] = {rr};
+    grid_reduce_df<1>(v, a.partials, &S->counters[2], s_red, [&](const double (&t)[1]) {
+        S->rr = t[0];
+        S->iter += 1;
+        int cond = (t[0] > S->atol_sq) && (S->iter < S->maxiter);
+        if (!finite(t[0])) {
+            S->status |= GB_DEV_NONFINITE;
+            cond = 0;
+        }
+        if (a.stag_window > 0 && cond && (S->iter % a.stag_window) == 0) {
+            if (S->iter > a.stag_window && t[0] > a.stag_factor * a.stag_factor * S->rr_ref) {
+                S->status |= GB_DEV_STAGNATION;
+                cond = 0;
+            }
+            S->rr_ref = t[0];
+        }
+        set_cond(S, cond, h, has_cond);
     });
 }
 
@@ -1298,7 +1394,7 @@ static WsLayout ws_layout(int kind, int64_t n, int spmv_grid, int vec_grid)
     L.scalars = align256(sizeof(KrylovScalars));
     L.partials = align256(sizeof(double) * 3 * (size_t)std::max(spmv_grid, vec_grid));
     L.vec = align256(sizeof(float) * (size_t)n);
-    L.nvec = (kind == KRYLOV_CG) ? 3 : (kind == KRYLOV_FCG ? 4 : 7);  // CG: r p Ap; FCG: + z; BiCGSTAB: 7
+    L.nvec = (kind == KRYLOV_CG) ? 3 : (kind == KRYLOV_FCG ? 5 : 7);  // CG: r p Ap; FCG: + z Az; BiCGSTAB: 7
     L.total = L.args + L.scalars + L.partials + L.nvec * L.vec + 256;
     return L;
 }
@@ -1378,15 +1474,17 @@ static int launch_iter_t(Solver* s, cudaStream_t st, cudaGraphConditionalHandle 
             gb::set_error("flexible solver: preconditioner callback failed");
             return GB_ERR_INVALID;
         }
-        GB_CHECK_CUDA(launch_pdl(k_fcg_dir, s->vec_grid, VEC_THREADS, 0, st, s->d_args, h, has_cond));
-        GB_CHECK_CUDA(launch_pdl(k_fcg_p, s->vec_grid, VEC_THREADS, 0, st, s->d_args));
-        if (s->st_S)
-            GB_CHECK_CUDA(launch_pdl(k_fcg_st27_ap, s->st_grid, ST_TILE, st27_smem<float>(), st, s->d_args, s->st_g,
-                                     s->st_S));
-        else
+        if (s->st_S) {
+            GB_CHECK_CUDA(launch_pdl(k_fcg_st27_az, s->st_grid, ST_TILE, st27_smem<float>(), st, s->d_args, s->st_g,
+                                     s->st_S, h, has_cond));
+            GB_CHECK_CUDA(launch_pdl(k_fcg_update, s->vec_grid, VEC_THREADS, 0, st, s->d_args, h, has_cond));
+        } else {
+            GB_CHECK_CUDA(launch_pdl(k_fcg_dir, s->vec_grid, VEC_THREADS, 0, st, s->d_args, h, has_cond));
+            GB_CHECK_CUDA(launch_pdl(k_fcg_p, s->vec_grid, VEC_THREADS, 0, st, s->d_args));
             GB_CHECK_CUDA(launch_pdl(k_cg_spmv<BR, VT>, s->spmv_grid, SPMV_THREADS, s->spmv_smem, st, s->d_args,
                                      s->nrow, s->sh));
-        GB_CHECK_CUDA(launch_pdl(k_cg_update, s->vec_grid, VEC_THREADS, 0, st, s->d_args, h, has_cond));
+            GB_CHECK_CUDA(launch_pdl(k_cg_update, s->vec_grid, VEC_THREADS, 0, st, s->d_args, h, has_cond));
+        }
     } else if (s->kind == KRYLOV_CG && use_loop(s)) {
         return launch_loop(s, st, 1);
     } else if (s->kind == KRYLOV_CG) {
@@ -1586,7 +1684,10 @@ GB_API int gb_krylov_create(int kind, int block_dim, int nrow, int64_t nnz, int6
         s->host.r = vecs[0];
         s->host.p = vecs[1];
         s->host.Ap = vecs[2];
-        if (kind == KRYLOV_FCG) s->host.z = vecs[3];
+        if (kind == KRYLOV_FCG) {
+            s->host.z = vecs[3];
+            s->host.v = vecs[4];  // A z (the stencil-form step)
+        }
     } else {
         s->host.r = vecs[0];
         s->host.r0 = vecs[1];
@@ -1794,7 +1895,7 @@ GB_API int gb_krylov_set_stencil(void* handle, int nx, int ny, int nz, const flo
         GB_REQUIRE((uintptr_t)S % 16 == 0, "krylov_set_stencil: S must be 16-byte aligned");
         static bool attr_set = false;
         if (!attr_set) {
-            GB_CHECK_CUDA(cudaFuncSetAttribute(k_fcg_st27_ap, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            GB_CHECK_CUDA(cudaFuncSetAttribute(k_fcg_st27_az, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                               (int)st27_smem<float>()));
             attr_set = true;
         }

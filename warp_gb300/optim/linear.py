@@ -1131,7 +1131,8 @@ class RefinedSolver:
                 # argument store, init and the persistent loop (one launch per host-checked chunk)
                 self.kernel_launches += 3 if self.inner._check_every == 0 else 2 + it
             else:
-                per_it = 3 if self.method != "fcg" else 4 + getattr(self.inner._precond_obj, "kernels_per_apply", 0)
+                per_it = 3 if self.method != "fcg" else ((2 if self.inner.stencil_product else 4) +
+                                                         getattr(self.inner._precond_obj, "kernels_per_apply", 0))
                 self.kernel_launches += 2 + per_it * it  # argument store, init, kernels per iteration
             if self.method == "fcg" and status & (N.DEV_STAGNATION | N.DEV_BREAKDOWN | N.DEV_NONFINITE):
                 # the flexible solve stalled: take its correction back, recompute the residual it was
