@@ -1275,6 +1275,8 @@ __global__ __launch_bounds__(VEC_THREADS) void k_bi_pupdate(const SolveArgs* __r
 // Flexible CG (FCG(1): each direction is A-orthogonalised against the previous one only)
 //   z = M(r) (callback);  beta = -(z.Ap_prev)/(p_prev.Ap_prev);  p = z + beta p;
 //   Ap = A p, alpha = (z.r)/(p.Ap) (k_cg_spmv);  x += alpha p, r -= alpha Ap (k_cg_update).
+// These four kernels serve the CSR product; on a stencil-form operator the same step takes the two
+// kernels k_fcg_st27_az and k_fcg_update above.
 // ---------------------------------------------------------------------------------------------
 __global__ __launch_bounds__(VEC_THREADS) void k_fcg_dir(const SolveArgs* __restrict__ args,
                                                          cudaGraphConditionalHandle h, int has_cond)
